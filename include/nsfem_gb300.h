@@ -1,0 +1,156 @@
+/*
+ * nsfem_gb300.h — C ABI of the GB300 (sm_103a) per-time-step hot path of the P2-P1 Taylor-Hood
+ * Navier-Stokes solver (semi-Lagrangian advection, implicit diffusion, pressure projection).
+ *
+ * The entry points replace, one for one, the GPU device layer the reference solver calls from its
+ * assembly driver (vasil-pashov/Navier_Stokes_FEM):
+ *   GPUSimulationDeviceManager::init / getDevice   include/gpu_simulation_device.h:208-220, cpp/gpu_simulation_device.cpp:518-550
+ *   GPUSimulationDevice::uploadKDTree              cpp/gpu_simulation_device.cpp:72-77
+ *   GPUSimulationDevice::uploadMatrix              include/gpu_simulation_device.h:28, cpp/gpu_simulation_device.cpp:133-140
+ *   GPUSimulationDevice::advect                    include/gpu_simulation_device.h:29-36, cpp/gpu_simulation_device.cpp:91-131
+ *   GPUSimulationDevice::spRMult                   include/gpu_simulation_device.h:38-48, cpp/gpu_simulation_device.cpp:142-165
+ *   GPUSimulationDevice::conjugateGradient         include/gpu_simulation_device.h:62-76, cpp/gpu_simulation_device.cpp:293-515
+ *   KDTree::findElement (point location)           gpu_cpu_shared/kd_tree.cuh:40-141
+ * plus a simulation-level surface that keeps the whole operator-split step resident on the GPU, replacing the
+ * per-step host loop of NavierStokesAssembly::semiLagrangianSolve (include/assembly.h:1477-1557) together with
+ * assembleAllMatrices (include/assembly.h:1302-1475).
+ *
+ * Conventions
+ *   - Every function returns an nsf_status; 0 is success.  nsf_last_error() gives the message of the last
+ *     failure on a handle (the reference's EC::ErrorCode{status, message}, include/error_code.h:9-39).
+ *   - Pointers are HOST memory unless the name ends in _dev; calls with host pointers are synchronous.
+ *   - The library owns all device memory; callers own host arrays.  A handle may be used from several
+ *     threads (calls are serialised by an internal lock, as the reference's concurrent uploadMatrix calls
+ *     from TBB tasks require, include/assembly.h:1330,1381,1422).  One CUDA stream per handle.
+ *   - Node coordinates are float [x0,y0,x1,y1,...]; elements are int [v0,v1,v2,m12,m02,m01] per triangle,
+ *     counter-clockwise; pressure nodes are the first nPressure nodes.
+ *   - Solves stop on the RELATIVE residual ||b - A x|| <= eps * ||b|| (eps * ||r0|| when b = 0).  The
+ *     reference's GPU CG stops on the absolute ||r||^2 < eps^2 (cpp/gpu_simulation_device.cpp:405,446,511).
+ *   - A solve that does not converge still writes its last iterate and returns NSF_ERR_NOT_CONVERGED (the
+ *     reference leaves x unwritten); an initial guess that already converges is copied to x.
+ */
+#ifndef NSFEM_GB300_H
+#define NSFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nsf_device nsf_device;
+
+enum nsf_status {
+    NSF_OK = 0,
+    NSF_ERR_CUDA = 1,             /* a CUDA runtime call failed (message carries file:line) */
+    NSF_ERR_NOT_CONVERGED = 2,    /* "Max iterations reached!" (cpp/gpu_simulation_device.cpp:382,514) */
+    NSF_ERR_BREAKDOWN = 3,        /* CG breakdown: p.Ap <= 0 or a non-finite scalar (matrix not SPD, NaN input) */
+    NSF_ERR_BARRIER_TIMEOUT = 4,  /* a grid-wide wait inside a persistent kernel ran past its time limit */
+    NSF_ERR_BAD_ARG = 5,
+    NSF_ERR_STATE = 6,            /* call order violated, e.g. stepping before nsf_sim_setup */
+    NSF_ERR_NO_DEVICE = 7
+};
+
+/* Matrix slots.  0-4 are GPUSimulationDevice::SimMatrix (include/gpu_simulation_device.h:16-24); 5 and 6 hold
+ * the Dirichlet lift weights (velocityDirichletWeights / pressureDirichletWeights, include/assembly.h:363-380),
+ * stored row = free node, column = Dirichlet node. */
+enum nsf_slot {
+    NSF_PRESSURE_STIFFNESS = 0,
+    NSF_VELOCITY_MASS = 1,
+    NSF_DIFFUSION = 2,
+    NSF_VELOCITY_DIVERGENCE = 3,   /* -(1/dt) * Div, P x 2Nv */
+    NSF_PRESSURE_DIVERGENCE = 4,   /* -dt * Grad, 2Nv x P */
+    NSF_VELOCITY_LIFT = 5,
+    NSF_PRESSURE_LIFT = 6,
+    NSF_SLOT_COUNT = 7
+};
+
+/* CG variants */
+enum nsf_solver {
+    NSF_SOLVER_FP64 = 0,   /* persistent FP64 CG megakernel: the plain method */
+    NSF_SOLVER_MIXED = 1   /* FP32 matrix/vectors inside, FP64 dots and scalars, FP64 iterative refinement */
+};
+
+/* ---- device (GPUSimulationDeviceManager::init + getDevice) ------------------------------------------- */
+int nsf_create(int device, nsf_device** out);
+void nsf_destroy(nsf_device* h);
+const char* nsf_last_error(const nsf_device* h);
+int nsf_device_info(nsf_device* h, int* smCount, int* cgGridBlocks, int* cgBlockThreads);
+int nsf_synchronize(nsf_device* h);
+
+/* ---- matrices (GPUSimulationDevice::uploadMatrix; GPUSparseMatrix::upload, cpp/gpu_sparse_matrix.cpp:7-50) */
+/* CSR with rows grouped and columns ascending within a row (the order GPUSparseMatrix::upload asserts). */
+int nsf_upload_matrix_csr(nsf_device* h, int slot, int rows, int cols, int64_t nnz, const int* rowptr,
+                          const int* col, const double* val);
+/* Triplets in any order; duplicates are summed (SMM::TripletMatrix semantics). */
+int nsf_upload_matrix_triplets(nsf_device* h, int slot, int rows, int cols, int64_t count, const int* row,
+                               const int* col, const double* val);
+int nsf_matrix_shape(nsf_device* h, int slot, int* rows, int* cols, int64_t* nnz);
+int nsf_download_matrix(nsf_device* h, int slot, int* rowptr, int* col, double* val);
+
+/* ---- sparse algebra (spRMult; conjugateGradient) ----------------------------------------------------- */
+int nsf_spmv(nsf_device* h, int slot, const double* x, double* y);
+/* mode: nsf_solver.  maxIterations -1 means `rows` (cpp/gpu_simulation_device.cpp:449).  iterations and
+ * relResidual may be NULL. */
+int nsf_conjugate_gradient(nsf_device* h, int slot, const double* b, const double* x0, double* x,
+                           int maxIterations, double eps, int mode, int* iterations, double* relResidual);
+/* The reference's own float signature (include/gpu_simulation_device.h:62-76); computes in FP64. */
+int nsf_conjugate_gradient_f32(nsf_device* h, int slot, const float* b, const float* x0, float* x,
+                               int maxIterations, float eps);
+/* Device-pointer form, asynchronous on the handle's stream except for the status read-back. */
+int nsf_conjugate_gradient_dev(nsf_device* h, int slot, const double* b_dev, const double* x0_dev, double* x_dev,
+                               int maxIterations, double eps, int mode, int* iterations, double* relResidual);
+
+/* ---- mesh, point location and advection (uploadKDTree; advect; KDTree::findElement) ------------------ */
+/* Uploads the mesh and builds the point-location tree on the GPU over triangle centroids. */
+int nsf_upload_mesh(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure);
+/* Containing element of each point, with the reference's semantics: the lowest-index triangle whose closed
+ * vertex bounding box holds the point and whose barycentric test passes (bit-exact float predicate);
+ * elem = -1 and `nearest` = closest mesh node (ties -> lowest index) when no triangle contains it. */
+int nsf_locate(nsf_device* h, int n, const float* pts, int* elem, float* xi, float* eta, int* nearest);
+/* The reference's advect signature: float velocities in host memory, synchronous. */
+int nsf_advect(nsf_device* h, int numNodes, const float* u, const float* v, float dt, float* uOut, float* vOut);
+int nsf_advect_f64(nsf_device* h, int numNodes, const double* u, const double* v, double dt, double* uOut,
+                   double* vOut);
+
+/* ---- resident simulation (NavierStokesAssembly::init + assembleAllMatrices + semiLagrangianSolve) ---- */
+/* Dirichlet data are given per listed occurrence, in the mesh file's group order, with their evaluated
+ * values (FemGrid2D::VelocityDirichlet / PressureDirichlet, include/grid.h:13-60).  Assembles every matrix
+ * on the GPU and sets u = 0 with Dirichlet values imposed, p = 0. */
+int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure,
+                  int nVelocityBC, const int* velocityBCNodes, const double* bcU, const double* bcV,
+                  int nPressureBC, const int* pressureBCNodes, const double* bcP, double viscosity, double dt);
+int nsf_sim_set_fields(nsf_device* h, const double* uv, const double* p);   /* uv = [u(Nv) | v(Nv)] */
+int nsf_sim_get_fields(nsf_device* h, double* uv, double* p);
+/* Runs nsteps operator-split steps on the resident fields.  iterations (5 per step: diffusion u, diffusion v,
+ * pressure, mass u, mass v) may be NULL. */
+int nsf_sim_step(nsf_device* h, int nsteps, int* iterations);
+/* The same, from and to host fields (the reference's host-visible velocity/pressure vectors). */
+int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int nsteps, double* uvOut,
+                      double* pOut, int* iterations);
+
+/* ---- configuration, timing, pinned memory ------------------------------------------------------------ */
+int nsf_set_tolerance(nsf_device* h, double eps);
+int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);
+int nsf_set_barrier_timeout(nsf_device* h, double seconds);
+/* Records CUDA events around every persistent CG launch while enabled (clears previous records). */
+int nsf_profile(nsf_device* h, int enable);
+/* Returns the number of records written (<= maxRecords). */
+int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* rows, int64_t* nnz, int* iterations,
+                     int* outer, float* ms);
+/* op 0 records a start event on the handle's stream, op 1 a stop event and writes the elapsed ms. */
+int nsf_timer(nsf_device* h, int op, float* ms);
+int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr);
+int nsf_host_free(nsf_device* h, void* ptr);
+
+/* ---- mesh-file boundary expressions (Expression::init + evaluate, cpp/expression.cpp:308-431) ---------- */
+/* Evaluates `expression` at (x, y) in double precision.  NSF_ERR_BAD_ARG on a parse error or a variable
+ * other than x and y; the message is written to `message` (may be NULL) up to `messageBytes`. */
+int nsf_eval_expression(const char* expression, double x, double y, double* value, char* message,
+                        size_t messageBytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSFEM_GB300_H */

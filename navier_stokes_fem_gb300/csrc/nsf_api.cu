@@ -1,0 +1,752 @@
+// The C ABI (include/nsfem_gb300.h): device handle, matrix upload, solves, point location, advection and the
+// resident operator-split step.  See the header for the reference interface each entry point replaces.
+#include "nsf_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <numeric>
+#include <stdexcept>
+
+namespace nsf {
+int assemble_all(nsf_device* h, double viscosity, double dt);
+}
+
+using namespace nsf;
+
+#define NSF_BEGIN(h)                                    \
+    if (!(h)) return NSF_ERR_BAD_ARG;                   \
+    std::lock_guard<std::recursive_mutex> lk_((h)->mu); \
+    try {                                               \
+        NSF_CUDA(cudaSetDevice((h)->device));
+
+#define NSF_END(h)                                      \
+    }                                                   \
+    catch (const nsf::Error& e) {                       \
+        (h)->lastError = e.msg;                         \
+        return e.status;                                \
+    }                                                   \
+    catch (const std::exception& e) {                   \
+        (h)->lastError = e.what();                      \
+        return NSF_ERR_CUDA;                            \
+    }                                                   \
+    (h)->lastError.clear();                             \
+    return NSF_OK;
+
+namespace {
+
+DevBuf<double>& scratch(nsf_device* h, int which) { return h->scratch[which]; }
+
+void check_slot(int slot) {
+    if (slot < 0 || slot >= NSF_SLOT_COUNT) throw bad_arg("matrix slot out of range");
+}
+
+const char* status_text(int st) {
+    switch (st) {
+        case NSF_OK: return "ok";
+        case NSF_ERR_NOT_CONVERGED: return "Max iterations reached!";
+        case NSF_ERR_BREAKDOWN: return "CG breakdown (matrix not SPD or non-finite values)";
+        case NSF_ERR_BARRIER_TIMEOUT: return "grid barrier wait timed out";
+        default: return "error";
+    }
+}
+
+void ensure_workspace(nsf_device* h, int rows) {
+    CgWorkspace& ws = h->ws;
+    ws.r.ensure(rows);
+    ws.q.ensure(rows);
+    ws.p0.ensure(rows);
+    ws.p1.ensure(rows);
+    ws.r32.ensure(rows);
+    ws.d32.ensure(rows);
+    ws.q32.ensure(rows);
+    ws.p32a.ensure(rows);
+    ws.p32b.ensure(rows);
+}
+
+cudaEvent_t pool_event(nsf_device* h) {
+    if (h->evUsed == h->evPool.size()) {
+        cudaEvent_t e;
+        NSF_CUDA(cudaEventCreate(&e));
+        h->evPool.push_back(e);
+    }
+    return h->evPool[h->evUsed++];
+}
+
+// Launch one persistent solve; returns the index of its CgInfo slot.
+int launch_solve(nsf_device* h, int slot, int mode, const double* b, const double* x0, double* x, int maxIt,
+                 double tol, const CgArgs* fused) {
+    Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
+    if (A.rows != A.cols) throw bad_arg("CG needs a square matrix");
+    if (mode == NSF_SOLVER_MIXED) make_fp32_values(A, h->stream);
+    ensure_workspace(h, A.rows);
+    CgWorkspace& ws = h->ws;
+    const int infoIndex = h->infoCursor;
+    h->infoCursor = (h->infoCursor + 1) % (int)ws.info.n;
+    CgArgs a{};
+    if (fused) a = *fused;
+    a.n = A.rows;
+    a.rowptr = A.rowptr.get();
+    a.col = A.col.get();
+    a.val = A.val.get();
+    a.val32 = A.val32.get();
+    a.b = b;
+    a.x0 = x0;
+    a.x = x;
+    a.r = ws.r.get();
+    a.q = ws.q.get();
+    a.pbuf0 = ws.p0.get();
+    a.pbuf1 = ws.p1.get();
+    a.r32 = ws.r32.get();
+    a.d32 = ws.d32.get();
+    a.q32 = ws.q32.get();
+    a.p32a = ws.p32a.get();
+    a.p32b = ws.p32b.get();
+    a.partials = ws.partials.get();
+    a.sync = ws.sync.get();
+    a.info = ws.info.get() + infoIndex;
+    a.maxIt = maxIt < 0 ? A.rows : maxIt;
+    a.tol2 = tol * tol;
+    a.innerTol2 = h->innerTol * h->innerTol;
+    a.maxOuter = 64;
+    a.timeoutNs = h->timeoutNs;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h->profile) {
+        e0 = pool_event(h);
+        e1 = pool_event(h);
+        NSF_CUDA(cudaEventRecord(e0, h->stream));
+    }
+    cg_launch(ws, a, mode, h->stream);
+    if (h->profile) {
+        NSF_CUDA(cudaEventRecord(e1, h->stream));
+        h->records.push_back({slot, mode, A.rows, A.nnz, e0, e1, infoIndex});
+    }
+    return infoIndex;
+}
+
+CgInfo read_info(nsf_device* h, int index) {
+    CgInfo info;
+    NSF_CUDA(cudaMemcpyAsync(&info, h->ws.info.get() + index, sizeof(CgInfo), cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    return info;
+}
+
+void throw_solve_status(const CgInfo& info, const std::string& what) {
+    if (info.status != NSF_OK)
+        throw Error{info.status, what + ": " + status_text(info.status) + " after " + std::to_string(info.iterations) +
+                                     " iterations"};
+}
+
+void upload_csr(nsf_device* h, int slot, int rows, int cols, int64_t nnz, const int* rowptr, const int* col,
+                const double* val) {
+    check_slot(slot);
+    if (rows <= 0 || cols <= 0 || nnz < 0) throw bad_arg("matrix dimensions must be positive");
+    if (nnz > INT32_MAX) throw bad_arg("matrix has more than 2^31-1 non-zeros");
+    if (rowptr[0] != 0 || rowptr[rows] != nnz) throw bad_arg("row pointers do not span [0, nnz]");
+    for (int r = 0; r < rows; ++r) {
+        if (rowptr[r + 1] < rowptr[r]) throw bad_arg("row pointers decrease");
+        for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            if (col[k] < 0 || col[k] >= cols) throw bad_arg("column index out of range");
+            if (k > rowptr[r] && col[k] <= col[k - 1]) throw bad_arg("columns must ascend within a row");
+        }
+    }
+    Csr& A = h->mats[slot];
+    A.rows = rows;
+    A.cols = cols;
+    A.nnz = nnz;
+    A.rowptr.upload(rowptr, rows + 1, h->stream);
+    A.col.upload(col, std::max<int64_t>(nnz, 0), h->stream);
+    A.val.upload(val, std::max<int64_t>(nnz, 0), h->stream);
+    A.has32 = false;
+    A.val32.release();
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+void sim_require(nsf_device* h) {
+    if (!h->sim.ready) throw Error{NSF_ERR_STATE, "nsf_sim_setup has not been called"};
+}
+
+// Launches one operator-split step on the resident fields; `infos` receives 5 info indices.
+void sim_step_launch(nsf_device* h, int infos[5]) {
+    SimState& S = h->sim;
+    MeshDev& m = h->mesh;
+    const int Nv = m.nNodes;
+    const int mode = h->solverMode;
+    cudaStream_t s = h->stream;
+    double* uv = S.uv.get();
+    double* tmp = S.tmp.get();
+    // advection (include/assembly.h:1519-1524)
+    advect_launch(m, S.dt, uv, uv + Nv, tmp, tmp + Nv, s);
+    // diffusion solves, u then v (include/assembly.h:1529-1545, 489-558): rhs = M u_adv - lift, g on Dirichlet rows
+    for (int ch = 0; ch < 2; ++ch) {
+        CgArgs f{};
+        const Csr& M = h->mats[NSF_VELOCITY_MASS];
+        f.bRowptr = M.rowptr.get();
+        f.bCol = M.col.get();
+        f.bVal = M.val.get();
+        f.bX = tmp + (size_t)ch * Nv;
+        f.lift = S.liftV[ch].get();
+        f.bcMask = S.bcV.get();
+        f.bcValue = S.gV[ch].get();
+        f.bOut = S.rhsV.get() + (size_t)ch * Nv;
+        infos[ch] = launch_solve(h, NSF_DIFFUSION, mode, f.bOut, tmp + (size_t)ch * Nv, uv + (size_t)ch * Nv, -1,
+                                 h->tol, &f);
+    }
+    // pressure projection (include/assembly.h:560-712): rhs_p = -(1/dt) Div u - lift, pinned nodes -> g
+    {
+        CgArgs f{};
+        const Csr& Bd = h->mats[NSF_VELOCITY_DIVERGENCE];
+        f.bRowptr = Bd.rowptr.get();
+        f.bCol = Bd.col.get();
+        f.bVal = Bd.val.get();
+        f.bX = uv;
+        f.lift = S.liftP.get();
+        f.bcMask = S.bcP.get();
+        f.bcValue = S.gP.get();
+        f.bOut = S.rhsP.get();
+        infos[2] = launch_solve(h, NSF_PRESSURE_STIFFNESS, mode, f.bOut, S.p.get(), S.p.get(), -1, h->tol, &f);
+    }
+    // velocity correction: M du = -dt Grad p per component with x0 = u, then u_out = du + u, Dirichlet re-imposed
+    spmv_launch(h->mats[NSF_PRESSURE_DIVERGENCE], S.p.get(), S.rhsV.get(), s);
+    for (int ch = 0; ch < 2; ++ch)
+        infos[3 + ch] = launch_solve(h, NSF_VELOCITY_MASS, mode, S.rhsV.get() + (size_t)ch * Nv,
+                                     uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, -1, h->tol, nullptr);
+    for (int ch = 0; ch < 2; ++ch)
+        axpy_bc_launch(Nv, uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, S.bcV.get(), S.gV[ch].get(), s);
+    std::swap(S.uv, S.tmp);
+}
+
+void run_steps(nsf_device* h, int nsteps, int* iterations) {
+    sim_require(h);
+    if (nsteps < 0) throw bad_arg("nsteps must be >= 0");
+    const int chunk = std::max(1, (int)(h->ws.info.n / 5) - 1);
+    int done = 0;
+    std::vector<int> idx;
+    while (done < nsteps) {
+        const int n = std::min(chunk, nsteps - done);
+        idx.assign((size_t)5 * n, 0);
+        for (int k = 0; k < n; ++k) sim_step_launch(h, &idx[(size_t)5 * k]);
+        std::vector<CgInfo> all(h->ws.info.n);
+        NSF_CUDA(cudaMemcpyAsync(all.data(), h->ws.info.get(), sizeof(CgInfo) * all.size(), cudaMemcpyDeviceToHost,
+                                 h->stream));
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        static const char* names[5] = {"diffusion u", "diffusion v", "pressure", "mass u", "mass v"};
+        for (int k = 0; k < n; ++k)
+            for (int j = 0; j < 5; ++j) {
+                const CgInfo& info = all[idx[(size_t)5 * k + j]];
+                if (iterations) iterations[(size_t)5 * (done + k) + j] = info.iterations;
+                if (info.status != NSF_OK)
+                    throw Error{info.status, "step " + std::to_string(done + k + 1) + ", " + names[j] + " solve: " +
+                                                 status_text(info.status) + " after " +
+                                                 std::to_string(info.iterations) + " iterations"};
+            }
+        done += n;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsf_create(int device, nsf_device** out) {
+    if (!out) return NSF_ERR_BAD_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return NSF_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return NSF_ERR_BAD_ARG;
+    nsf_device* h = new nsf_device();
+    h->device = device;
+    try {
+        NSF_CUDA(cudaSetDevice(device));
+        NSF_CUDA(cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, device));
+        NSF_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        cg_configure(h->ws, device);
+    } catch (const Error& e) {
+        fprintf(stderr, "nsf_create: %s\n", e.msg.c_str());
+        delete h;
+        return e.status;
+    }
+    *out = h;
+    return NSF_OK;
+}
+
+void nsf_destroy(nsf_device* h) {
+    if (!h) return;
+    {
+        std::lock_guard<std::recursive_mutex> lk(h->mu);
+        cudaSetDevice(h->device);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        for (auto e : h->evPool) cudaEventDestroy(e);
+        for (int i = 0; i < NSF_SLOT_COUNT; ++i) h->mats[i] = Csr();
+        for (int i = 0; i < 4; ++i) scratch(h, i).release();
+        if (h->stream) cudaStreamDestroy(h->stream);
+    }
+    delete h;
+}
+
+const char* nsf_last_error(const nsf_device* h) { return h ? h->lastError.c_str() : "null handle"; }
+
+int nsf_device_info(nsf_device* h, int* smCount, int* cgGridBlocks, int* cgBlockThreads) {
+    NSF_BEGIN(h)
+    if (smCount) *smCount = h->smCount;
+    if (cgGridBlocks) *cgGridBlocks = h->ws.grid;
+    if (cgBlockThreads) *cgBlockThreads = h->ws.block;
+    NSF_END(h)
+}
+
+int nsf_synchronize(nsf_device* h) {
+    NSF_BEGIN(h)
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_upload_matrix_csr(nsf_device* h, int slot, int rows, int cols, int64_t nnz, const int* rowptr,
+                          const int* col, const double* val) {
+    NSF_BEGIN(h)
+    if (!rowptr || (nnz > 0 && (!col || !val))) throw bad_arg("null array");
+    upload_csr(h, slot, rows, cols, nnz, rowptr, col, val);
+    NSF_END(h)
+}
+
+int nsf_upload_matrix_triplets(nsf_device* h, int slot, int rows, int cols, int64_t count, const int* row,
+                               const int* col, const double* val) {
+    NSF_BEGIN(h)
+    if (count < 0 || (count > 0 && (!row || !col || !val))) throw bad_arg("null array");
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    for (int64_t k = 0; k < count; ++k)
+        if (row[k] < 0 || row[k] >= rows || col[k] < 0 || col[k] >= cols) throw bad_arg("triplet index out of range");
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        return row[a] != row[b] ? row[a] < row[b] : col[a] < col[b];
+    });
+    std::vector<int> rp(rows + 1, 0), c;
+    std::vector<double> v;
+    for (int64_t k = 0; k < count; ++k) {
+        const int64_t i = order[k];
+        if (!c.empty() && k > 0 && row[order[k - 1]] == row[i] && col[order[k - 1]] == col[i]) {
+            v.back() += val[i];
+        } else {
+            c.push_back(col[i]);
+            v.push_back(val[i]);
+            rp[row[i] + 1]++;
+        }
+    }
+    for (int r = 0; r < rows; ++r) rp[r + 1] += rp[r];
+    upload_csr(h, slot, rows, cols, (int64_t)c.size(), rp.data(), c.data(), v.data());
+    NSF_END(h)
+}
+
+int nsf_matrix_shape(nsf_device* h, int slot, int* rows, int* cols, int64_t* nnz) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    const Csr& A = h->mats[slot];
+    if (rows) *rows = A.rows;
+    if (cols) *cols = A.cols;
+    if (nnz) *nnz = A.nnz;
+    NSF_END(h)
+}
+
+int nsf_download_matrix(nsf_device* h, int slot, int* rowptr, int* col, double* val) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot is empty"};
+    if (rowptr) NSF_CUDA(cudaMemcpyAsync(rowptr, A.rowptr.get(), sizeof(int) * (A.rows + 1), cudaMemcpyDeviceToHost, h->stream));
+    if (col && A.nnz) NSF_CUDA(cudaMemcpyAsync(col, A.col.get(), sizeof(int) * A.nnz, cudaMemcpyDeviceToHost, h->stream));
+    if (val && A.nnz) NSF_CUDA(cudaMemcpyAsync(val, A.val.get(), sizeof(double) * A.nnz, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_spmv(nsf_device* h, int slot, const double* x, double* y) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot is empty"};
+    if (!x || !y) throw bad_arg("null vector");
+    DevBuf<double>& dx = scratch(h, 0);
+    DevBuf<double>& dy = scratch(h, 1);
+    dx.upload(x, A.cols, h->stream);
+    dy.ensure(A.rows);
+    spmv_launch(A, dx.get(), dy.get(), h->stream);
+    NSF_CUDA(cudaMemcpyAsync(y, dy.get(), sizeof(double) * A.rows, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_conjugate_gradient_dev(nsf_device* h, int slot, const double* b_dev, const double* x0_dev, double* x_dev,
+                               int maxIterations, double eps, int mode, int* iterations, double* relResidual) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    if (!b_dev || !x0_dev || !x_dev) throw bad_arg("null vector");
+    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (!(eps > 0)) throw bad_arg("eps must be positive");
+    const int idx = launch_solve(h, slot, mode, b_dev, x0_dev, x_dev, maxIterations, eps, nullptr);
+    const CgInfo info = read_info(h, idx);
+    if (iterations) *iterations = info.iterations;
+    if (relResidual) *relResidual = info.bb > 0 ? std::sqrt(info.rr / info.bb) : 0.0;
+    throw_solve_status(info, "conjugate gradient");
+    NSF_END(h)
+}
+
+int nsf_conjugate_gradient(nsf_device* h, int slot, const double* b, const double* x0, double* x, int maxIterations,
+                           double eps, int mode, int* iterations, double* relResidual) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot is empty"};
+    if (!b || !x0 || !x) throw bad_arg("null vector");
+    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (!(eps > 0)) throw bad_arg("eps must be positive");
+    DevBuf<double>& db = scratch(h, 0);
+    DevBuf<double>& dx0 = scratch(h, 1);
+    DevBuf<double>& dx = scratch(h, 2);
+    db.upload(b, A.rows, h->stream);
+    dx0.upload(x0, A.rows, h->stream);
+    dx.ensure(A.rows);
+    const int idx = launch_solve(h, slot, mode, db.get(), dx0.get(), dx.get(), maxIterations, eps, nullptr);
+    NSF_CUDA(cudaMemcpyAsync(x, dx.get(), sizeof(double) * A.rows, cudaMemcpyDeviceToHost, h->stream));
+    const CgInfo info = read_info(h, idx);
+    if (iterations) *iterations = info.iterations;
+    if (relResidual) *relResidual = info.bb > 0 ? std::sqrt(info.rr / info.bb) : 0.0;
+    throw_solve_status(info, "conjugate gradient");
+    NSF_END(h)
+}
+
+int nsf_conjugate_gradient_f32(nsf_device* h, int slot, const float* b, const float* x0, float* x, int maxIterations,
+                               float eps) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot is empty"};
+    if (!b || !x0 || !x) throw bad_arg("null vector");
+    std::vector<double> bd(b, b + A.rows), xd0(x0, x0 + A.rows), xd(A.rows);
+    int st = nsf_conjugate_gradient(h, slot, bd.data(), xd0.data(), xd.data(), maxIterations, eps, NSF_SOLVER_FP64,
+                                    nullptr, nullptr);
+    for (int i = 0; i < A.rows; ++i) x[i] = (float)xd[i];
+    if (st != NSF_OK) throw Error{st, h->lastError};
+    NSF_END(h)
+}
+
+int nsf_upload_mesh(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure) {
+    NSF_BEGIN(h)
+    if (nNodes <= 0 || nElements <= 0 || !xy || !elements) throw bad_arg("empty mesh");
+    if (nPressure <= 0 || nPressure > nNodes) throw bad_arg("pressure node count out of range");
+    for (int64_t k = 0; k < (int64_t)6 * nElements; ++k)
+        if (elements[k] < 0 || elements[k] >= nNodes) throw bad_arg("element references a node out of range");
+    for (int64_t k = 0; k < (int64_t)2 * nNodes; ++k)
+        if (!std::isfinite(xy[k])) throw bad_arg("non-finite node coordinate");
+    MeshDev& m = h->mesh;
+    m.nNodes = nNodes;
+    m.nEl = nElements;
+    m.nP = nPressure;
+    m.hxy.assign(xy, xy + 2 * (size_t)nNodes);
+    m.hel.assign(elements, elements + 6 * (size_t)nElements);
+    m.xy.upload((const float2*)xy, nNodes, h->stream);
+    m.el.upload(elements, 6 * (size_t)nElements, h->stream);
+    tree_build(m, h->stream);
+    h->sim.ready = false;
+    NSF_END(h)
+}
+
+int nsf_locate(nsf_device* h, int n, const float* pts, int* elem, float* xi, float* eta, int* nearest) {
+    NSF_BEGIN(h)
+    if (h->mesh.nEl == 0) throw Error{NSF_ERR_STATE, "no mesh uploaded"};
+    if (n < 0 || (n > 0 && (!pts || !elem || !xi || !eta || !nearest))) throw bad_arg("null array");
+    if (n == 0) return NSF_OK;
+    DevBuf<float2> dp;
+    DevBuf<int> de, dn;
+    DevBuf<float> dxi, deta;
+    dp.upload((const float2*)pts, n, h->stream);
+    de.alloc(n);
+    dn.alloc(n);
+    dxi.alloc(n);
+    deta.alloc(n);
+    locate_launch(h->mesh, n, dp.get(), de.get(), dxi.get(), deta.get(), dn.get(), h->stream);
+    NSF_CUDA(cudaMemcpyAsync(elem, de.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(nearest, dn.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(xi, dxi.get(), sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(eta, deta.get(), sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_advect(nsf_device* h, int numNodes, const float* u, const float* v, float dt, float* uOut, float* vOut) {
+    NSF_BEGIN(h)
+    if (h->mesh.nEl == 0) throw Error{NSF_ERR_STATE, "no mesh uploaded"};
+    if (numNodes != h->mesh.nNodes) throw bad_arg("numNodes differs from the mesh's node count");
+    if (!u || !v || !uOut || !vOut) throw bad_arg("null vector");
+    DevBuf<float> a, b, c, d;
+    a.upload(u, numNodes, h->stream);
+    b.upload(v, numNodes, h->stream);
+    c.alloc(numNodes);
+    d.alloc(numNodes);
+    advect_f32_launch(h->mesh, dt, a.get(), b.get(), c.get(), d.get(), h->stream);
+    NSF_CUDA(cudaMemcpyAsync(uOut, c.get(), sizeof(float) * numNodes, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(vOut, d.get(), sizeof(float) * numNodes, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_advect_f64(nsf_device* h, int numNodes, const double* u, const double* v, double dt, double* uOut,
+                   double* vOut) {
+    NSF_BEGIN(h)
+    if (h->mesh.nEl == 0) throw Error{NSF_ERR_STATE, "no mesh uploaded"};
+    if (numNodes != h->mesh.nNodes) throw bad_arg("numNodes differs from the mesh's node count");
+    if (!u || !v || !uOut || !vOut) throw bad_arg("null vector");
+    DevBuf<double>& a = scratch(h, 0);
+    DevBuf<double>& c = scratch(h, 1);
+    a.ensure(2 * (size_t)numNodes);
+    c.ensure(2 * (size_t)numNodes);
+    NSF_CUDA(cudaMemcpyAsync(a.get(), u, sizeof(double) * numNodes, cudaMemcpyHostToDevice, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(a.get() + numNodes, v, sizeof(double) * numNodes, cudaMemcpyHostToDevice, h->stream));
+    advect_launch(h->mesh, dt, a.get(), a.get() + numNodes, c.get(), c.get() + numNodes, h->stream);
+    NSF_CUDA(cudaMemcpyAsync(uOut, c.get(), sizeof(double) * numNodes, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(vOut, c.get() + numNodes, sizeof(double) * numNodes, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure,
+                  int nVelocityBC, const int* velocityBCNodes, const double* bcU, const double* bcV, int nPressureBC,
+                  const int* pressureBCNodes, const double* bcP, double viscosity, double dt) {
+    NSF_BEGIN(h)
+    if (!(dt > 0) || !(viscosity >= 0)) throw bad_arg("dt must be positive and viscosity non-negative");
+    if (nVelocityBC < 0 || nPressureBC < 0) throw bad_arg("negative boundary count");
+    if ((nVelocityBC > 0 && (!velocityBCNodes || !bcU || !bcV)) || (nPressureBC > 0 && (!pressureBCNodes || !bcP)))
+        throw bad_arg("null boundary array");
+    int st = nsf_upload_mesh(h, nNodes, xy, nElements, elements, nPressure);
+    if (st != NSF_OK) throw Error{st, h->lastError};
+    SimState& S = h->sim;
+    S.ready = false;
+    S.viscosity = viscosity;
+    S.dt = dt;
+    const int Nv = nNodes, P = nPressure;
+    cudaStream_t s = h->stream;
+    // Dirichlet data: mask, imposed value (last listed occurrence) and lift weight (sum over occurrences,
+    // because the reference subtracts the lift once per listed occurrence, include/assembly.h:505-523)
+    S.hbcV.assign(Nv, 0);
+    S.hbcP.assign(P, 0);
+    std::vector<double> gset[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
+    std::vector<double> glift[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
+    std::vector<double> gsetP(P, 0.0), gliftP(P, 0.0);
+    for (int k = 0; k < nVelocityBC; ++k) {
+        const int nd = velocityBCNodes[k];
+        if (nd < 0 || nd >= Nv) throw bad_arg("velocity Dirichlet node out of range");
+        S.hbcV[nd] = 1;
+        gset[0][nd] = bcU[k];
+        gset[1][nd] = bcV[k];
+        glift[0][nd] += bcU[k];
+        glift[1][nd] += bcV[k];
+    }
+    for (int k = 0; k < nPressureBC; ++k) {
+        const int nd = pressureBCNodes[k];
+        if (nd < 0 || nd >= P) throw bad_arg("pressure Dirichlet node out of range");
+        S.hbcP[nd] = 1;
+        gsetP[nd] = bcP[k];
+        gliftP[nd] += bcP[k];
+    }
+    S.bcV.upload(S.hbcV.data(), Nv, s);
+    S.bcP.upload(S.hbcP.data(), P, s);
+    for (int ch = 0; ch < 2; ++ch) {
+        S.hgV[ch] = gset[ch];
+        S.gV[ch].upload(gset[ch].data(), Nv, s);
+    }
+    S.hgP = gsetP;
+    S.gP.upload(gsetP.data(), P, s);
+    S.nColours = assemble_all(h, viscosity, dt);
+    // constant lift vectors: lift = W g (the Dirichlet data do not depend on time: the expressions see x, y only)
+    DevBuf<double> g;
+    for (int ch = 0; ch < 2; ++ch) {
+        g.upload(glift[ch].data(), Nv, s);
+        S.liftV[ch].alloc(Nv);
+        spmv_launch(h->mats[NSF_VELOCITY_LIFT], g.get(), S.liftV[ch].get(), s);
+        NSF_CUDA(cudaStreamSynchronize(s));
+    }
+    g.upload(gliftP.data(), P, s);
+    S.liftP.alloc(P);
+    spmv_launch(h->mats[NSF_PRESSURE_LIFT], g.get(), S.liftP.get(), s);
+    NSF_CUDA(cudaStreamSynchronize(s));
+    // fields: u = 0 with Dirichlet values (imposeVelocityDirichlet), p = 0
+    std::vector<double> uv0(2 * (size_t)Nv, 0.0);
+    for (int k = 0; k < nVelocityBC; ++k) {
+        uv0[velocityBCNodes[k]] = bcU[k];
+        uv0[velocityBCNodes[k] + (size_t)Nv] = bcV[k];
+    }
+    S.uv.upload(uv0.data(), uv0.size(), s);
+    S.tmp.alloc(2 * (size_t)Nv);
+    S.tmp.zero(s);
+    S.rhsV.alloc(2 * (size_t)Nv);
+    S.rhsP.alloc(P);
+    S.p.alloc(P);
+    S.p.zero(s);
+    ensure_workspace(h, std::max(Nv, P));
+    if (h->solverMode == NSF_SOLVER_MIXED)
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], s);
+    NSF_CUDA(cudaStreamSynchronize(s));
+    S.ready = true;
+    NSF_END(h)
+}
+
+int nsf_sim_set_fields(nsf_device* h, const double* uv, const double* p) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    if (!uv || !p) throw bad_arg("null field");
+    const int Nv = h->mesh.nNodes, P = h->mesh.nP;
+    NSF_CUDA(cudaMemcpyAsync(h->sim.uv.get(), uv, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(h->sim.p.get(), p, sizeof(double) * P, cudaMemcpyHostToDevice, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_sim_get_fields(nsf_device* h, double* uv, double* p) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    const int Nv = h->mesh.nNodes, P = h->mesh.nP;
+    if (uv) NSF_CUDA(cudaMemcpyAsync(uv, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost, h->stream));
+    if (p) NSF_CUDA(cudaMemcpyAsync(p, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_sim_step(nsf_device* h, int nsteps, int* iterations) {
+    NSF_BEGIN(h)
+    run_steps(h, nsteps, iterations);
+    NSF_END(h)
+}
+
+int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int nsteps, double* uvOut, double* pOut,
+                      int* iterations) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    const int Nv = h->mesh.nNodes, P = h->mesh.nP;
+    if (uvIn) NSF_CUDA(cudaMemcpyAsync(h->sim.uv.get(), uvIn, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice, h->stream));
+    if (pIn) NSF_CUDA(cudaMemcpyAsync(h->sim.p.get(), pIn, sizeof(double) * P, cudaMemcpyHostToDevice, h->stream));
+    run_steps(h, nsteps, iterations);
+    if (uvOut) NSF_CUDA(cudaMemcpyAsync(uvOut, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost, h->stream));
+    if (pOut) NSF_CUDA(cudaMemcpyAsync(pOut, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_set_tolerance(nsf_device* h, double eps) {
+    NSF_BEGIN(h)
+    if (!(eps > 0)) throw bad_arg("tolerance must be positive");
+    h->tol = eps;
+    NSF_END(h)
+}
+
+int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
+    NSF_BEGIN(h)
+    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (innerTolerance > 0) h->innerTol = innerTolerance;
+    h->solverMode = mode;
+    if (mode == NSF_SOLVER_MIXED && h->sim.ready) {
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], h->stream);
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    NSF_END(h)
+}
+
+int nsf_set_barrier_timeout(nsf_device* h, double seconds) {
+    NSF_BEGIN(h)
+    if (!(seconds >= 0)) throw bad_arg("timeout must be >= 0");
+    h->timeoutNs = (long long)(seconds * 1e9);
+    NSF_END(h)
+}
+
+int nsf_profile(nsf_device* h, int enable) {
+    NSF_BEGIN(h)
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    h->records.clear();
+    h->evUsed = 0;
+    h->profile = enable != 0;
+    NSF_END(h)
+}
+
+int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* rows, int64_t* nnz, int* iterations,
+                     int* outer, float* ms) {
+    if (!h) return -NSF_ERR_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    try {
+        NSF_CUDA(cudaSetDevice(h->device));
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        std::vector<CgInfo> all(h->ws.info.n);
+        NSF_CUDA(cudaMemcpy(all.data(), h->ws.info.get(), sizeof(CgInfo) * all.size(), cudaMemcpyDeviceToHost));
+        const int n = std::min<int>(maxRecords, (int)h->records.size());
+        for (int i = 0; i < n; ++i) {
+            const auto& r = h->records[i];
+            float t = 0;
+            NSF_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+            if (slot) slot[i] = r.slot;
+            if (mode) mode[i] = r.mode;
+            if (rows) rows[i] = r.rows;
+            if (nnz) nnz[i] = r.nnz;
+            if (iterations) iterations[i] = all[r.infoIndex].iterations;
+            if (outer) outer[i] = all[r.infoIndex].outer;
+            if (ms) ms[i] = t;
+        }
+        return n;
+    } catch (const Error& e) {
+        h->lastError = e.msg;
+        return -e.status;
+    }
+}
+
+int nsf_timer(nsf_device* h, int op, float* ms) {
+    NSF_BEGIN(h)
+    static thread_local cudaEvent_t start = nullptr, stop = nullptr;
+    if (!start) {
+        NSF_CUDA(cudaEventCreate(&start));
+        NSF_CUDA(cudaEventCreate(&stop));
+    }
+    if (op == 0) {
+        NSF_CUDA(cudaEventRecord(start, h->stream));
+    } else {
+        NSF_CUDA(cudaEventRecord(stop, h->stream));
+        NSF_CUDA(cudaEventSynchronize(stop));
+        float t = 0;
+        NSF_CUDA(cudaEventElapsedTime(&t, start, stop));
+        if (ms) *ms = t;
+    }
+    NSF_END(h)
+}
+
+int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr) {
+    NSF_BEGIN(h)
+    if (!ptr) throw bad_arg("null output pointer");
+    NSF_CUDA(cudaMallocHost(ptr, bytes));
+    NSF_END(h)
+}
+
+int nsf_host_free(nsf_device* h, void* ptr) {
+    NSF_BEGIN(h)
+    if (ptr) NSF_CUDA(cudaFreeHost(ptr));
+    NSF_END(h)
+}
+
+}  // extern "C"
+
+#include "host/expression.h"
+
+extern "C" int nsf_eval_expression(const char* expression, double x, double y, double* value, char* message,
+                                   size_t messageBytes) {
+    try {
+        if (!expression || !value) throw std::runtime_error("null argument");
+        const nsfhost::Expression e(expression);
+        *value = e.evaluate({{'x', x}, {'y', y}});
+        if (message && messageBytes) message[0] = '\0';
+        return NSF_OK;
+    } catch (const std::exception& err) {
+        if (message && messageBytes) {
+            strncpy(message, err.what(), messageBytes - 1);
+            message[messageBytes - 1] = '\0';
+        }
+        return NSF_ERR_BAD_ARG;
+    }
+}

@@ -1,0 +1,222 @@
+// Internal declarations shared by the GB300 solver's translation units.  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdarg>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/nsfem_gb300.h"
+
+namespace nsf {
+
+// ------------------------------------------------------------------------------------------------
+// error handling: every entry point returns an nsf_status and leaves a message on the handle
+// ------------------------------------------------------------------------------------------------
+struct Error {
+    int status;
+    std::string msg;
+};
+
+#define NSF_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            throw ::nsf::Error{NSF_ERR_CUDA, std::string(#call) + " failed: " + cudaGetErrorString(e_) + \
+                                                 " (" + __FILE__ + ":" + std::to_string(__LINE__) + ")"}; \
+    } while (0)
+
+inline Error bad_arg(const std::string& m) { return Error{NSF_ERR_BAD_ARG, m}; }
+
+// ------------------------------------------------------------------------------------------------
+// device memory owned by a handle
+// ------------------------------------------------------------------------------------------------
+template <typename T> struct DevBuf {
+    T* ptr = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : ptr(o.ptr), n(o.n) { o.ptr = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); ptr = o.ptr; n = o.n; o.ptr = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && ptr) return;
+        release();
+        if (count) NSF_CUDA(cudaMalloc((void**)&ptr, count * sizeof(T)));
+        n = count;
+    }
+    void ensure(size_t count) { if (count > n) alloc(count); }
+    void upload(const T* host, size_t count, cudaStream_t s) {
+        alloc(count);
+        if (count) NSF_CUDA(cudaMemcpyAsync(ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void zero(cudaStream_t s) { if (n) NSF_CUDA(cudaMemsetAsync(ptr, 0, n * sizeof(T), s)); }
+    T* get() const { return ptr; }
+};
+
+// CSR matrix resident on the device.  Row pointers and column indices are int32 (nnz < 2^31 is checked at
+// upload); FP64 values are always present, FP32 values are made on demand for the mixed-precision solver.
+struct Csr {
+    int rows = 0, cols = 0;
+    int64_t nnz = 0;
+    DevBuf<int> rowptr, col;
+    DevBuf<double> val;
+    DevBuf<float> val32;
+    bool has32 = false;
+    bool valid() const { return rows > 0 && rowptr.ptr != nullptr; }
+};
+
+// One solve's outcome, written by the CG kernels (device) and read back by the host.
+struct CgInfo {
+    int iterations;      // inner iterations in total
+    int status;          // nsf_status
+    int outer;           // refinement sweeps (mixed precision), 1 for the FP64 solver
+    int pad;
+    double rr;           // final ||r||^2 (recursive residual; FP64 true residual for the mixed solver)
+    double bb;           // ||b||^2
+};
+
+// grid-barrier word pair; zeroed before every persistent launch
+struct GridSync {
+    unsigned long long arrived;
+    int abort;
+    int where;
+};
+
+// Kernel-level arguments of the persistent CG solvers.
+struct CgArgs {
+    int n;
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    const float* val32;
+    const double* b;
+    const double* x0;
+    double* x;
+    double* r;
+    double* q;
+    double* pbuf0;
+    double* pbuf1;
+    float* r32;      // mixed precision inner vectors
+    float* d32;
+    float* q32;
+    float* p32a;
+    float* p32b;
+    double* partials;   // 4 * gridDim.x
+    GridSync* sync;
+    CgInfo* info;
+    int maxIt;
+    double tol2;
+    double innerTol2;
+    int maxOuter;
+    long long timeoutNs;
+    // optional rhs construction fused into the solver prologue:
+    //   b_i = bcMask[i] ? bcValue[i] : (Bm x_b)_i - lift[i]   (written to `bOut` and used as b)
+    const int* bRowptr;
+    const int* bCol;
+    const double* bVal;
+    const double* bX;
+    const double* lift;
+    const unsigned char* bcMask;
+    const double* bcValue;
+    double* bOut;
+};
+
+// the workspace shared by every solve on a handle (sized for the largest system)
+struct CgWorkspace {
+    DevBuf<double> r, q, p0, p1;
+    DevBuf<float> r32, d32, q32, p32a, p32b;
+    DevBuf<double> partials;
+    DevBuf<GridSync> sync;
+    DevBuf<CgInfo> info;     // ring of infos (one per solve in a step)
+    int grid = 0;            // persistent grid size (blocks)
+    int block = 0;
+};
+
+// launch helpers implemented in nsf_cg.cu / nsf_sparse.cu
+void cg_configure(CgWorkspace& ws, int device);
+void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, cudaStream_t s);
+void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
+void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
+                     const double* bcValue, double* y, cudaStream_t s);
+void axpy_bc_launch(int n, const double* a, double* y, const unsigned char* mask, const double* bcValue,
+                    cudaStream_t s);
+void make_fp32_values(Csr& A, cudaStream_t s);
+
+// ------------------------------------------------------------------------------------------------
+// Mesh, point-location tree and simulation state
+// ------------------------------------------------------------------------------------------------
+struct LocateTree {
+    int nLeaves = 0;          // padded to a power of two
+    int leafSize = 0;
+    int depth = 0;
+    DevBuf<int> triSorted;    // [nLeaves * leafSize], -1 padded
+    DevBuf<float4> box;       // heap-ordered node boxes (minx, miny, maxx, maxy), 2*nLeaves-1
+};
+
+struct MeshDev {
+    int nNodes = 0, nEl = 0, nP = 0;
+    DevBuf<float2> xy;
+    DevBuf<int> el;
+    std::vector<float> hxy;
+    std::vector<int> hel;
+    LocateTree tree;
+};
+
+void tree_build(MeshDev& m, cudaStream_t s);
+void locate_launch(const MeshDev& m, int n, const float2* pts, int* elem, float* xi, float* eta, int* nearest,
+                   cudaStream_t s);
+void advect_launch(const MeshDev& m, double dt, const double* u, const double* v, double* uo, double* vo,
+                   cudaStream_t s);
+void advect_f32_launch(const MeshDev& m, float dt, const float* u, const float* v, float* uo, float* vo,
+                       cudaStream_t s);
+
+struct SimState {
+    bool ready = false;
+    double viscosity = 0, dt = 0;
+    DevBuf<double> uv, tmp, p, rhsV, rhsP;
+    DevBuf<double> liftV[2], liftP;
+    DevBuf<unsigned char> bcV, bcP;
+    DevBuf<double> gV[2], gP;      // values imposed on Dirichlet rows (last listed occurrence wins)
+    std::vector<double> hgV[2], hgP;
+    std::vector<unsigned char> hbcV, hbcP;
+    int nColours = 0;
+};
+
+}  // namespace nsf
+
+// the opaque handle behind the C ABI
+struct nsf_device {
+    int device = 0;
+    int smCount = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    std::string lastError;
+    nsf::Csr mats[NSF_SLOT_COUNT];
+    nsf::CgWorkspace ws;
+    nsf::MeshDev mesh;
+    nsf::SimState sim;
+    nsf::DevBuf<double> scratch[4];   // host-pointer entry points stage their vectors here
+    double tol = 1e-8;
+    double innerTol = 1e-4;
+    long long timeoutNs = 2000000000LL;
+    int solverMode = NSF_SOLVER_FP64;
+    // per-solve records (profiling of the persistent CG kernels)
+    bool profile = false;
+    std::vector<cudaEvent_t> evPool;
+    size_t evUsed = 0;
+    struct SolveRecord { int slot; int mode; int rows; int64_t nnz; cudaEvent_t a, b; int infoIndex; };
+    std::vector<SolveRecord> records;
+    int infoCursor = 0;
+};

@@ -1,0 +1,355 @@
+// Point location and semi-Lagrangian advection on the GPU.
+//
+// Replaces the reference's CPU-built KD tree (cpp/kd_tree_builder.cpp:81-149) and its advect kernel
+// (gpu/advection.cu:14-57, driven by cpp/gpu_simulation_device.cpp:91-131).
+//
+// Tree: triangles are ordered by the Morton code of their centroid (a radix sort on the GPU), cut into
+// leaves of kLeafSize consecutive triangles, and the leaves form an implicit complete binary tree whose
+// nodes carry the union of their triangles' closed vertex bounding boxes.  No pointers, no recursion, and
+// the build is three data-parallel passes.
+//
+// Query semantics match the reference exactly: its tree sends every triangle whose closed vertex box holds
+// the point into the point's leaf (straddlers go to both sides, kd_tree_builder.cpp:134-141), and each leaf
+// lists triangles in ascending index, so its "first triangle in the leaf passing isPointInTriagle" is the
+// LOWEST-index triangle whose box holds the point and whose predicate passes.  This kernel visits every
+// node whose box holds the point and keeps that minimum.  The predicate is evaluated with IEEE
+// round-to-nearest float intrinsics in the reference's operation order (kd_tree_common.cuh:38-60), so
+// element ids and (xi, eta) are bit-identical.  When no triangle contains the point, the nearest mesh node
+// (all six nodes of each triangle, as nearestNeghbourProcessLeaf does, kd_tree.cuh:149-169) is found by a
+// box-distance branch and bound; equal distances resolve to the lowest node index.
+#include "nsf_internal.cuh"
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cfloat>
+#include <climits>
+
+namespace nsf {
+
+constexpr int kLeafSize = 8;
+constexpr int kStack = 48;
+
+__device__ __forceinline__ float2 node_xy(const float2* xy, int i) { return xy[i]; }
+
+// isPointInTriagle with every float operation rounded on its own (no contraction)
+__device__ __forceinline__ bool point_in_triangle(float px, float py, float2 A, float2 B, float2 C, float& xi,
+                                                  float& eta) {
+    const float abx = __fsub_rn(B.x, A.x), aby = __fsub_rn(B.y, A.y);
+    const float acx = __fsub_rn(C.x, A.x), acy = __fsub_rn(C.y, A.y);
+    const float apx = __fsub_rn(px, A.x), apy = __fsub_rn(py, A.y);
+    const float D = __fsub_rn(__fmul_rn(abx, acy), __fmul_rn(aby, acx));
+    const float sgn = D > 0.f ? 1.f : -1.f;
+    const float s1 = __fmul_rn(__fsub_rn(__fmul_rn(apx, acy), __fmul_rn(apy, acx)), sgn);
+    if (s1 < 0.f || s1 > D) return false;
+    const float s2 = __fmul_rn(__fsub_rn(__fmul_rn(apy, abx), __fmul_rn(apx, aby)), sgn);
+    if (s2 < 0.f || s1 > __fsub_rn(D, s2)) return false;
+    const float inv = __frcp_rn(fabsf(D));
+    xi = __fmul_rn(s1, inv);
+    eta = __fmul_rn(s2, inv);
+    return true;
+}
+
+__device__ __forceinline__ bool box_holds(float4 b, float px, float py) {
+    return b.x <= px && px <= b.z && b.y <= py && py <= b.w;
+}
+
+__device__ __forceinline__ float box_dist2(float4 b, float px, float py) {
+    const float dx = fmaxf(fmaxf(__fsub_rn(b.x, px), __fsub_rn(px, b.z)), 0.f);
+    const float dy = fmaxf(fmaxf(__fsub_rn(b.y, py), __fsub_rn(py, b.w)), 0.f);
+    return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+}
+
+struct TreeView {
+    const float2* xy;
+    const int* el;
+    const int* tri;
+    const float4* box;
+    int nLeaves;
+};
+
+// Containing element (lowest index) or -1; on -1, `nearest` holds the closest node.
+__device__ int locate_point(const TreeView& t, float px, float py, float& xi, float& eta, int& nearest) {
+    int stack[kStack];
+    int sp = 0;
+    stack[sp++] = 0;
+    int best = INT_MAX;
+    const int firstLeaf = t.nLeaves - 1;
+    while (sp > 0) {
+        const int nd = stack[--sp];
+        if (!box_holds(t.box[nd], px, py)) continue;
+        if (nd >= firstLeaf) {
+            const int* slots = t.tri + (size_t)(nd - firstLeaf) * kLeafSize;
+            for (int s = 0; s < kLeafSize; ++s) {
+                const int e = slots[s];
+                if (e < 0) break;
+                if (e >= best) continue;
+                const int* en = t.el + 6 * (size_t)e;
+                const float2 A = t.xy[en[0]], B = t.xy[en[1]], C = t.xy[en[2]];
+                const float4 tb = make_float4(fminf(A.x, fminf(B.x, C.x)), fminf(A.y, fminf(B.y, C.y)),
+                                              fmaxf(A.x, fmaxf(B.x, C.x)), fmaxf(A.y, fmaxf(B.y, C.y)));
+                if (!box_holds(tb, px, py)) continue;
+                float a, b;
+                if (point_in_triangle(px, py, A, B, C, a, b)) { best = e; xi = a; eta = b; }
+            }
+        } else if (sp + 2 <= kStack) {
+            stack[sp++] = 2 * nd + 2;
+            stack[sp++] = 2 * nd + 1;
+        }
+    }
+    if (best != INT_MAX) return best;
+
+    // nearest mesh node: branch and bound on box distance, nearer child first
+    float bestD = FLT_MAX;
+    int bestNode = -1;
+    sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int nd = stack[--sp];
+        if (box_dist2(t.box[nd], px, py) > bestD) continue;
+        if (nd >= firstLeaf) {
+            const int* slots = t.tri + (size_t)(nd - firstLeaf) * kLeafSize;
+            for (int s = 0; s < kLeafSize; ++s) {
+                const int e = slots[s];
+                if (e < 0) break;
+                const int* en = t.el + 6 * (size_t)e;
+                for (int j = 0; j < 6; ++j) {
+                    const int v = en[j];
+                    const float2 q = t.xy[v];
+                    const float dx = __fsub_rn(px, q.x), dy = __fsub_rn(py, q.y);
+                    const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+                    if (d < bestD || (d == bestD && v < bestNode)) { bestD = d; bestNode = v; }
+                }
+            }
+        } else if (sp + 2 <= kStack) {
+            const int l = 2 * nd + 1, r = 2 * nd + 2;
+            const float dl = box_dist2(t.box[l], px, py), dr = box_dist2(t.box[r], px, py);
+            if (dl <= dr) { stack[sp++] = r; stack[sp++] = l; }
+            else { stack[sp++] = l; stack[sp++] = r; }
+        }
+    }
+    nearest = bestNode;
+    return -1;
+}
+
+// P2 shape functions (include/assembly.h:217-224) evaluated left to right with every double operation
+// rounded on its own, the same sequence the oracle compiles without contraction.
+__device__ __forceinline__ void p2_eval_d(double xi, double eta, double N[6]) {
+    const double x2 = __dmul_rn(__dmul_rn(2.0, xi), xi);
+    const double e2 = __dmul_rn(__dmul_rn(2.0, eta), eta);
+    const double xe4 = __dmul_rn(__dmul_rn(4.0, xi), eta);
+    N[0] = __dadd_rn(__dadd_rn(__dadd_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(3.0, xi)), __dmul_rn(3.0, eta)), x2), xe4), e2);
+    N[1] = __dsub_rn(x2, xi);
+    N[2] = __dsub_rn(e2, eta);
+    N[3] = xe4;
+    N[4] = __dsub_rn(__dsub_rn(__dmul_rn(4.0, eta), xe4), __dmul_rn(__dmul_rn(4.0, eta), eta));
+    N[5] = __dsub_rn(__dsub_rn(__dmul_rn(4.0, xi), __dmul_rn(__dmul_rn(4.0, xi), xi)), xe4);
+}
+__device__ __forceinline__ void p2_eval_f(float xi, float eta, float N[6]) {
+    const float x2 = __fmul_rn(__fmul_rn(2.f, xi), xi);
+    const float e2 = __fmul_rn(__fmul_rn(2.f, eta), eta);
+    const float xe4 = __fmul_rn(__fmul_rn(4.f, xi), eta);
+    N[0] = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(1.f, __fmul_rn(3.f, xi)), __fmul_rn(3.f, eta)), x2), xe4), e2);
+    N[1] = __fsub_rn(x2, xi);
+    N[2] = __fsub_rn(e2, eta);
+    N[3] = xe4;
+    N[4] = __fsub_rn(__fsub_rn(__fmul_rn(4.f, eta), xe4), __fmul_rn(__fmul_rn(4.f, eta), eta));
+    N[5] = __fsub_rn(__fsub_rn(__fmul_rn(4.f, xi), __fmul_rn(__fmul_rn(4.f, xi), xi)), xe4);
+}
+
+__global__ void locate_kernel(TreeView t, int n, const float2* __restrict__ pts, int* elem, float* xiOut,
+                              float* etaOut, int* nearestOut) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float2 p = pts[i];
+        float xi = 0.f, eta = 0.f;
+        int nn = -1;
+        const int e = locate_point(t, p.x, p.y, xi, eta, nn);
+        elem[i] = e;
+        xiOut[i] = xi;
+        etaOut[i] = eta;
+        nearestOut[i] = e >= 0 ? -1 : nn;
+    }
+}
+
+// Back-trace x - dt*u in float (the reference's Point2D arithmetic, include/assembly.h:1690-1692), locate,
+// interpolate in double.
+__global__ void advect_kernel(TreeView t, int nNodes, float fdt, const double* __restrict__ u,
+                              const double* __restrict__ v, double* __restrict__ uo, double* __restrict__ vo) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nNodes; i += gridDim.x * blockDim.x) {
+        const float2 pos = t.xy[i];
+        const double ui = u[i], vi = v[i];
+        const float px = __fsub_rn(pos.x, __fmul_rn((float)ui, fdt));
+        const float py = __fsub_rn(pos.y, __fmul_rn((float)vi, fdt));
+        float xi = 0.f, eta = 0.f;
+        int nn = -1;
+        const int e = locate_point(t, px, py, xi, eta, nn);
+        if (e >= 0) {
+            double N[6];
+            p2_eval_d((double)xi, (double)eta, N);
+            const int* en = t.el + 6 * (size_t)e;
+            double su = 0.0, sv = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int nd = en[k];
+                su = __dadd_rn(su, __dmul_rn(N[k], u[nd]));
+                sv = __dadd_rn(sv, __dmul_rn(N[k], v[nd]));
+            }
+            uo[i] = su;
+            vo[i] = sv;
+        } else {
+            // nn stays -1 only for a non-finite departure point (a non-finite velocity): keep the node's value
+            const int src = nn >= 0 ? nn : i;
+            uo[i] = u[src];
+            vo[i] = v[src];
+        }
+    }
+}
+
+__global__ void advect_f32_kernel(TreeView t, int nNodes, float fdt, const float* __restrict__ u,
+                                  const float* __restrict__ v, float* __restrict__ uo, float* __restrict__ vo) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nNodes; i += gridDim.x * blockDim.x) {
+        const float2 pos = t.xy[i];
+        const float px = __fsub_rn(pos.x, __fmul_rn(u[i], fdt));
+        const float py = __fsub_rn(pos.y, __fmul_rn(v[i], fdt));
+        float xi = 0.f, eta = 0.f;
+        int nn = -1;
+        const int e = locate_point(t, px, py, xi, eta, nn);
+        if (e >= 0) {
+            float N[6];
+            p2_eval_f(xi, eta, N);
+            const int* en = t.el + 6 * (size_t)e;
+            float su = 0.f, sv = 0.f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                su = __fadd_rn(su, __fmul_rn(N[k], u[en[k]]));
+                sv = __fadd_rn(sv, __fmul_rn(N[k], v[en[k]]));
+            }
+            uo[i] = su;
+            vo[i] = sv;
+        } else {
+            const int src = nn >= 0 ? nn : i;
+            uo[i] = u[src];
+            vo[i] = v[src];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// build
+// ---------------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned spread_bits(unsigned v) {   // 16 -> 32 bits, interleaving zeros
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+__global__ void morton_kernel(int nEl, const float2* __restrict__ xy, const int* __restrict__ el, float4 bb,
+                              unsigned long long* keys) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nEl; e += gridDim.x * blockDim.x) {
+        const int* en = el + 6 * (size_t)e;
+        const float2 A = xy[en[0]], B = xy[en[1]], C = xy[en[2]];
+        const float cx = (A.x + B.x + C.x) * (1.0f / 3.0f), cy = (A.y + B.y + C.y) * (1.0f / 3.0f);
+        const float sx = bb.z > bb.x ? (cx - bb.x) / (bb.z - bb.x) : 0.f;
+        const float sy = bb.w > bb.y ? (cy - bb.y) / (bb.w - bb.y) : 0.f;
+        const unsigned qx = (unsigned)fminf(fmaxf(sx * 65535.f, 0.f), 65535.f);
+        const unsigned qy = (unsigned)fminf(fmaxf(sy * 65535.f, 0.f), 65535.f);
+        const unsigned code = spread_bits(qx) | (spread_bits(qy) << 1);
+        keys[e] = ((unsigned long long)code << 32) | (unsigned)e;
+    }
+}
+
+__global__ void leaf_kernel(int nEl, int nLeaves, const unsigned long long* __restrict__ sorted,
+                            const float2* __restrict__ xy, const int* __restrict__ el, int* tri, float4* box) {
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nLeaves; l += gridDim.x * blockDim.x) {
+        float4 b = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
+        for (int s = 0; s < kLeafSize; ++s) {
+            const long long k = (long long)l * kLeafSize + s;
+            int e = -1;
+            if (k < nEl) {
+                e = (int)(sorted[k] & 0xFFFFFFFFull);
+                const int* en = el + 6 * (size_t)e;
+                for (int j = 0; j < 3; ++j) {
+                    const float2 p = xy[en[j]];
+                    b.x = fminf(b.x, p.x); b.y = fminf(b.y, p.y);
+                    b.z = fmaxf(b.z, p.x); b.w = fmaxf(b.w, p.y);
+                }
+            }
+            tri[k] = e;
+        }
+        box[nLeaves - 1 + l] = b;
+    }
+}
+
+__global__ void level_kernel(int first, int count, float4* box) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int nd = first + i;
+        const float4 l = box[2 * nd + 1], r = box[2 * nd + 2];
+        box[nd] = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
+    }
+}
+
+static int blocks_for(long long n, int t) { return (int)std::max<long long>(1, std::min<long long>((n + t - 1) / t, 152LL * 64)); }
+
+void tree_build(MeshDev& m, cudaStream_t s) {
+    const int nEl = m.nEl;
+    float4 bb = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
+    for (int i = 0; i < m.nNodes; ++i) {
+        bb.x = std::min(bb.x, m.hxy[2 * i]); bb.y = std::min(bb.y, m.hxy[2 * i + 1]);
+        bb.z = std::max(bb.z, m.hxy[2 * i]); bb.w = std::max(bb.w, m.hxy[2 * i + 1]);
+    }
+    int leaves = 1, depth = 0;
+    while ((long long)leaves * kLeafSize < nEl) { leaves <<= 1; ++depth; }
+    LocateTree& t = m.tree;
+    t.nLeaves = leaves;
+    t.leafSize = kLeafSize;
+    t.depth = depth;
+    if (depth + 2 > kStack) throw Error{NSF_ERR_BAD_ARG, "mesh too large for the point-location stack"};
+    DevBuf<unsigned long long> keys, sorted;
+    keys.alloc(std::max(1, nEl));
+    sorted.alloc(std::max(1, nEl));
+    morton_kernel<<<blocks_for(nEl, 256), 256, 0, s>>>(nEl, m.xy.get(), m.el.get(), bb, keys.get());
+    NSF_CUDA(cudaGetLastError());
+    size_t tmpBytes = 0;
+    NSF_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmpBytes, keys.get(), sorted.get(), nEl, 0, 64, s));
+    DevBuf<unsigned char> tmp;
+    tmp.alloc(std::max<size_t>(tmpBytes, 1));
+    NSF_CUDA(cub::DeviceRadixSort::SortKeys(tmp.get(), tmpBytes, keys.get(), sorted.get(), nEl, 0, 64, s));
+    t.triSorted.alloc((size_t)leaves * kLeafSize);
+    t.box.alloc((size_t)2 * leaves - 1);
+    leaf_kernel<<<blocks_for(leaves, 256), 256, 0, s>>>(nEl, leaves, sorted.get(), m.xy.get(), m.el.get(),
+                                                       t.triSorted.get(), t.box.get());
+    NSF_CUDA(cudaGetLastError());
+    for (int lvl = depth - 1; lvl >= 0; --lvl) {
+        const int first = (1 << lvl) - 1, count = 1 << lvl;
+        level_kernel<<<blocks_for(count, 256), 256, 0, s>>>(first, count, t.box.get());
+        NSF_CUDA(cudaGetLastError());
+    }
+    NSF_CUDA(cudaStreamSynchronize(s));   // keys/sorted/tmp are released on return
+}
+
+static TreeView view(const MeshDev& m) {
+    return TreeView{m.xy.get(), m.el.get(), m.tree.triSorted.get(), m.tree.box.get(), m.tree.nLeaves};
+}
+
+void locate_launch(const MeshDev& m, int n, const float2* pts, int* elem, float* xi, float* eta, int* nearest,
+                   cudaStream_t s) {
+    if (n <= 0) return;
+    locate_kernel<<<blocks_for(n, 128), 128, 0, s>>>(view(m), n, pts, elem, xi, eta, nearest);
+    NSF_CUDA(cudaGetLastError());
+}
+
+void advect_launch(const MeshDev& m, double dt, const double* u, const double* v, double* uo, double* vo,
+                   cudaStream_t s) {
+    advect_kernel<<<blocks_for(m.nNodes, 128), 128, 0, s>>>(view(m), m.nNodes, (float)dt, u, v, uo, vo);
+    NSF_CUDA(cudaGetLastError());
+}
+
+void advect_f32_launch(const MeshDev& m, float dt, const float* u, const float* v, float* uo, float* vo,
+                       cudaStream_t s) {
+    advect_f32_kernel<<<blocks_for(m.nNodes, 128), 128, 0, s>>>(view(m), m.nNodes, dt, u, v, uo, vo);
+    NSF_CUDA(cudaGetLastError());
+}
+
+}  // namespace nsf

@@ -1,0 +1,359 @@
+"""ORACLE — test infrastructure, never part of the product.
+
+CPU checker for the GB300 hot path.  Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
+CPU-baseline leg may import this package, and only as the thing results are compared against (or, for
+the baseline, the thing timed beside the GPU).  Contents:
+
+* ``liboracle.so`` (built from ``nsfem_oracle.cpp`` by ``make``): the C++ restatement of the reference's
+  semi-Lagrangian path - assembly, Dirichlet elimination, CG, the reference's KD tree and advection, and
+  the operator-split step - templated on the scalar type (FP64 oracle / the reference's FP32 arithmetic).
+* ``_ref/libref_kdtree.so`` (built by ``make ref`` from the reference's own sources, only where the
+  reference checkout exists): the reference's KDTreeBuilder + KDTree::findElement, used to pin the port.
+* ``evaluate_expression``: a restatement of the reference's boundary-condition expression language
+  (cpp/expression.cpp: ``+ - * / ^``, unary minus, ``sin``/``cos``, variables x y z t, constants E, Pi;
+  precedence +,- < *,/ < unary minus < ^ (left associative) < function call).
+
+Parity status: the element lookup is pinned against the reference's compiled tree.  The CG stopping
+rule cannot be pinned (the reference's CPU CG is in the absent sparse_matrix_math submodule); it is
+restated from the thesis algorithm (tex/Chapters/01_chapter_FEM.tex:644-661) with a relative residual.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import re
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+SLOTS = {
+    "pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
+    "pressure_divergence": 4, "velocity_dirichlet_weights": 5, "pressure_dirichlet_weights": 6,
+}
+
+_p = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+_fptr = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_dptr = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_iptr = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_lptr = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile liboracle.so (and the reference tree when the reference sources are present)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    ref_dir = os.environ.get("NSFEM_REFERENCE_DIR", "/root/reference")
+    if ref is None:
+        ref = os.path.isdir(os.path.join(ref_dir, "cpp"))
+    if ref:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref_dir}"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build(ref=False)
+        L = ctypes.CDLL(path)
+        L.orc_create.restype = _p
+        L.orc_create.argtypes = [_i, _fptr, _i, _iptr, _i, _i, _iptr, _dptr, _dptr, _i, _iptr, _dptr, _d, _d, _i]
+        L.orc_destroy.argtypes = [_p]
+        L.orc_set_threads.argtypes = [_i]
+        L.orc_max_threads.restype = _i
+        L.orc_matrix_shape.argtypes = [_p, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_int64)]
+        L.orc_matrix_get.argtypes = [_p, _i, _lptr, _iptr, _dptr]
+        L.orc_spmv.argtypes = [_p, _i, _dptr, _dptr]
+        L.orc_cg.restype = _i
+        L.orc_cg.argtypes = [_p, _i, _dptr, _dptr, _dptr, _i, _d, ctypes.POINTER(_i), ctypes.POINTER(_d)]
+        L.orc_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
+        L.orc_tree_size.argtypes = [_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]
+        L.orc_advect.argtypes = [_p, _dptr, _dptr, _dptr, _dptr]
+        L.orc_step.restype = _i
+        L.orc_step.argtypes = [_p, _i, _iptr]
+        L.orc_set_fields.argtypes = [_p, _dptr, _dptr]
+        L.orc_get_fields.argtypes = [_p, _dptr, _dptr]
+        L.orc_point_in_triangle.restype = _i
+        L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
+        _LIB = L
+    return _LIB
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libref_kdtree.so"))
+
+
+def ref_lib():
+    global _REF
+    if _REF is None:
+        path = os.path.join(_HERE, "_ref", "libref_kdtree.so")
+        L = ctypes.CDLL(path)
+        L.ref_tree_create.restype = _p
+        L.ref_tree_create.argtypes = [_i, _fptr, _i, _iptr, _i]
+        L.ref_tree_destroy.argtypes = [_p]
+        L.ref_tree_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
+        L.ref_grid_bbox.argtypes = [_p, _fptr]
+        _REF = L
+    return _REF
+
+
+# ---------------------------------------------------------------------------------------------------
+# Boundary-condition expressions (restatement of cpp/expression.cpp semantics)
+# ---------------------------------------------------------------------------------------------------
+_TOKEN = re.compile(r"\s*(?:(sin|cos)|(Pi|E)|(\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?)|([xyzt])|([-+*/^()]))")
+
+
+def _tokenize(expr: str):
+    pos, out = 0, []
+    expr = expr.strip()
+    while pos < len(expr):
+        m = _TOKEN.match(expr, pos)
+        if not m or m.end() == pos:
+            raise ValueError(f"Error while parsing expression: {expr}. Unexpected symbol at {pos}")
+        fn, const, num, var, op = m.groups()
+        if fn:
+            out.append(("fn", fn))
+        elif const:
+            out.append(("num", math.e if const == "E" else math.pi))
+        elif num:
+            out.append(("num", float(num)))
+        elif var:
+            out.append(("var", var))
+        else:
+            out.append(("op", op))
+        pos = m.end()
+    return out
+
+
+def evaluate_expression(expr: str, variables: dict) -> float:
+    """Evaluate a reference BC expression in double precision."""
+    toks = _tokenize(expr)
+    i = 0
+
+    def peek():
+        return toks[i] if i < len(toks) else (None, None)
+
+    def take():
+        nonlocal i
+        t = toks[i]
+        i += 1
+        return t
+
+    def atom():
+        kind, val = peek()
+        if kind == "num":
+            take()
+            return val
+        if kind == "var":
+            take()
+            if val not in variables:
+                raise ValueError(f"Missing variable: {val}")
+            return float(variables[val])
+        if kind == "fn":
+            take()
+            if peek() != ("op", "("):
+                raise ValueError(f"Error parsing expression: {expr}. Functions must be surrounded by ()")
+            return math.sin(atom()) if val == "sin" else math.cos(atom())
+        if (kind, val) == ("op", "("):
+            take()
+            v = add()
+            if peek() != ("op", ")"):
+                raise ValueError(f"Error parsing expression: {expr}. Mismatched brackets.")
+            take()
+            return v
+        raise ValueError(f"Wrong expression: {expr}")
+
+    def power():
+        v = atom()
+        while peek() == ("op", "^"):
+            take()
+            if peek() == ("op", "-"):
+                take()
+                e = -power()
+            else:
+                e = atom()
+            v = v ** e
+        return v
+
+    def unary():
+        if peek() == ("op", "-"):
+            take()
+            return -unary()
+        return power()
+
+    def mul():
+        v = unary()
+        while peek() in (("op", "*"), ("op", "/")):
+            op = take()[1]
+            r = unary()
+            v = v * r if op == "*" else v / r
+        return v
+
+    def add():
+        v = mul()
+        while peek() in (("op", "+"), ("op", "-")):
+            op = take()[1]
+            r = mul()
+            v = v + r if op == "+" else v - r
+        return v
+
+    v = add()
+    if i != len(toks):
+        raise ValueError(f"Wrong expression: {expr}")
+    return float(v)
+
+
+def bc_occurrences(mesh):
+    """Dirichlet data as the reference walks it: every (group, node) occurrence in file order.
+
+    Returns (u_nodes int32, gu float64, gv float64, p_nodes int32, gp float64).  Values are the group's
+    expressions evaluated in double at the node's (float) coordinates with variables x and y.
+    """
+    un, gu, gv, pn, gp = [], [], [], [], []
+    for nodes, ue, ve in mesh.u_dirichlet:
+        for nd in nodes:
+            x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
+            un.append(int(nd))
+            gu.append(evaluate_expression(ue, {"x": x, "y": y}))
+            gv.append(evaluate_expression(ve, {"x": x, "y": y}))
+    for nodes, pe in mesh.p_dirichlet:
+        for nd in nodes:
+            x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
+            pn.append(int(nd))
+            gp.append(evaluate_expression(pe, {"x": x, "y": y}))
+    return (np.asarray(un, np.int32), np.asarray(gu, np.float64), np.asarray(gv, np.float64),
+            np.asarray(pn, np.int32), np.asarray(gp, np.float64))
+
+
+class Oracle:
+    """The CPU restatement of one simulation (mesh + BCs + nu + dt), FP64 by default."""
+
+    def __init__(self, mesh, viscosity: float, dt: float, real_bits: int = 64):
+        L = lib()
+        self.mesh = mesh
+        self.nv, self.np_ = mesh.n_nodes, mesh.n_pressure
+        un, gu, gv, pn, gp = bc_occurrences(mesh)
+        nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float32).reshape(-1)
+        els = np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1)
+        self._h = L.orc_create(mesh.n_nodes, nodes, mesh.n_elements, els, mesh.n_pressure, len(un), un, gu, gv,
+                               len(pn), pn, gp, float(viscosity), float(dt), int(real_bits))
+        self.dt = dt
+        self.viscosity = viscosity
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def matrix(self, name):
+        """(rowptr int64, col int32, val float64, shape) of one assembled matrix."""
+        L = lib()
+        slot = SLOTS[name] if isinstance(name, str) else int(name)
+        r, c, nnz = _i(), _i(), ctypes.c_int64()
+        L.orc_matrix_shape(self._h, slot, ctypes.byref(r), ctypes.byref(c), ctypes.byref(nnz))
+        rp = np.zeros(r.value + 1, np.int64)
+        col = np.zeros(nnz.value, np.int32)
+        val = np.zeros(nnz.value, np.float64)
+        L.orc_matrix_get(self._h, slot, rp, col, val)
+        return rp, col, val, (r.value, c.value)
+
+    def scipy_matrix(self, name):
+        import scipy.sparse as sp
+        rp, col, val, shape = self.matrix(name)
+        return sp.csr_matrix((val, col, rp), shape=shape)
+
+    def spmv(self, name, x):
+        rp, col, val, shape = self.matrix(name)
+        y = np.zeros(shape[0])
+        lib().orc_spmv(self._h, SLOTS[name], np.ascontiguousarray(x, np.float64), y)
+        return y
+
+    def cg(self, name, b, x0, max_iter=-1, tol=1e-8):
+        n = len(b)
+        x = np.zeros(n)
+        it, rr = _i(), _d()
+        st = lib().orc_cg(self._h, SLOTS[name], np.ascontiguousarray(b, np.float64),
+                          np.ascontiguousarray(x0, np.float64), x, int(max_iter), float(tol),
+                          ctypes.byref(it), ctypes.byref(rr))
+        return x, st, it.value, rr.value
+
+    def locate(self, pts):
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 2)
+        n = pts.shape[0]
+        e = np.zeros(n, np.int32)
+        xi = np.zeros(n, np.float32)
+        eta = np.zeros(n, np.float32)
+        nn = np.zeros(n, np.int32)
+        lib().orc_locate(self._h, n, pts.reshape(-1), e, xi, eta, nn)
+        return e, xi, eta, nn
+
+    def tree_size(self):
+        a, b, c = _i(), _i(), _i()
+        lib().orc_tree_size(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def advect(self, u, v):
+        uo, vo = np.zeros(self.nv), np.zeros(self.nv)
+        lib().orc_advect(self._h, np.ascontiguousarray(u, np.float64), np.ascontiguousarray(v, np.float64), uo, vo)
+        return uo, vo
+
+    def step(self, n=1):
+        iters = np.zeros(5 * n, np.int32)
+        st = lib().orc_step(self._h, int(n), iters)
+        return st, iters.reshape(n, 5)
+
+    def set_fields(self, uv, p):
+        lib().orc_set_fields(self._h, np.ascontiguousarray(uv, np.float64), np.ascontiguousarray(p, np.float64))
+
+    def fields(self):
+        uv, p = np.zeros(2 * self.nv), np.zeros(self.np_)
+        lib().orc_get_fields(self._h, uv, p)
+        return uv, p
+
+
+class ReferenceTree:
+    """The reference's own KD tree (oracle/_ref), built over a mesh; only where the reference compiled."""
+
+    def __init__(self, mesh):
+        L = ref_lib()
+        nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float32).reshape(-1)
+        els = np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1)
+        self._h = L.ref_tree_create(mesh.n_nodes, nodes, mesh.n_elements, els, mesh.n_pressure)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_tree_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def locate(self, pts):
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 2)
+        n = pts.shape[0]
+        e = np.zeros(n, np.int32)
+        xi = np.zeros(n, np.float32)
+        eta = np.zeros(n, np.float32)
+        nn = np.zeros(n, np.int32)
+        ref_lib().ref_tree_locate(self._h, n, pts.reshape(-1), e, xi, eta, nn)
+        return e, xi, eta, nn
+
+    def bbox(self):
+        out = np.zeros(4, np.float32)
+        ref_lib().ref_grid_bbox(self._h, out)
+        return out
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())

@@ -1,0 +1,138 @@
+"""The persistent CG megakernels (FP64 and mixed precision) through the C ABI, against the oracle CG and an
+FP64 residual recomputed on the host; plus the error paths (iteration cap, breakdown, barrier time limit)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import navier_stokes_fem_gb300 as nsf
+import oracle
+from navier_stokes_fem_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def system():
+    m = M.cavity(32)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    d = nsf.GPUSimulationDevice(0)
+    for name in ("pressure_stiffness", "diffusion", "velocity_mass"):
+        rp, col, val, shape = o.matrix(name)
+        d.upload_matrix(name, rp.astype(np.int32), col, val, shape)
+    yield d, o
+    d.close()
+
+
+def _relres(o, name, x, b):
+    A = o.scipy_matrix(name)
+    return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name", ["pressure_stiffness", "diffusion", "velocity_mass"])
+def test_fp64_cg_matches_oracle(system, name):
+    d, o = system
+    n = d.matrix_shape(name)[0]
+    rng = np.random.default_rng(1)
+    b = rng.standard_normal(n)
+    x0 = 0.1 * rng.standard_normal(n)
+    x, it, rr = d.conjugate_gradient(name, b, x0, eps=TOL)
+    xr, st, itr, _ = o.cg(name, b, x0, tol=TOL)
+    assert st == 0
+    assert _relres(o, name, x, b) < 1.5 * TOL
+    assert abs(it - itr) <= max(2, itr // 50)
+    assert rr <= TOL
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["pressure_stiffness", "diffusion"])
+def test_mixed_cg_reaches_fp64_residual(system, name):
+    d, o = system
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(2).standard_normal(n)
+    x, it, rr = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="mixed")
+    xr, st, itr, _ = o.cg(name, b, np.zeros(n), tol=TOL)
+    assert _relres(o, name, x, b) < 1.5 * TOL          # FP64 true residual drives the refinement loop
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+
+
+def test_cg_edge_cases(system):
+    d, o = system
+    name = "pressure_stiffness"
+    n = d.matrix_shape(name)[0]
+    z = np.zeros(n)
+    x, it, rr = d.conjugate_gradient(name, z, z)                   # b = 0, x0 = 0: converged, x = 0
+    assert it == 0 and not x.any()
+    b = np.random.default_rng(3).standard_normal(n)
+    xs, _, _ = d.conjugate_gradient(name, b, z)
+    x2, it2, _ = d.conjugate_gradient(name, b, xs)                 # initial guess already converged
+    assert it2 == 0 and np.array_equal(x2, xs)
+    x3, it3, rr3, st = d.conjugate_gradient(name, b, z, max_iterations=3, raise_on_error=False)
+    assert st == 2 and it3 == 3 and np.abs(x3).sum() > 0          # NOT_CONVERGED, last iterate written
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient(name, b, z, max_iterations=3)
+    assert e.value.status == 2 and "Max iterations reached!" in e.value.message
+    bn = b.copy()
+    bn[5] = np.nan
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient(name, bn, z)
+    assert e.value.status == 3
+
+
+def test_cg_breakdown_on_indefinite_matrix():
+    d = nsf.GPUSimulationDevice(0)
+    n = 64
+    A = sp.diags([np.r_[np.ones(n // 2), -np.ones(n // 2)]], [0]).tocsr()
+    d.upload_matrix("velocity_mass", A.indptr, A.indices, A.data, A.shape)
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient("velocity_mass", np.ones(n), np.zeros(n))
+    assert e.value.status == 3
+    d.close()
+
+
+def test_barrier_time_limit_returns_status_and_handle_survives(system):
+    d, o = system
+    name = "pressure_stiffness"
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(4).standard_normal(n)
+    d.set_barrier_timeout(0.0)                                    # every grid-wide wait expires at once
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient(name, b, np.zeros(n))
+    assert e.value.status == 4
+    d.set_barrier_timeout(2.0)
+    x, it, _ = d.conjugate_gradient(name, b, np.zeros(n))        # the context is still healthy
+    assert _relres(o, name, x, b) < 1.5 * TOL
+
+
+def test_triplet_upload_sums_duplicates_and_f32_signature():
+    d = nsf.GPUSimulationDevice(0)
+    rng = np.random.default_rng(8)
+    n = 200
+    R = sp.random(n, n, density=0.03, random_state=8)
+    A = (R @ R.T + sp.eye(n) * n * 0.1).tocoo()
+    rows = np.r_[A.row, A.row]
+    cols = np.r_[A.col, A.col]
+    vals = np.r_[A.data * 0.25, A.data * 0.75]
+    perm = rng.permutation(len(rows))
+    d.upload_matrix_triplets("pressure_stiffness", rows[perm], cols[perm], vals[perm], A.shape)
+    G = d.scipy_matrix("pressure_stiffness")
+    assert abs(G - A.tocsr()).max() < 1e-14
+    b = rng.standard_normal(n).astype(np.float32)
+    x = d.conjugate_gradient_f32("pressure_stiffness", b, np.zeros(n, np.float32), eps=1e-6)
+    assert np.linalg.norm(A @ x.astype(np.float64) - b) / np.linalg.norm(b) < 1e-5
+    y = d.sp_r_mult("pressure_stiffness", np.ones(n))
+    assert np.allclose(y, A.tocsr() @ np.ones(n), rtol=1e-13)
+    d.close()
+
+
+def test_bad_arguments_are_statuses():
+    d = nsf.GPUSimulationDevice(0)
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient("diffusion", np.ones(4), np.zeros(4))            # empty slot
+    assert e.value.status == 6
+    with pytest.raises(nsf.NSFemError) as e:
+        d.upload_matrix("velocity_mass", np.array([0, 1, 1]), np.array([5]), np.array([1.0]), (2, 2))
+    assert e.value.status == 5
+    with pytest.raises(nsf.NSFemError):
+        d.locate(np.zeros((3, 2), np.float32))                               # no mesh yet
+    d.close()

@@ -1,0 +1,101 @@
+"""GPU point location and advection against the reference's own tree (golden fixtures) and the oracle port.
+
+Element ids and the float barycentrics must be bit-identical; the nearest-node fallback may differ only where two
+nodes are at exactly the same float distance (the reference keeps the first one its traversal meets, the GPU the
+lowest index), and such ties are counted and checked to be true ties."""
+import numpy as np
+import pytest
+
+import navier_stokes_fem_gb300 as nsf
+import oracle
+from navier_stokes_fem_gb300 import mesh as M
+from tests._meshes import golden_mesh
+
+pytestmark = pytest.mark.gpu
+TAGS = ["mesh_small", "cavity32", "perturbed12"]
+
+
+@pytest.fixture(scope="module")
+def dev():
+    d = nsf.GPUSimulationDevice(0)
+    yield d
+    d.close()
+
+
+def _check_nearest_ties(m, pts, got, want):
+    diff = np.nonzero(got != want)[0]
+    for i in diff:
+        p = pts[i].astype(np.float32)
+        dg = np.float32(p[0] - m.nodes[got[i], 0]) ** 2 + np.float32(p[1] - m.nodes[got[i], 1]) ** 2
+        dw = np.float32(p[0] - m.nodes[want[i], 0]) ** 2 + np.float32(p[1] - m.nodes[want[i], 1]) ** 2
+        assert dg == dw, f"point {i}: nearest {got[i]} vs {want[i]} is not a tie"
+        assert got[i] < want[i]
+    return len(diff)
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_locate_matches_reference_tree(dev, golden, tag):
+    m = golden_mesh(golden, tag)
+    dev.upload_kd_tree(m)
+    pts = golden[f"{tag}/points"]
+    e, xi, eta, nn = dev.locate(pts)
+    assert np.array_equal(e, golden[f"{tag}/elem"])
+    assert np.array_equal(xi.view(np.uint32), golden[f"{tag}/xi"].view(np.uint32))
+    assert np.array_equal(eta.view(np.uint32), golden[f"{tag}/eta"].view(np.uint32))
+    outside = e < 0
+    ties = _check_nearest_ties(m, pts[outside], nn[outside], golden[f"{tag}/nearest"][outside])
+    assert ties <= max(2, outside.sum() // 100)
+
+
+@pytest.mark.parametrize("maker", [lambda: M.cavity(64), lambda: M.channel_with_obstacle(128, 32)])
+def test_locate_matches_oracle_large_random(dev, maker):
+    m = maker()
+    dev.upload_kd_tree(m)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    rng = np.random.default_rng(9)
+    lo, hi = m.nodes.min(0) - 0.02, m.nodes.max(0) + 0.02
+    pts = np.concatenate([rng.uniform(lo, hi, size=(200000, 2)), m.nodes,
+                          (m.nodes[:-1] + m.nodes[1:]) * 0.5]).astype(np.float32)
+    g, r = dev.locate(pts), o.locate(pts)
+    for a, b in zip(g[:3], r[:3]):
+        assert np.array_equal(a, b)
+    outside = g[0] < 0
+    _check_nearest_ties(m, pts[outside], g[3][outside], r[3][outside])
+
+
+def test_locate_edge_cases(dev):
+    m = M.cavity(8)
+    dev.upload_kd_tree(m)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    pts = np.array([[0, 0], [1, 1], [0.5, 0.5], [0.125, 0.125], [-1e30, 0.5], [2.0, 2.0], [0.0625, 0.0],
+                    [1.0, 0.5], [np.float32(1) + np.float32(1e-7), 0.5]], np.float32)
+    g, r = dev.locate(pts), o.locate(pts)
+    for a, b in zip(g, r):
+        assert np.array_equal(a, b)
+    e, *_ = dev.locate(np.zeros((0, 2), np.float32))
+    assert e.size == 0
+
+
+def test_advect_f64_bitexact_vs_oracle(dev):
+    m = M.cavity(32)
+    dev.upload_kd_tree(m)
+    o = oracle.Oracle(m, 0.01, 0.05)
+    rng = np.random.default_rng(4)
+    x, y = m.nodes[:, 0].astype(np.float64), m.nodes[:, 1].astype(np.float64)
+    u = np.sin(3 * y) + 0.3 * rng.standard_normal(m.n_nodes)
+    v = -np.cos(2 * x) + 0.3 * rng.standard_normal(m.n_nodes)
+    gu, gv = dev.advect_f64(u, v, 0.05)
+    ru, rv = o.advect(u, v)
+    assert np.array_equal(gu, ru) and np.array_equal(gv, rv)
+
+
+def test_advect_f32_reference_signature(dev):
+    m = M.channel_with_obstacle(64, 16)
+    dev.upload_kd_tree(m)
+    o = oracle.Oracle(m, 1e-3, 0.02, real_bits=32)
+    y = m.nodes[:, 1].astype(np.float64)
+    u = (4 * y * (1 - y)).astype(np.float32)
+    v = (0.1 * np.sin(6 * y)).astype(np.float32)
+    gu, gv = dev.advect(u, v, 0.02)
+    ru, rv = o.advect(u.astype(np.float64), v.astype(np.float64))
+    assert np.array_equal(gu, ru.astype(np.float32)) and np.array_equal(gv, rv.astype(np.float32))

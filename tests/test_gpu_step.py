@@ -1,0 +1,91 @@
+"""Whole operator-split steps resident on the GPU against the FP64 oracle (the restated reference path):
+velocity and pressure within 1e-6 relative L2 after N steps, CG iteration counts within a few per solve."""
+import numpy as np
+import pytest
+
+import navier_stokes_fem_gb300 as nsf
+import oracle
+from navier_stokes_fem_gb300 import mesh as M
+from tests._meshes import golden_mesh, rel
+
+pytestmark = pytest.mark.gpu
+FIELD_TOL = 1e-6          # FP64 path vs FP64 oracle, relative L2
+MIXED_TOL = 1e-6          # mixed precision (FP64-refined to the same 1e-8 residual) vs FP64 oracle
+
+
+def _run(m, nu, dt, steps, solver="fp64"):
+    sim = nsf.NavierStokesAssembly(m, nu, dt, solver=solver)
+    it = sim.step(steps)
+    uv, p = sim.fields()
+    sim.close()
+    return uv, p, it
+
+
+def _oracle(m, nu, dt, steps):
+    o = oracle.Oracle(m, nu, dt)
+    st, it = o.step(steps)
+    assert st == 0
+    uv, p = o.fields()
+    return uv, p, it
+
+
+def test_cavity32_100_steps_fp64():
+    m = M.cavity(32)
+    uv, p, it = _run(m, 0.01, 0.01, 100)
+    ruv, rp, rit = _oracle(m, 0.01, 0.01, 100)
+    assert rel(uv, ruv) < FIELD_TOL and rel(p, rp) < FIELD_TOL
+    assert np.abs(it - rit).max() <= 3
+    assert abs(int(it.sum()) - int(rit.sum())) <= 0.01 * rit.sum()
+
+
+def test_mesh_small_reference_asset(golden):
+    m = golden_mesh(golden, "mesh_small")
+    uv, p, it = _run(m, 0.001, 0.01, 20)
+    ruv, rp, rit = _oracle(m, 0.001, 0.01, 20)
+    assert rel(uv, ruv) < FIELD_TOL and rel(p, rp) < FIELD_TOL
+
+
+def test_channel_with_obstacle_small():
+    m = M.channel_with_obstacle(128, 32)
+    uv, p, it = _run(m, 1e-3, 2e-3, 10)
+    ruv, rp, rit = _oracle(m, 1e-3, 2e-3, 10)
+    assert rel(uv, ruv) < FIELD_TOL and rel(p, rp) < FIELD_TOL
+
+
+def test_mixed_precision_cavity32():
+    m = M.cavity(32)
+    uv, p, it = _run(m, 0.01, 0.01, 50, solver="mixed")
+    ruv, rp, _ = _oracle(m, 0.01, 0.01, 50)
+    assert rel(uv, ruv) < MIXED_TOL and rel(p, rp) < MIXED_TOL
+
+
+def test_host_field_api_roundtrip():
+    m = M.cavity(16)
+    a = nsf.NavierStokesAssembly(m, 0.01, 0.01)
+    b = nsf.NavierStokesAssembly(m, 0.01, 0.01)
+    a.step(3)
+    uv0, p0 = a.fields()
+    uv_out, p_out = np.zeros_like(uv0), np.zeros_like(p0)
+    b.step_host(uv0, p0, 2, uv_out, p_out)
+    a.step(2)
+    uv1, p1 = a.fields()
+    assert np.array_equal(uv_out, uv1) and np.array_equal(p_out, p1)
+    a.close()
+    b.close()
+
+
+def test_steps_are_deterministic():
+    m = M.channel_with_obstacle(64, 16)
+    a = _run(m, 1e-3, 2e-3, 5)
+    b = _run(m, 1e-3, 2e-3, 5)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_state_errors():
+    d = nsf.GPUSimulationDevice(0)
+    with pytest.raises(nsf.NSFemError) as e:
+        from navier_stokes_fem_gb300 import library
+        st = library().nsf_sim_step(d.handle, 1, None)
+        d._check(st)
+    assert e.value.status == 6
+    d.close()

@@ -1,0 +1,173 @@
+"""CPU tests of the oracle itself: pinned against the reference's own KD tree (golden fixtures and, where the
+reference checkout exists, live), closed-form assembly properties, CG residuals and the expression language."""
+import numpy as np
+import pytest
+
+import oracle
+from navier_stokes_fem_gb300 import mesh as M
+from tests._meshes import golden_mesh, rel
+
+TAGS = ["mesh_small", "cavity32", "perturbed12"]
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_oracle_tree_matches_reference_fixture(golden, tag):
+    m = golden_mesh(golden, tag)
+    o = oracle.Oracle(m, 0.01, 0.01) if m.u_dirichlet else _oracle_no_bc(m)
+    e, xi, eta, nn = o.locate(golden[f"{tag}/points"])
+    assert np.array_equal(e, golden[f"{tag}/elem"])
+    assert np.array_equal(xi.view(np.uint32), golden[f"{tag}/xi"].view(np.uint32))
+    assert np.array_equal(eta.view(np.uint32), golden[f"{tag}/eta"].view(np.uint32))
+    assert np.array_equal(nn, golden[f"{tag}/nearest"])
+    assert (e < 0).sum() > 100 and (e >= 0).sum() > 1000
+
+
+def _oracle_no_bc(m, nu=0.01, dt=0.01):
+    return oracle.Oracle(m, nu, dt)
+
+
+def test_reference_grid_bbox_quirk(golden):
+    # BBox2D::expand keeps the LAST node as the max corner (gpu_cpu_shared/misc_common.cuh:59-65)
+    bb = golden["cavity32/bbox"]
+    last = golden["cavity32/nodes"][-1]
+    assert bb[0] == 0 and bb[1] == 0 and bb[2] == last[0] and bb[3] == last[1]
+    assert bb[2] < 1.0
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference checkout not compiled here")
+def test_oracle_tree_matches_reference_live():
+    m = M.channel_with_obstacle(64, 16)
+    rng = np.random.default_rng(5)
+    pts = np.concatenate([rng.uniform([-0.1, -0.1], [4.1, 1.1], size=(20000, 2)), m.nodes]).astype(np.float32)
+    a = oracle.Oracle(m, 1e-3, 2e-3).locate(pts)
+    b = oracle.ReferenceTree(m).locate(pts)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_tree_depth_rule():
+    # maxDepth = min(29, round(8 + 1.3 ln T)) (cpp/kd_tree_builder.cpp:87)
+    for n in (4, 16, 32):
+        m = M.cavity(n)
+        o = oracle.Oracle(m, 0.01, 0.01)
+        _, _, depth = o.tree_size()
+        assert depth == min(29, int(round(8 + 1.3 * np.log(np.float32(2 * n * n)))))
+
+
+@pytest.mark.parametrize("n", [4, 16])
+def test_mass_and_stiffness_closed_forms(n):
+    m = M.cavity(n)
+    m.u_dirichlet, m.p_dirichlet = [], []            # no elimination: the raw operators
+    o = oracle.Oracle(m, 0.5, 0.1)
+    Mm = o.scipy_matrix("velocity_mass")
+    D = o.scipy_matrix("diffusion")
+    K = o.scipy_matrix("pressure_stiffness")
+    B = o.scipy_matrix("velocity_divergence")
+    G = o.scipy_matrix("pressure_divergence")
+    one_v, one_p = np.ones(m.n_nodes), np.ones(m.n_pressure)
+    assert abs(Mm.sum() - 1.0) < 1e-13                       # sum of all mass entries = area
+    # P2: vertex shape functions integrate to 0, midside ones to |T|/3
+    row = Mm @ one_v
+    assert np.abs(row[: m.n_pressure]).max() < 1e-14
+    assert np.allclose(row[m.n_pressure:].sum(), 1.0, atol=1e-13)
+    assert np.abs(K @ one_p).max() < 1e-12                  # stiffness annihilates constants
+    assert np.abs(D @ one_v - row).max() < 1e-12            # diffusion = M + dt*nu*K
+    assert np.abs(B @ np.ones(2 * m.n_nodes)).max() < 1e-9  # div of a constant field
+    assert np.abs(G @ one_p).max() < 1e-12                  # grad of a constant pressure
+    assert abs(Mm - Mm.T).max() < 1e-15 and abs(K - K.T).max() < 1e-15
+
+
+def test_cavity_pattern_counts():
+    # nnz of the P2 pattern 46n^2+16n+1 and of the P1 pattern 7n^2+6n+1 on the diagonal-split cavity
+    for n in (4, 32):
+        m = M.cavity(n)
+        m.u_dirichlet, m.p_dirichlet = [], []
+        o = oracle.Oracle(m, 0.01, 0.01)
+        assert o.matrix("velocity_mass")[1].size == 46 * n * n + 16 * n + 1
+        assert o.matrix("pressure_stiffness")[1].size == 7 * n * n + 6 * n + 1
+
+
+def test_dirichlet_elimination_structure():
+    m = M.cavity(8)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    D = o.scipy_matrix("diffusion").tocsr()
+    bc = np.unique(np.concatenate([g[0] for g in m.u_dirichlet]))
+    for r in bc[:20]:
+        row = D.getrow(r)
+        assert row.nnz == 1 and row.indices[0] == r and row.data[0] == 1.0
+    free = np.setdiff1d(np.arange(m.n_nodes), bc)
+    assert abs(D[free][:, bc]).max() == 0
+    W = o.scipy_matrix("velocity_dirichlet_weights")      # transposed storage: row = Dirichlet node
+    assert set(np.unique(W.tocoo().row)).issubset(set(bc))
+
+
+def test_cg_oracle_relative_residual():
+    m = M.cavity(16)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    A = o.scipy_matrix("pressure_stiffness")
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(A.shape[0])
+    x, st, it, rr = o.cg("pressure_stiffness", b, np.zeros_like(b))
+    assert st == 0 and it > 10
+    assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) < 1.5e-8
+    # already converged initial guess: zero iterations, x = x0
+    x2, st2, it2, _ = o.cg("pressure_stiffness", b, x)
+    assert st2 == 0 and it2 == 0 and np.array_equal(x2, x)
+
+
+def test_oracle_fp32_tracks_fp64():
+    m = M.cavity(16)
+    a, b = oracle.Oracle(m, 0.01, 0.01), oracle.Oracle(m, 0.01, 0.01, real_bits=32)
+    a.step(5)
+    b.step(5)
+    assert rel(b.fields()[0], a.fields()[0]) < 1e-4
+
+
+@pytest.mark.parametrize("expr,x,y,value", [
+    ("4*1.5*y*(0.41-y)/(0.41*0.41)", 0.0, 0.205, 1.5), ("-2^2", 0, 0, -4.0), ("2^-1", 0, 0, 0.5),
+    ("2^3^2", 0, 0, 64.0), ("sin(Pi/2)+cos(0)*E", 0, 0, 1 + np.e), ("1-x-y*3/2", 0.25, 0.5, 0.0),
+    ("-(x+1)*-2", 1.0, 0, 4.0), ("4*y*(1-y)", 0, 0.5, 1.0), ("0", 3, 4, 0.0), ("1e-3*x", 2, 0, 2e-3),
+])
+def test_expression_known_answers(expr, x, y, value):
+    import navier_stokes_fem_gb300 as nsf
+
+    assert oracle.evaluate_expression(expr, {"x": x, "y": y}) == pytest.approx(value, abs=1e-15)
+    assert nsf.evaluate_expression(expr, x, y) == pytest.approx(value, abs=1e-15)
+
+
+@pytest.mark.parametrize("bad", ["z+1", "(1+2", "sin 3", "1+*", "x$"])
+def test_expression_errors(bad):
+    import navier_stokes_fem_gb300 as nsf
+
+    with pytest.raises(Exception):
+        nsf.evaluate_expression(bad, 0.0, 0.0)
+    with pytest.raises(Exception):
+        oracle.evaluate_expression(bad, {"x": 0.0, "y": 0.0})
+
+
+def test_mesh_generators():
+    c = M.cavity(32)
+    assert (c.n_elements, c.n_nodes, c.n_pressure) == (2048, 4225, 1089)
+    ch = M.channel_with_obstacle(1024, 256)
+    assert ch.n_elements == 2 * (1024 * 256 - 50 * 50)
+    assert ch.n_nodes == 2049 * 513 - 99 * 99
+    for m in (c, ch):
+        v = m.nodes[m.elements[:, :3]].astype(np.float64)
+        area = (v[:, 1, 0] - v[:, 0, 0]) * (v[:, 2, 1] - v[:, 0, 1]) - (v[:, 1, 1] - v[:, 0, 1]) * (v[:, 2, 0] - v[:, 0, 0])
+        assert (area > 0).all()                                # counter-clockwise
+        allbc = np.concatenate([g[0] for g in m.u_dirichlet])
+        assert len(allbc) == len(np.unique(allbc))              # each boundary node in one group
+        assert m.elements[:, :3].max() < m.n_pressure <= m.elements[:, 3:].min()
+
+
+def test_mesh_json_roundtrip(tmp_path):
+    m = M.cavity(4)
+    p = tmp_path / "m.json"
+    M.write_mesh_json(m, str(p))
+    r = M.read_mesh_json(str(p))
+    assert np.array_equal(r.nodes, m.nodes) and np.array_equal(r.elements, m.elements)
+    assert [g[1:] for g in r.u_dirichlet] == [g[1:] for g in m.u_dirichlet]
+    s = tmp_path / "scene.json"
+    M.write_scene_json(str(s), "m.json", 1.0, 0.01, 0.01)
+    sc = M.read_scene_json(str(s))
+    assert sc["mesh_path"] == str(p)

@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark of the per-time-step hot path: ms per operator-split time step and CG iterations per solve at a
+1e-8 relative residual, on one GB300 (N GPUs run N independent replicas; the path does not shard).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--solver fp64|mixed] [--impl reference]
+
+A step is one pass of the hot path over the resident fields: advection, two diffusion solves, the pressure solve,
+the gradient product and two mass solves (NavierStokesAssembly::semiLagrangianSolve's loop body,
+include/assembly.h:1516-1556).  `value` is device time per step (CUDA events on the library's stream) with the
+fields resident in HBM; `e2e` is the same step through the C ABI with host fields copied in and out every step.
+`--impl reference` times the CPU oracle (the restated reference path; the reference's own CPU CG lives in an absent
+submodule) on the same workload with every host thread.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/time-step & CG iters at 1e-8 resid: learned-PCG mixed vs plain FP64 CG, GB300"
+
+WORKLOADS = {
+    # the lid-driven cavity the reference can run on a CPU: 32x32, nu=0.01, dt=0.01
+    "cavity32": dict(kind="cavity", n=32, nu=0.01, dt=0.01),
+    # channel 4x1 on 1024x256 cells, [0.9,1.1]x[0.4,0.6] removed, nu=1e-3, dt=2e-3
+    "channel1024x256": dict(kind="channel", nx=1024, ny=256, nu=1e-3, dt=2e-3),
+    # the large combined form: 2048x2048 cavity, nu=1e-4, dt=1e-4
+    "cavity2048": dict(kind="cavity", n=2048, nu=1e-4, dt=1e-4),
+    "cavity512": dict(kind="cavity", n=512, nu=1e-3, dt=1e-3),
+}
+DEFAULT_WORKLOAD = "channel1024x256"
+L2_BYTES = 129 << 20
+
+
+def make_mesh(w):
+    from navier_stokes_fem_gb300 import mesh as M
+
+    if w["kind"] == "cavity":
+        return M.cavity(w["n"])
+    return M.channel_with_obstacle(w["nx"], w["ny"])
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        idxs = sorted({r[0] for r in rows})
+        want = vis.split(",")[0] if vis.split(",")[0] in idxs else idxs[0]
+        rows = [r for r in rows if r[0] == want]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        loaded = [s for s in sm if s >= 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def algorithmic_bytes(mode, n, nnz, its, outer):
+    """Minimal DRAM bytes of one persistent CG launch (int32 indices).
+
+    FP64 iteration: nnz*(8+4) + 4(n+1) + 11 vector passes of 8n (SpMV gathers p and writes q, dot fused; x and r
+    read+write with p and q reads; p update reads r, p and writes p).  Prologue: one SpMV with x0 plus b, r, p, x.
+    Mixed: inner FP32 iterations nnz*(4+4) + 4(n+1) + 11*4n; every refinement sweep one FP64 residual
+    nnz*(8+4) + 4(n+1) + 28n and an x += d pass of 20n.
+    """
+    if mode == 0:
+        it_bytes = 12 * nnz + 4 * (n + 1) + 88 * n
+        return (12 * nnz + 4 * (n + 1) + 40 * n) + its * it_bytes
+    inner = 8 * nnz + 4 * (n + 1) + 44 * n
+    sweep = 12 * nnz + 4 * (n + 1) + 28 * n
+    return (outer + 1) * sweep + outer * 20 * n + its * inner
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(mesh, w, sample_steps, threads=None):
+    """The FP64 oracle on the host cores: setup, then `sample_steps` steps timed."""
+    import oracle
+
+    oracle.build(ref=False)
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.max_threads()
+    t0 = time.perf_counter()
+    o = oracle.Oracle(mesh, w["nu"], w["dt"])
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    st, it = o.step(sample_steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"ms_per_step": 1e3 * dt / sample_steps, "cores": cores, "setup_s": setup, "iterations": it,
+            "status": st}
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup()
+    w = WORKLOADS[args.workload]
+    if rank != 0:
+        barrier(pg)
+        return
+    mesh = make_mesh(w)
+    import oracle
+
+    oracle.build(ref=False)
+    cores = oracle.max_threads()
+    o = oracle.Oracle(mesh, w["nu"], w["dt"])
+    st, _ = o.step(args.warmup)
+    times, its = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st, it = o.step(1)
+        times.append(time.perf_counter() - t0)
+        its.append(it[0])
+    ms = 1e3 * sum(times) / len(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block(args, w, mesh, solver="fp64 CG (CPU oracle)"),
+        "cg_iterations_per_step": np.mean(its, axis=0).round(1).tolist() if its else None,
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} timed steps after {args.warmup} warm-up steps of the full workload"},
+        "e2e": {"value": round(ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    o.close()
+    print(json.dumps(line), flush=True)
+    barrier(pg)
+
+
+def config_block(args, w, mesh, solver):
+    cfg = {"workload": args.workload, "triangles": mesh.n_elements, "velocity_nodes": mesh.n_nodes,
+           "pressure_nodes": mesh.n_pressure, "nu": w["nu"], "dt": w["dt"], "tol": 1e-8, "solver": solver,
+           "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+    return cfg
+
+
+def run_gpu(args):
+    world, rank, local, pg = dist_setup()
+    import navier_stokes_fem_gb300 as nsf
+
+    w = WORKLOADS[args.workload]
+    mesh = make_mesh(w)
+    t0 = time.perf_counter()
+    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
+                                   inner_tolerance=args.inner_tol)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        sim.flush_l2(256 << 20)
+        sim.step(1)
+    sim.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    sim.profile(True)
+    launches0 = sim.launch_count()
+    barrier(pg)
+    sim.synchronize()
+    sim.timer_start()
+    its = []
+    for _ in range(args.steps):
+        sim.flush_l2(256 << 20)       # L2 evicted between steps (the step's matrices exceed L2 anyway)
+        its.append(sim.step(1)[0])
+    ms_total = sim.timer_stop()
+    sim.synchronize()
+    barrier(pg)
+    launches = sim.launch_count() - launches0
+    clk = clocks.stop()
+    prof = sim.profile_read()
+    sim.profile(False)
+    ms = max_over_ranks(pg, ms_total / args.steps)
+
+    # roofline of the dominant kernel: the persistent CG solver, over every launch in the timed region
+    bytes_total = 0.0
+    for m_, n_, z_, i_, o_ in zip(prof["mode"], prof["rows"], prof["nnz"], prof["iterations"], prof["outer"]):
+        bytes_total += algorithmic_bytes(int(m_), int(n_), int(z_), int(i_), int(o_))
+    cg_ms = float(np.sum(prof["ms"]))
+    peak, peak_kind = peaks()
+    achieved = bytes_total / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else 0.0
+    n_launch = len(prof["ms"])
+
+    # end to end through the C ABI: host fields copied in and out around every step (pinned buffers)
+    uv, p = sim.fields()
+    uv_in, p_in = sim.pinned(uv.shape), sim.pinned(p.shape)
+    uv_out, p_out = sim.pinned(uv.shape), sim.pinned(p.shape)
+    uv_in[:] = uv
+    p_in[:] = p
+    e2e_steps = max(1, min(args.steps, 3))
+    sim.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.step_host(uv_in, p_in, 1, uv_out, p_out)
+        uv_in, uv_out = uv_out, uv_in
+        p_in, p_out = p_out, p_in
+    e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / e2e_steps)
+    field_bytes = int(uv.nbytes + p.nbytes)
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        base = cpu_baseline(mesh, w, args.cpu_steps)
+    sim.close()
+    if rank != 0:
+        return
+    its = np.asarray(its)
+    line = {
+        "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.solver == "fp64" else "f32+f64",
+        "data": "synthetic (seeded structured mesh; inputs resident in HBM, L2 flushed between steps)",
+        "config": config_block(args, w, mesh, args.solver),
+        "cg_iterations_per_step": its.mean(axis=0).round(1).tolist(),
+        "cg_solves": ["diffusion u", "diffusion v", "pressure", "mass u", "mass v"],
+        "setup_s": round(setup_s, 3),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                     "kernel": "cg_fp64_kernel" if args.solver == "fp64" else "cg_mixed_kernel",
+                     "launches": n_launch, "kernel_ms_per_step": round(cg_ms / args.steps, 3),
+                     "algorithmic_bytes_per_launch": round(bytes_total / max(n_launch, 1)),
+                     "traffic": None},
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": field_bytes,
+                "d2h_bytes_per_step": field_bytes, "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if base is not None:
+        line["cpu_baseline"] = {"value": round(base["ms_per_step"], 3), "unit": "ms/step", "cores": base["cores"],
+                                "kind": "port",
+                                "sample": f"FP64 oracle, first {args.cpu_steps} step(s) of the same workload "
+                                          f"(setup {base['setup_s']:.1f} s excluded)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--solver", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--inner-tol", type=float, default=-1.0)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

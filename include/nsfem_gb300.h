@@ -143,6 +143,10 @@ int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* r
 int nsf_timer(nsf_device* h, int op, float* ms);
 int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr);
 int nsf_host_free(nsf_device* h, void* ptr);
+/* Number of kernels this handle has launched so far (all of the library's own kernels, memsets excluded). */
+int nsf_launch_count(nsf_device* h, int64_t* launches);
+/* Overwrites a device buffer of `bytes` bytes on the handle's stream (evicts the L2 between timed steps). */
+int nsf_flush_l2(nsf_device* h, size_t bytes);
 
 /* ---- mesh-file boundary expressions (Expression::init + evaluate, cpp/expression.cpp:308-431) ---------- */
 /* Evaluates `expression` at (x, y) in double precision.  NSF_ERR_BAD_ARG on a parse error or a variable

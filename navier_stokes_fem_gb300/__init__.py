@@ -92,6 +92,8 @@ _SIGS = {
     "nsf_host_alloc": (_i, [_v, _sz, _P(_v)]),
     "nsf_host_free": (_i, [_v, _v]),
     "nsf_eval_expression": (_i, [ctypes.c_char_p, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
+    "nsf_launch_count": (_i, [_v, _P(_i64)]),
+    "nsf_flush_l2": (_i, [_v, _sz]),
 }
 
 
@@ -347,6 +349,14 @@ class GPUSimulationDevice:
         ms = _f()
         self._check(library().nsf_timer(self._h, 1, ctypes.byref(ms)))
         return ms.value
+
+    def launch_count(self) -> int:
+        n = _i64()
+        self._check(library().nsf_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def flush_l2(self, nbytes: int = 512 << 20):
+        self._check(library().nsf_flush_l2(self._h, int(nbytes)))
 
     def pinned(self, shape, dtype=np.float64):
         """A numpy array in page-locked host memory (freed with the handle's process)."""

@@ -15,7 +15,9 @@ int assemble_all(nsf_device* h, double viscosity, double dt);
 
 using namespace nsf;
 
-#define NSF_BEGIN(h)                                    \
+std::atomic<long long> nsf::g_launches{0};
+
+#define NSF_BEGIN(h)                                 \
     if (!(h)) return NSF_ERR_BAD_ARG;                   \
     std::lock_guard<std::recursive_mutex> lk_((h)->mu); \
     try {                                               \
@@ -727,6 +729,20 @@ int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr) {
 int nsf_host_free(nsf_device* h, void* ptr) {
     NSF_BEGIN(h)
     if (ptr) NSF_CUDA(cudaFreeHost(ptr));
+    NSF_END(h)
+}
+
+int nsf_launch_count(nsf_device* h, int64_t* launches) {
+    NSF_BEGIN(h)
+    if (!launches) throw bad_arg("null output pointer");
+    *launches = g_launches.load();
+    NSF_END(h)
+}
+
+int nsf_flush_l2(nsf_device* h, size_t bytes) {
+    NSF_BEGIN(h)
+    h->flush.ensure(bytes);
+    NSF_CUDA(cudaMemsetAsync(h->flush.get(), (int)(h->flushToggle++ & 0xFF), bytes, h->stream));
     NSF_END(h)
 }
 

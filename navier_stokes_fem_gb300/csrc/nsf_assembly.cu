@@ -399,6 +399,7 @@ int assemble_all(nsf_device* h, double viscosity, double dt) {
     scale_kernel<<<blocks(Bd.nnz, 256), 256, 0, s>>>(Bd.nnz, -(1.0 / dt), Bd.val.get());
     scale_kernel<<<blocks(Gd.nnz, 256), 256, 0, s>>>(Gd.nnz, -dt, Gd.val.get());
     NSF_CUDA(cudaGetLastError());
+    count_launch(nColours + 4);
     int missing = 0;
     NSF_CUDA(cudaMemcpyFromSymbolAsync(&missing, g_missingSlots, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
     NSF_CUDA(cudaStreamSynchronize(s));

@@ -402,6 +402,7 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, cudaStream_t s) {
     void* params[] = {&a};
     const void* fn = mode == NSF_SOLVER_MIXED ? (const void*)cg_mixed_kernel : (const void*)cg_fp64_kernel;
     NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
+    count_launch();
 }
 
 }  // namespace nsf

@@ -1,6 +1,7 @@
 // Internal declarations shared by the GB300 solver's translation units.  Not part of the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstdarg>
@@ -29,6 +30,10 @@ struct Error {
     } while (0)
 
 inline Error bad_arg(const std::string& m) { return Error{NSF_ERR_BAD_ARG, m}; }
+
+// Every launch of one of the library's kernels is counted here (process-wide), for nsf_launch_count.
+extern std::atomic<long long> g_launches;
+inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ------------------------------------------------------------------------------------------------
 // device memory owned by a handle
@@ -208,6 +213,8 @@ struct nsf_device {
     nsf::MeshDev mesh;
     nsf::SimState sim;
     nsf::DevBuf<double> scratch[4];   // host-pointer entry points stage their vectors here
+    nsf::DevBuf<unsigned char> flush; // L2 eviction buffer (nsf_flush_l2)
+    unsigned flushToggle = 0;
     double tol = 1e-8;
     double innerTol = 1e-4;
     long long timeoutNs = 2000000000LL;

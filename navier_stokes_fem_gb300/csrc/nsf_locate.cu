@@ -311,6 +311,7 @@ void tree_build(MeshDev& m, cudaStream_t s) {
     sorted.alloc(std::max(1, nEl));
     morton_kernel<<<blocks_for(nEl, 256), 256, 0, s>>>(nEl, m.xy.get(), m.el.get(), bb, keys.get());
     NSF_CUDA(cudaGetLastError());
+    count_launch();
     size_t tmpBytes = 0;
     NSF_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmpBytes, keys.get(), sorted.get(), nEl, 0, 64, s));
     DevBuf<unsigned char> tmp;
@@ -321,10 +322,12 @@ void tree_build(MeshDev& m, cudaStream_t s) {
     leaf_kernel<<<blocks_for(leaves, 256), 256, 0, s>>>(nEl, leaves, sorted.get(), m.xy.get(), m.el.get(),
                                                        t.triSorted.get(), t.box.get());
     NSF_CUDA(cudaGetLastError());
+    count_launch();
     for (int lvl = depth - 1; lvl >= 0; --lvl) {
         const int first = (1 << lvl) - 1, count = 1 << lvl;
         level_kernel<<<blocks_for(count, 256), 256, 0, s>>>(first, count, t.box.get());
         NSF_CUDA(cudaGetLastError());
+    count_launch();
     }
     NSF_CUDA(cudaStreamSynchronize(s));   // keys/sorted/tmp are released on return
 }
@@ -338,18 +341,21 @@ void locate_launch(const MeshDev& m, int n, const float2* pts, int* elem, float*
     if (n <= 0) return;
     locate_kernel<<<blocks_for(n, 128), 128, 0, s>>>(view(m), n, pts, elem, xi, eta, nearest);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void advect_launch(const MeshDev& m, double dt, const double* u, const double* v, double* uo, double* vo,
                    cudaStream_t s) {
     advect_kernel<<<blocks_for(m.nNodes, 128), 128, 0, s>>>(view(m), m.nNodes, (float)dt, u, v, uo, vo);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void advect_f32_launch(const MeshDev& m, float dt, const float* u, const float* v, float* uo, float* vo,
                        cudaStream_t s) {
     advect_f32_kernel<<<blocks_for(m.nNodes, 128), 128, 0, s>>>(view(m), m.nNodes, dt, u, v, uo, vo);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace nsf

@@ -65,6 +65,7 @@ void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s) {
     spmv_kernel<<<grid_for((int64_t)A.rows * kLanes, kSpmvThreads), kSpmvThreads, 0, s>>>(
         A.rows, A.rowptr.get(), A.col.get(), A.val.get(), x, nullptr, nullptr, nullptr, y);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
@@ -72,12 +73,14 @@ void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const un
     spmv_kernel<<<grid_for((int64_t)A.rows * kLanes, kSpmvThreads), kSpmvThreads, 0, s>>>(
         A.rows, A.rowptr.get(), A.col.get(), A.val.get(), x, lift, mask, bcValue, y);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void axpy_bc_launch(int n, const double* a, double* y, const unsigned char* mask, const double* bcValue,
                     cudaStream_t s) {
     axpy_bc_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, y, mask, bcValue);
     NSF_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void make_fp32_values(Csr& A, cudaStream_t s) {
@@ -85,6 +88,7 @@ void make_fp32_values(Csr& A, cudaStream_t s) {
     A.val32.alloc((size_t)A.nnz);
     to_fp32_kernel<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.val.get(), A.val32.get());
     NSF_CUDA(cudaGetLastError());
+    count_launch();
     A.has32 = true;
 }
 

@@ -79,6 +79,7 @@ def lib():
         L.orc_step.argtypes = [_p, _i, _iptr]
         L.orc_set_fields.argtypes = [_p, _dptr, _dptr]
         L.orc_get_fields.argtypes = [_p, _dptr, _dptr]
+        L.orc_set_tolerance.argtypes = [_p, _d]
         L.orc_point_in_triangle.restype = _i
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
         _LIB = L
@@ -304,6 +305,10 @@ class Oracle:
         uo, vo = np.zeros(self.nv), np.zeros(self.nv)
         lib().orc_advect(self._h, np.ascontiguousarray(u, np.float64), np.ascontiguousarray(v, np.float64), uo, vo)
         return uo, vo
+
+    def set_tolerance(self, tol: float):
+        """Relative residual of every CG solve of `step` (1e-8 by default)."""
+        lib().orc_set_tolerance(self._h, float(tol))
 
     def step(self, n=1):
         iters = np.zeros(5 * n, np.int32)

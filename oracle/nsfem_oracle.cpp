@@ -377,6 +377,7 @@ struct SolverBase {
     virtual void set_fields(const double* uv, const double* p) = 0;
     virtual void get_fields(double* uv, double* p) = 0;
     virtual void spmv(int slot, const double* x, double* y) = 0;
+    virtual void set_tol(double t) = 0;
     KDTree tree;
     std::vector<float> xy;
     std::vector<int> el;
@@ -546,6 +547,8 @@ template <typename R> struct Solver : SolverBase {
         for (int i = 0; i < Nv; ++i) { uo[i] = (double)c[i]; vo[i] = (double)d[i]; }
     }
 
+    void set_tol(double t) override { tol = t; }
+
     int solve(int slot, const R* b, const R* x0, R* x, int* it) {
         double rr;
         return conjugate_gradient(mats[slot], b, x0, x, -1, tol, it, &rr);
@@ -669,6 +672,7 @@ int orc_tree_size(void* h, int* nNodes, int* nLeafTris, int* maxDepth) {
 }
 void orc_advect(void* h, const double* u, const double* v, double* uo, double* vo) { ((SolverBase*)h)->advect(u, v, uo, vo); }
 int orc_step(void* h, int nsteps, int* iters) { return ((SolverBase*)h)->step(nsteps, iters); }
+void orc_set_tolerance(void* h, double tol) { ((SolverBase*)h)->set_tol(tol); }
 void orc_set_fields(void* h, const double* uv, const double* p) { ((SolverBase*)h)->set_fields(uv, p); }
 void orc_get_fields(void* h, double* uv, double* p) { ((SolverBase*)h)->get_fields(uv, p); }
 

@@ -10,7 +10,9 @@ from tests._meshes import golden_mesh, rel
 
 pytestmark = pytest.mark.gpu
 FIELD_TOL = 1e-6          # FP64 path vs FP64 oracle, relative L2
-MIXED_TOL = 1e-6          # mixed precision (FP64-refined to the same 1e-8 residual) vs FP64 oracle
+# mixed precision (FP64-refined to the same 1e-8 residual) vs the discrete solution; the plain FP64 path at 1e-8
+# is itself ~1e-4 away from it on this case (6e-5 velocity, 9.5e-5 pressure after 50 steps)
+MIXED_TOL = 1e-3
 
 
 def _run(m, nu, dt, steps, solver="fp64"):
@@ -53,10 +55,20 @@ def test_channel_with_obstacle_small():
 
 
 def test_mixed_precision_cavity32():
+    """Two solvers that both stop at a 1e-8 relative residual can differ by ~cond(A)*1e-8 in the solution, so the
+    mixed form is held against the discrete solution itself (the FP64 oracle driven to 1e-13): its error must be
+    within MIXED_TOL and of the same size as the plain FP64 path's own error at 1e-8."""
     m = M.cavity(32)
     uv, p, it = _run(m, 0.01, 0.01, 50, solver="mixed")
-    ruv, rp, _ = _oracle(m, 0.01, 0.01, 50)
-    assert rel(uv, ruv) < MIXED_TOL and rel(p, rp) < MIXED_TOL
+    uv64, p64, _ = _run(m, 0.01, 0.01, 50, solver="fp64")
+    o = oracle.Oracle(m, 0.01, 0.01)
+    o.set_tolerance(1e-13)
+    assert o.step(50)[0] == 0
+    xuv, xp = o.fields()
+    err_mixed = max(rel(uv, xuv), rel(p, xp))
+    err_fp64 = max(rel(uv64, xuv), rel(p64, xp))
+    assert err_mixed < MIXED_TOL
+    assert err_mixed < 10 * max(err_fp64, 1e-9)
 
 
 def test_host_field_api_roundtrip():

@@ -37,6 +37,7 @@ WORKLOADS = {
     # the large combined form: 2048x2048 cavity, nu=1e-4, dt=1e-4
     "cavity2048": dict(kind="cavity", n=2048, nu=1e-4, dt=1e-4),
     "cavity512": dict(kind="cavity", n=512, nu=1e-3, dt=1e-3),
+    "cavity1024": dict(kind="cavity", n=1024, nu=1e-4, dt=1e-4),
 }
 DEFAULT_WORKLOAD = "channel1024x256"
 L2_BYTES = 129 << 20
@@ -311,6 +312,21 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+def run_cg_probe(args):
+    """Two pressure-matrix solves with a fixed iteration count (for kernel profiling of the CG megakernel)."""
+    import navier_stokes_fem_gb300 as nsf
+
+    w = WORKLOADS[args.workload]
+    mesh = make_mesh(w)
+    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], solver=args.solver, inner_tolerance=args.inner_tol)
+    b = np.random.default_rng(0).standard_normal(mesh.n_pressure)
+    for _ in range(2):
+        x, it, rr, st = sim.conjugate_gradient("pressure_stiffness", b, np.zeros_like(b), max_iterations=args.cg_probe,
+                                               solver=args.solver, raise_on_error=False)
+        print(json.dumps({"probe": "pressure CG", "rows": mesh.n_pressure, "iterations": it, "status": st}))
+    sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,10 +338,13 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=-1.0)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cg-probe", type=int, default=0, help="profiling aid: 2 pressure solves of this many iterations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.cg_probe:
+        run_cg_probe(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -148,6 +148,22 @@ int nsf_launch_count(nsf_device* h, int64_t* launches);
 /* Overwrites a device buffer of `bytes` bytes on the handle's stream (evicts the L2 between timed steps). */
 int nsf_flush_l2(nsf_device* h, size_t bytes);
 
+/* ---- allocation-free solve ----------------------------------------------------------------------------- */
+/* No counterpart in the reference.  The FP64 CG solve for callers that cannot call cudaMalloc: a host
+ * application whose device memory is all owned by its own pool or fixed budget, or a time-critical loop where a
+ * cudaMalloc (which can synchronise the device) is not acceptable.  Needs no handle and allocates nothing: the
+ * caller passes the CSR matrix (int32 indices, columns ascending per row), b, x0 and x in device memory it
+ * owns; the solver's work vectors live in an 8 MB array compiled into the library, which every GPU that loads
+ * the library holds until exit.  rows <= NSF_NOALLOC_MAX_ROWS, else NSF_ERR_BAD_ARG with a message on stderr.
+ * The first call on each device looks up that array's device address (cudaGetSymbolAddress) with the device
+ * current; make that first call before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU (other streams or threads) race, so serialise them.  Runs on `stream` (a cudaStream_t, NULL = default)
+ * and returns after the solve finished; statuses as nsf_conjugate_gradient. */
+#define NSF_NOALLOC_MAX_ROWS 262144
+int nsf_conjugate_gradient_noalloc(int rows, const int* rowptr_dev, const int* col_dev, const double* val_dev,
+                                   const double* b_dev, const double* x0_dev, double* x_dev, int maxIterations,
+                                   double eps, void* stream, int* iterations, double* relResidual);
+
 /* ---- mesh-file boundary expressions (Expression::init + evaluate, cpp/expression.cpp:308-431) ---------- */
 /* Evaluates `expression` at (x, y) in double precision.  NSF_ERR_BAD_ARG on a parse error or a variable
  * other than x and y; the message is written to `message` (may be NULL) up to `messageBytes`. */

@@ -93,6 +93,7 @@ _SIGS = {
     "nsf_host_free": (_i, [_v, _v]),
     "nsf_eval_expression": (_i, [ctypes.c_char_p, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
     "nsf_launch_count": (_i, [_v, _P(_i64)]),
+    "nsf_conjugate_gradient_noalloc": (_i, [_i, _v, _v, _v, _v, _v, _v, _i, _d, _v, _P(_i), _P(_d)]),
     "nsf_flush_l2": (_i, [_v, _sz]),
 }
 

@@ -405,4 +405,27 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, cudaStream_t s) {
     count_launch();
 }
 
+// The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.
+int cg_fp64_grid(int device, int* block) {
+    int sms = 0, coop = 0, occ64 = 0, occMixed = 0;
+    NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NSF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+    if (!coop) throw Error{NSF_ERR_NO_DEVICE, "device does not support cooperative launches"};
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, 0));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, 0));
+    const int perSm = std::min(2, std::min(occ64, occMixed));
+    if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
+    *block = kCgThreads;
+    return sms * perSm;
+}
+
+// Launches the FP64 solver with caller-provided workspace pointers (everything in `a` already set).
+void cg_launch_fp64_raw(const CgArgs& args, int grid, int block, cudaStream_t s) {
+    NSF_CUDA(cudaMemsetAsync(args.sync, 0, sizeof(GridSync), s));
+    CgArgs a = args;
+    void* params[] = {&a};
+    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)cg_fp64_kernel, dim3(grid), dim3(block), params, 0, s));
+    count_launch();
+}
+
 }  // namespace nsf

@@ -130,6 +130,23 @@ int nsf_sim_step(nsf_device* h, int nsteps, int* iterations);
 int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int nsteps, double* uvOut,
                       double* pOut, int* iterations);
 
+/* ---- batched form: many independent instances in one persistent launch per step -------------------- */
+/* No single counterpart in the reference, which runs one mesh per process: each instance is a complete
+ * NavierStokesAssembly problem (same arguments as nsf_sim_setup).  nsf_batch_add assembles one instance and
+ * returns its index; nsf_batch_finalize divides the co-resident CTAs among the instances (an autotuner times
+ * `autotuneRounds` trial steps on saved fields and keeps the fastest split) and captures the step as a CUDA
+ * graph; nsf_batch_step replays it.  iterations: nsteps x count x 5 (diffusion u, v, pressure, mass u, v). */
+int nsf_batch_clear(nsf_device* h);
+int nsf_batch_add(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure,
+                  int nVelocityBC, const int* velocityBCNodes, const double* bcU, const double* bcV, int nPressureBC,
+                  const int* pressureBCNodes, const double* bcP, double viscosity, double dt, int* index);
+int nsf_batch_finalize(nsf_device* h, int autotuneRounds);
+int nsf_batch_step(nsf_device* h, int nsteps, int* iterations);
+int nsf_batch_get_fields(nsf_device* h, int index, double* uv, double* p);
+int nsf_batch_set_fields(nsf_device* h, int index, const double* uv, const double* p);
+/* The plan in use: CTAs per instance (count entries), total CTAs, and the autotuner's trial step times. */
+int nsf_batch_plan(nsf_device* h, int* blocks, int* gridBlocks, float* trialMs, int maxTrials, int* nTrials);
+
 /* ---- configuration, timing, pinned memory ------------------------------------------------------------ */
 int nsf_set_tolerance(nsf_device* h, double eps);
 int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);

@@ -22,7 +22,8 @@ import numpy as np
 from . import mesh as mesh_io
 
 __all__ = [
-    "NSFemError", "GPUSimulationDevice", "NavierStokesAssembly", "library", "library_path", "evaluate_expression",
+    "NSFemError", "GPUSimulationDevice", "NavierStokesAssembly", "BatchedNavierStokes", "library", "library_path",
+    "evaluate_expression",
     "bc_occurrences", "SLOT", "SOLVER", "STATUS", "declared_symbols",
 ]
 
@@ -93,6 +94,14 @@ _SIGS = {
     "nsf_host_free": (_i, [_v, _v]),
     "nsf_eval_expression": (_i, [ctypes.c_char_p, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
     "nsf_launch_count": (_i, [_v, _P(_i64)]),
+    "nsf_batch_clear": (_i, [_v]),
+    "nsf_batch_add": (_i, [_v, _i, _arr(np.float32), _i, _arr(np.int32), _i, _i, _arr(np.int32), _arr(np.float64),
+                           _arr(np.float64), _i, _arr(np.int32), _arr(np.float64), _d, _d, _P(_i)]),
+    "nsf_batch_finalize": (_i, [_v, _i]),
+    "nsf_batch_step": (_i, [_v, _i, _v]),
+    "nsf_batch_get_fields": (_i, [_v, _i, _v, _v]),
+    "nsf_batch_set_fields": (_i, [_v, _i, _v, _v]),
+    "nsf_batch_plan": (_i, [_v, _v, _P(_i), _v, _i, _P(_i)]),
     "nsf_conjugate_gradient_noalloc": (_i, [_i, _v, _v, _v, _v, _v, _v, _i, _d, _v, _P(_i), _P(_d)]),
     "nsf_flush_l2": (_i, [_v, _sz]),
 }
@@ -431,3 +440,56 @@ class NavierStokesAssembly(GPUSimulationDevice):
                                                 uv_out.ctypes.data_as(_v), p_out.ctypes.data_as(_v),
                                                 it.ctypes.data_as(_v)))
         return it[:5 * n].reshape(n, 5)
+
+
+class BatchedNavierStokes(GPUSimulationDevice):
+    """Many independent NavierStokesAssembly problems advanced together: one persistent launch per step in
+    which every instance is served by its own team of CTAs, the step replayed from a CUDA graph.
+
+    ``problems`` is a list of (mesh, viscosity, dt).  Team sizes are picked by the library's autotuner over
+    ``autotune_rounds`` timed trial steps (the fields are restored afterwards)."""
+
+    def __init__(self, problems, device: int = 0, solver: str = "fp64", tol: float = 1e-8,
+                 inner_tolerance: float = -1.0, autotune_rounds: int = 3):
+        super().__init__(device)
+        self.set_tolerance(tol)
+        self.set_solver(solver, inner_tolerance)
+        self.sizes = []
+        for mesh, nu, dt in problems:
+            un, gu, gv, pn, gp = _bc_fast(mesh) if mesh.n_nodes > 200_000 else bc_occurrences(mesh)
+            idx = _i()
+            self._check(library().nsf_batch_add(
+                self._h, mesh.n_nodes, np.ascontiguousarray(mesh.nodes, np.float32).reshape(-1), mesh.n_elements,
+                np.ascontiguousarray(mesh.elements, np.int32).reshape(-1), mesh.n_pressure, len(un), un, gu, gv,
+                len(pn), pn, gp, float(nu), float(dt), ctypes.byref(idx)))
+            self.sizes.append((mesh.n_nodes, mesh.n_pressure))
+        self._check(library().nsf_batch_finalize(self._h, int(autotune_rounds)))
+
+    @property
+    def count(self) -> int:
+        return len(self.sizes)
+
+    def step(self, n: int = 1):
+        """n steps of every instance; returns int32 [n, count, 5] CG iterations."""
+        it = np.zeros(max(n, 1) * self.count * 5, np.int32)
+        self._check(library().nsf_batch_step(self._h, int(n), it.ctypes.data_as(_v)))
+        return it[: n * self.count * 5].reshape(n, self.count, 5)
+
+    def fields(self, index: int):
+        nv, npr = self.sizes[index]
+        uv, p = np.zeros(2 * nv), np.zeros(npr)
+        self._check(library().nsf_batch_get_fields(self._h, int(index), uv.ctypes.data_as(_v), p.ctypes.data_as(_v)))
+        return uv, p
+
+    def set_fields(self, index: int, uv, p):
+        uv = np.ascontiguousarray(uv, np.float64)
+        p = np.ascontiguousarray(p, np.float64)
+        self._check(library().nsf_batch_set_fields(self._h, int(index), uv.ctypes.data_as(_v), p.ctypes.data_as(_v)))
+
+    def plan(self):
+        blocks = np.zeros(self.count, np.int32)
+        grid, nt = _i(), _i()
+        trials = np.zeros(64, np.float32)
+        self._check(library().nsf_batch_plan(self._h, blocks.ctypes.data_as(_v), ctypes.byref(grid),
+                                             trials.ctypes.data_as(_v), 64, ctypes.byref(nt)))
+        return {"blocks": blocks, "grid_blocks": grid.value, "trial_ms": trials[: nt.value].tolist()}

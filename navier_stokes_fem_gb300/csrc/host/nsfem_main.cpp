@@ -35,6 +35,7 @@ const std::map<std::string, Param> kParams = {
     {"solver", {"Linear solver: fp64 (plain FP64 CG) or mixed (FP32 inner CG, FP64 refinement)", false, false}},
     {"device", {"CUDA device index", true, false}},
     {"tol", {"Relative residual of every CG solve (default 1e-8)", false, false}},
+    {"resume", {"Continue from a result file out_<t>.json of an earlier run (steps t+1 .. steps)", false, false}},
 };
 
 void usage(FILE* f) {
@@ -120,13 +121,18 @@ int main(int argc, char** argv) {
     const auto t1 = std::chrono::steady_clock::now();
     std::vector<double> uv(2 * (size_t)scene.nNodes), p(scene.nPressure);
     try {
-        if (!outPath.empty()) {
+        int firstStep = 1;
+        if (args.count("resume")) {
+            firstStep = nsfhost::read_solution(args["resume"], scene.nNodes, scene.nPressure, uv, p) + 1;
+            if ((st = nsf_sim_set_fields(h, uv.data(), p.data())) != NSF_OK) return fail(st);
+            printf("Resuming after time step %d\n", firstStep - 1);
+        } else if (!outPath.empty()) {
             if ((st = nsf_sim_get_fields(h, uv.data(), p.data())) != NSF_OK) return fail(st);
             nsfhost::write_solution(outPath, 0, scene.nNodes, scene.nPressure, uv.data(), p.data());
         }
         std::vector<int> it(5);
         long long total[5] = {0, 0, 0, 0, 0};
-        for (int step = 1; step <= steps; ++step) {
+        for (int step = firstStep; step <= steps; ++step) {
             if ((st = nsf_sim_step(h, 1, it.data())) != NSF_OK) return fail(st);
             for (int k = 0; k < 5; ++k) total[k] += it[k];
             if (!outPath.empty()) {

@@ -104,4 +104,21 @@ void write_solution(const std::string& folder, int timeStep, int nNodes, int nPr
     f << "}\n";
 }
 
+int read_solution(const std::string& path, int nNodes, int nPressure, std::vector<double>& uv,
+                  std::vector<double>& p) {
+    const Json j = parse_json_file(path);
+    const Json &u = j["u"], &v = j["v"], &pp = j["p"];
+    if ((int)u.size() != nNodes || (int)v.size() != nNodes || (int)pp.size() != nPressure)
+        throw std::runtime_error("solution file " + path + " does not match the mesh's node counts");
+    uv.assign(2 * (size_t)nNodes, 0.0);
+    p.assign(nPressure, 0.0);
+    for (int i = 0; i < nNodes; ++i) {
+        uv[i] = u[i].num;
+        uv[nNodes + i] = v[i].num;
+    }
+    for (int i = 0; i < nPressure; ++i) p[i] = pp[i].num;
+    if (!j["timeStep"].is_number()) throw std::runtime_error("solution file " + path + " has no timeStep");
+    return (int)j["timeStep"].num;
+}
+
 }  // namespace nsfhost

@@ -32,4 +32,9 @@ void load_mesh(const std::string& meshPath, Scene& s);
 void write_solution(const std::string& folder, int timeStep, int nNodes, int nPressure, const double* uv,
                     const double* p);
 
+// Reads an out_<t>.json back (uv = [u | v], p); returns its timeStep.  The reference has no reader for its own
+// result files beyond the convergence-order estimate (cpp/main.cpp:53-61); this one resumes a run.
+int read_solution(const std::string& path, int nNodes, int nPressure, std::vector<double>& uv,
+                  std::vector<double>& p);
+
 }  // namespace nsfhost

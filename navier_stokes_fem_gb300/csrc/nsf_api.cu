@@ -9,11 +9,103 @@
 #include <numeric>
 #include <stdexcept>
 
+using namespace nsf;
+
 namespace nsf {
-int assemble_all(nsf_device* h, double viscosity, double dt);
+
+// Validates and uploads a mesh, then builds its point-location tree.
+void upload_mesh_into(MeshDev& m, cudaStream_t s, int nNodes, const float* xy, int nElements, const int* elements,
+                      int nPressure) {
+    if (nNodes <= 0 || nElements <= 0 || !xy || !elements) throw bad_arg("empty mesh");
+    if (nPressure <= 0 || nPressure > nNodes) throw bad_arg("pressure node count out of range");
+    for (int64_t k = 0; k < (int64_t)6 * nElements; ++k)
+        if (elements[k] < 0 || elements[k] >= nNodes) throw bad_arg("element references a node out of range");
+    for (int64_t k = 0; k < (int64_t)2 * nNodes; ++k)
+        if (!std::isfinite(xy[k])) throw bad_arg("non-finite node coordinate");
+    m.nNodes = nNodes;
+    m.nEl = nElements;
+    m.nP = nPressure;
+    m.hxy.assign(xy, xy + 2 * (size_t)nNodes);
+    m.hel.assign(elements, elements + 6 * (size_t)nElements);
+    m.xy.upload((const float2*)xy, nNodes, s);
+    m.el.upload(elements, 6 * (size_t)nElements, s);
+    tree_build(m, s);
 }
 
-using namespace nsf;
+void setup_instance(MeshDev& m, SimState& S, Csr* mats, cudaStream_t s, int nNodes, const float* xy, int nElements,
+                    const int* elements, int nPressure, int nVelocityBC, const int* velocityBCNodes, const double* bcU,
+                    const double* bcV, int nPressureBC, const int* pressureBCNodes, const double* bcP, double viscosity,
+                    double dt) {
+    if (!(dt > 0) || !(viscosity >= 0)) throw bad_arg("dt must be positive and viscosity non-negative");
+    if (nVelocityBC < 0 || nPressureBC < 0) throw bad_arg("negative boundary count");
+    if ((nVelocityBC > 0 && (!velocityBCNodes || !bcU || !bcV)) || (nPressureBC > 0 && (!pressureBCNodes || !bcP)))
+        throw bad_arg("null boundary array");
+    upload_mesh_into(m, s, nNodes, xy, nElements, elements, nPressure);
+    S.ready = false;
+    S.viscosity = viscosity;
+    S.dt = dt;
+    const int Nv = nNodes, P = nPressure;
+    // Dirichlet data: mask, imposed value (last listed occurrence) and lift weight (sum over occurrences,
+    // because the reference subtracts the lift once per listed occurrence, include/assembly.h:505-523)
+    S.hbcV.assign(Nv, 0);
+    S.hbcP.assign(P, 0);
+    std::vector<double> gset[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
+    std::vector<double> glift[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
+    std::vector<double> gsetP(P, 0.0), gliftP(P, 0.0);
+    for (int k = 0; k < nVelocityBC; ++k) {
+        const int nd = velocityBCNodes[k];
+        if (nd < 0 || nd >= Nv) throw bad_arg("velocity Dirichlet node out of range");
+        S.hbcV[nd] = 1;
+        gset[0][nd] = bcU[k];
+        gset[1][nd] = bcV[k];
+        glift[0][nd] += bcU[k];
+        glift[1][nd] += bcV[k];
+    }
+    for (int k = 0; k < nPressureBC; ++k) {
+        const int nd = pressureBCNodes[k];
+        if (nd < 0 || nd >= P) throw bad_arg("pressure Dirichlet node out of range");
+        S.hbcP[nd] = 1;
+        gsetP[nd] = bcP[k];
+        gliftP[nd] += bcP[k];
+    }
+    S.bcV.upload(S.hbcV.data(), Nv, s);
+    S.bcP.upload(S.hbcP.data(), P, s);
+    for (int ch = 0; ch < 2; ++ch) {
+        S.hgV[ch] = gset[ch];
+        S.gV[ch].upload(gset[ch].data(), Nv, s);
+    }
+    S.hgP = gsetP;
+    S.gP.upload(gsetP.data(), P, s);
+    S.nColours = assemble_instance(m, S, mats, s, viscosity, dt);
+    // constant lift vectors: lift = W g (the Dirichlet data do not depend on time: the expressions see x, y only)
+    DevBuf<double> g;
+    for (int ch = 0; ch < 2; ++ch) {
+        g.upload(glift[ch].data(), Nv, s);
+        S.liftV[ch].alloc(Nv);
+        spmv_launch(mats[NSF_VELOCITY_LIFT], g.get(), S.liftV[ch].get(), s);
+        NSF_CUDA(cudaStreamSynchronize(s));
+    }
+    g.upload(gliftP.data(), P, s);
+    S.liftP.alloc(P);
+    spmv_launch(mats[NSF_PRESSURE_LIFT], g.get(), S.liftP.get(), s);
+    NSF_CUDA(cudaStreamSynchronize(s));
+    // fields: u = 0 with Dirichlet values (imposeVelocityDirichlet), p = 0
+    std::vector<double> uv0(2 * (size_t)Nv, 0.0);
+    for (int k = 0; k < nVelocityBC; ++k) {
+        uv0[velocityBCNodes[k]] = bcU[k];
+        uv0[velocityBCNodes[k] + (size_t)Nv] = bcV[k];
+    }
+    S.uv.upload(uv0.data(), uv0.size(), s);
+    S.tmp.alloc(2 * (size_t)Nv);
+    S.tmp.zero(s);
+    S.rhsV.alloc(2 * (size_t)Nv);
+    S.rhsP.alloc(P);
+    S.p.alloc(P);
+    S.p.zero(s);
+    NSF_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace nsf
 
 std::atomic<long long> nsf::g_launches{0};
 
@@ -175,7 +267,8 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     SimState& S = h->sim;
     MeshDev& m = h->mesh;
     const int Nv = m.nNodes;
-    const int mode = h->solverMode;
+    // mixed precision per system, unless that system already had to finish in FP64 (see run_steps)
+    auto mode = [&](int slot) { return h->solverMode == NSF_SOLVER_MIXED && !h->mixedOff[slot] ? NSF_SOLVER_MIXED : NSF_SOLVER_FP64; };
     cudaStream_t s = h->stream;
     double* uv = S.uv.get();
     double* tmp = S.tmp.get();
@@ -193,7 +286,7 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
         f.bcMask = S.bcV.get();
         f.bcValue = S.gV[ch].get();
         f.bOut = S.rhsV.get() + (size_t)ch * Nv;
-        infos[ch] = launch_solve(h, NSF_DIFFUSION, mode, f.bOut, tmp + (size_t)ch * Nv, uv + (size_t)ch * Nv, -1,
+        infos[ch] = launch_solve(h, NSF_DIFFUSION, mode(NSF_DIFFUSION), f.bOut, tmp + (size_t)ch * Nv, uv + (size_t)ch * Nv, -1,
                                  h->tol, &f);
     }
     // pressure projection (include/assembly.h:560-712): rhs_p = -(1/dt) Div u - lift, pinned nodes -> g
@@ -208,17 +301,20 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
         f.bcMask = S.bcP.get();
         f.bcValue = S.gP.get();
         f.bOut = S.rhsP.get();
-        infos[2] = launch_solve(h, NSF_PRESSURE_STIFFNESS, mode, f.bOut, S.p.get(), S.p.get(), -1, h->tol, &f);
+        infos[2] = launch_solve(h, NSF_PRESSURE_STIFFNESS, mode(NSF_PRESSURE_STIFFNESS), f.bOut, S.p.get(), S.p.get(), -1, h->tol, &f);
     }
     // velocity correction: M du = -dt Grad p per component with x0 = u, then u_out = du + u, Dirichlet re-imposed
     spmv_launch(h->mats[NSF_PRESSURE_DIVERGENCE], S.p.get(), S.rhsV.get(), s);
     for (int ch = 0; ch < 2; ++ch)
-        infos[3 + ch] = launch_solve(h, NSF_VELOCITY_MASS, mode, S.rhsV.get() + (size_t)ch * Nv,
+        infos[3 + ch] = launch_solve(h, NSF_VELOCITY_MASS, mode(NSF_VELOCITY_MASS), S.rhsV.get() + (size_t)ch * Nv,
                                      uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, -1, h->tol, nullptr);
     for (int ch = 0; ch < 2; ++ch)
         axpy_bc_launch(Nv, uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, S.bcV.get(), S.gV[ch].get(), s);
     std::swap(S.uv, S.tmp);
 }
+
+constexpr int kSolveSlot[5] = {NSF_DIFFUSION, NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS,
+                                NSF_VELOCITY_MASS};
 
 void run_steps(nsf_device* h, int nsteps, int* iterations) {
     sim_require(h);
@@ -239,6 +335,7 @@ void run_steps(nsf_device* h, int nsteps, int* iterations) {
             for (int j = 0; j < 5; ++j) {
                 const CgInfo& info = all[idx[(size_t)5 * k + j]];
                 if (iterations) iterations[(size_t)5 * (done + k) + j] = info.iterations;
+                if (info.fallback) h->mixedOff[kSolveSlot[j]] = true;   // FP32 cannot resolve this system
                 if (info.status != NSF_OK)
                     throw Error{info.status, "step " + std::to_string(done + k + 1) + ", " + names[j] + " solve: " +
                                                  status_text(info.status) + " after " +
@@ -437,21 +534,7 @@ int nsf_conjugate_gradient_f32(nsf_device* h, int slot, const float* b, const fl
 
 int nsf_upload_mesh(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure) {
     NSF_BEGIN(h)
-    if (nNodes <= 0 || nElements <= 0 || !xy || !elements) throw bad_arg("empty mesh");
-    if (nPressure <= 0 || nPressure > nNodes) throw bad_arg("pressure node count out of range");
-    for (int64_t k = 0; k < (int64_t)6 * nElements; ++k)
-        if (elements[k] < 0 || elements[k] >= nNodes) throw bad_arg("element references a node out of range");
-    for (int64_t k = 0; k < (int64_t)2 * nNodes; ++k)
-        if (!std::isfinite(xy[k])) throw bad_arg("non-finite node coordinate");
-    MeshDev& m = h->mesh;
-    m.nNodes = nNodes;
-    m.nEl = nElements;
-    m.nP = nPressure;
-    m.hxy.assign(xy, xy + 2 * (size_t)nNodes);
-    m.hel.assign(elements, elements + 6 * (size_t)nElements);
-    m.xy.upload((const float2*)xy, nNodes, h->stream);
-    m.el.upload(elements, 6 * (size_t)nElements, h->stream);
-    tree_build(m, h->stream);
+    upload_mesh_into(h->mesh, h->stream, nNodes, xy, nElements, elements, nPressure);
     h->sim.ready = false;
     NSF_END(h)
 }
@@ -518,80 +601,14 @@ int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, con
                   int nVelocityBC, const int* velocityBCNodes, const double* bcU, const double* bcV, int nPressureBC,
                   const int* pressureBCNodes, const double* bcP, double viscosity, double dt) {
     NSF_BEGIN(h)
-    if (!(dt > 0) || !(viscosity >= 0)) throw bad_arg("dt must be positive and viscosity non-negative");
-    if (nVelocityBC < 0 || nPressureBC < 0) throw bad_arg("negative boundary count");
-    if ((nVelocityBC > 0 && (!velocityBCNodes || !bcU || !bcV)) || (nPressureBC > 0 && (!pressureBCNodes || !bcP)))
-        throw bad_arg("null boundary array");
-    int st = nsf_upload_mesh(h, nNodes, xy, nElements, elements, nPressure);
-    if (st != NSF_OK) throw Error{st, h->lastError};
-    SimState& S = h->sim;
-    S.ready = false;
-    S.viscosity = viscosity;
-    S.dt = dt;
-    const int Nv = nNodes, P = nPressure;
-    cudaStream_t s = h->stream;
-    // Dirichlet data: mask, imposed value (last listed occurrence) and lift weight (sum over occurrences,
-    // because the reference subtracts the lift once per listed occurrence, include/assembly.h:505-523)
-    S.hbcV.assign(Nv, 0);
-    S.hbcP.assign(P, 0);
-    std::vector<double> gset[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
-    std::vector<double> glift[2] = {std::vector<double>(Nv, 0.0), std::vector<double>(Nv, 0.0)};
-    std::vector<double> gsetP(P, 0.0), gliftP(P, 0.0);
-    for (int k = 0; k < nVelocityBC; ++k) {
-        const int nd = velocityBCNodes[k];
-        if (nd < 0 || nd >= Nv) throw bad_arg("velocity Dirichlet node out of range");
-        S.hbcV[nd] = 1;
-        gset[0][nd] = bcU[k];
-        gset[1][nd] = bcV[k];
-        glift[0][nd] += bcU[k];
-        glift[1][nd] += bcV[k];
-    }
-    for (int k = 0; k < nPressureBC; ++k) {
-        const int nd = pressureBCNodes[k];
-        if (nd < 0 || nd >= P) throw bad_arg("pressure Dirichlet node out of range");
-        S.hbcP[nd] = 1;
-        gsetP[nd] = bcP[k];
-        gliftP[nd] += bcP[k];
-    }
-    S.bcV.upload(S.hbcV.data(), Nv, s);
-    S.bcP.upload(S.hbcP.data(), P, s);
-    for (int ch = 0; ch < 2; ++ch) {
-        S.hgV[ch] = gset[ch];
-        S.gV[ch].upload(gset[ch].data(), Nv, s);
-    }
-    S.hgP = gsetP;
-    S.gP.upload(gsetP.data(), P, s);
-    S.nColours = assemble_all(h, viscosity, dt);
-    // constant lift vectors: lift = W g (the Dirichlet data do not depend on time: the expressions see x, y only)
-    DevBuf<double> g;
-    for (int ch = 0; ch < 2; ++ch) {
-        g.upload(glift[ch].data(), Nv, s);
-        S.liftV[ch].alloc(Nv);
-        spmv_launch(h->mats[NSF_VELOCITY_LIFT], g.get(), S.liftV[ch].get(), s);
-        NSF_CUDA(cudaStreamSynchronize(s));
-    }
-    g.upload(gliftP.data(), P, s);
-    S.liftP.alloc(P);
-    spmv_launch(h->mats[NSF_PRESSURE_LIFT], g.get(), S.liftP.get(), s);
-    NSF_CUDA(cudaStreamSynchronize(s));
-    // fields: u = 0 with Dirichlet values (imposeVelocityDirichlet), p = 0
-    std::vector<double> uv0(2 * (size_t)Nv, 0.0);
-    for (int k = 0; k < nVelocityBC; ++k) {
-        uv0[velocityBCNodes[k]] = bcU[k];
-        uv0[velocityBCNodes[k] + (size_t)Nv] = bcV[k];
-    }
-    S.uv.upload(uv0.data(), uv0.size(), s);
-    S.tmp.alloc(2 * (size_t)Nv);
-    S.tmp.zero(s);
-    S.rhsV.alloc(2 * (size_t)Nv);
-    S.rhsP.alloc(P);
-    S.p.alloc(P);
-    S.p.zero(s);
-    ensure_workspace(h, std::max(Nv, P));
+    h->sim.ready = false;
+    setup_instance(h->mesh, h->sim, h->mats, h->stream, nNodes, xy, nElements, elements, nPressure, nVelocityBC,
+                   velocityBCNodes, bcU, bcV, nPressureBC, pressureBCNodes, bcP, viscosity, dt);
+    ensure_workspace(h, std::max(nNodes, nPressure));
     if (h->solverMode == NSF_SOLVER_MIXED)
-        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], s);
-    NSF_CUDA(cudaStreamSynchronize(s));
-    S.ready = true;
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], h->stream);
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    h->sim.ready = true;
     NSF_END(h)
 }
 
@@ -636,6 +653,134 @@ int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int 
     NSF_END(h)
 }
 
+int nsf_batch_clear(nsf_device* h) {
+    NSF_BEGIN(h)
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->batchGraphExec) { cudaGraphExecDestroy(h->batchGraphExec); h->batchGraphExec = nullptr; }
+    if (h->batchGraph) { cudaGraphDestroy(h->batchGraph); h->batchGraph = nullptr; }
+    h->batch.clear();
+    h->batchReady = false;
+    h->batchStepsDone = 0;
+    NSF_END(h)
+}
+
+int nsf_batch_add(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure,
+                  int nVelocityBC, const int* velocityBCNodes, const double* bcU, const double* bcV, int nPressureBC,
+                  const int* pressureBCNodes, const double* bcP, double viscosity, double dt, int* index) {
+    NSF_BEGIN(h)
+    if (h->batchReady) throw Error{NSF_ERR_STATE, "the batch is finalized; call nsf_batch_clear first"};
+    std::unique_ptr<Instance> in(new Instance());
+    setup_instance(in->mesh, in->sim, in->mats, h->stream, nNodes, xy, nElements, elements, nPressure, nVelocityBC,
+                   velocityBCNodes, bcU, bcV, nPressureBC, pressureBCNodes, bcP, viscosity, dt);
+    const size_t n = (size_t)std::max(nNodes, nPressure);
+    in->r.alloc(n);
+    in->q.alloc(n);
+    in->p0.alloc(n);
+    in->p1.alloc(n);
+    in->r32.alloc(n);
+    in->d32.alloc(n);
+    in->q32.alloc(n);
+    in->p32a.alloc(n);
+    in->p32b.alloc(n);
+    in->info.alloc((size_t)kStepInfoCap * 5);
+    in->info.zero(h->stream);
+    in->stepCounter.alloc(1);
+    in->stepCounter.zero(h->stream);
+    in->teamNs.alloc(1);
+    in->teamNs.zero(h->stream);
+    if (h->solverMode == NSF_SOLVER_MIXED)
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(in->mats[slot], h->stream);
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    in->sim.ready = true;
+    h->batch.push_back(std::move(in));
+    if (index) *index = (int)h->batch.size() - 1;
+    NSF_END(h)
+}
+
+int nsf_batch_finalize(nsf_device* h, int autotuneRounds) {
+    NSF_BEGIN(h)
+    if (h->batch.empty()) throw Error{NSF_ERR_STATE, "no instances added"};
+    h->batchCapacity = step_kernel_capacity(h->device);
+    if ((int)h->batch.size() > h->batchCapacity)
+        throw bad_arg("more instances than co-resident CTAs (" + std::to_string(h->batchCapacity) + ")");
+    for (auto& in : h->batch)
+        if (h->solverMode == NSF_SOLVER_MIXED)
+            for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(in->mats[slot], h->stream);
+    batch_autotune(h, std::max(0, autotuneRounds));
+    batch_capture_graph(h);
+    h->batchReady = true;
+    h->batchStepsDone = 0;
+    NSF_END(h)
+}
+
+int nsf_batch_step(nsf_device* h, int nsteps, int* iterations) {
+    NSF_BEGIN(h)
+    if (!h->batchReady) throw Error{NSF_ERR_STATE, "nsf_batch_finalize has not been called"};
+    if (nsteps < 0) throw bad_arg("nsteps must be >= 0");
+    const size_t n = h->batch.size();
+    std::vector<CgInfo> infos((size_t)kStepInfoCap * 5);
+    int done = 0;
+    while (done < nsteps) {
+        const int chunk = std::min(kStepInfoCap, nsteps - done);
+        for (int k = 0; k < chunk; ++k) {
+            NSF_CUDA(cudaGraphLaunch(h->batchGraphExec, h->stream));
+            count_launch();
+        }
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        static const char* names[5] = {"diffusion u", "diffusion v", "pressure", "mass u", "mass v"};
+        for (size_t i = 0; i < n; ++i) {
+            NSF_CUDA(cudaMemcpy(infos.data(), h->batch[i]->info.get(), sizeof(CgInfo) * infos.size(),
+                                cudaMemcpyDeviceToHost));
+            for (int k = 0; k < chunk; ++k) {
+                const int stepIdx = h->batchStepsDone + k;
+                const CgInfo* inf = &infos[(size_t)(stepIdx % kStepInfoCap) * 5];
+                for (int j = 0; j < 5; ++j) {
+                    if (iterations) iterations[((size_t)(done + k) * n + i) * 5 + j] = inf[j].iterations;
+                    if (inf[j].status != NSF_OK)
+                        throw Error{inf[j].status, "instance " + std::to_string(i) + ", step " +
+                                                       std::to_string(stepIdx + 1) + ", " + names[j] + " solve: " +
+                                                       status_text(inf[j].status)};
+                }
+            }
+        }
+        h->batchStepsDone += chunk;
+        done += chunk;
+    }
+    NSF_END(h)
+}
+
+int nsf_batch_get_fields(nsf_device* h, int index, double* uv, double* p) {
+    NSF_BEGIN(h)
+    if (index < 0 || index >= (int)h->batch.size()) throw bad_arg("instance index out of range");
+    const Instance& in = *h->batch[index];
+    if (uv) NSF_CUDA(cudaMemcpyAsync(uv, in.sim.uv.get(), sizeof(double) * in.sim.uv.n, cudaMemcpyDeviceToHost, h->stream));
+    if (p) NSF_CUDA(cudaMemcpyAsync(p, in.sim.p.get(), sizeof(double) * in.sim.p.n, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_batch_set_fields(nsf_device* h, int index, const double* uv, const double* p) {
+    NSF_BEGIN(h)
+    if (index < 0 || index >= (int)h->batch.size()) throw bad_arg("instance index out of range");
+    Instance& in = *h->batch[index];
+    if (uv) NSF_CUDA(cudaMemcpyAsync(in.sim.uv.get(), uv, sizeof(double) * in.sim.uv.n, cudaMemcpyHostToDevice, h->stream));
+    if (p) NSF_CUDA(cudaMemcpyAsync(in.sim.p.get(), p, sizeof(double) * in.sim.p.n, cudaMemcpyHostToDevice, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_batch_plan(nsf_device* h, int* blocks, int* gridBlocks, float* trialMs, int maxTrials, int* nTrials) {
+    NSF_BEGIN(h)
+    if (blocks)
+        for (size_t i = 0; i < h->batch.size(); ++i) blocks[i] = h->batch[i]->blocks;
+    if (gridBlocks) *gridBlocks = h->batchGrid;
+    const int nt = (int)h->autotuneMs.size();
+    if (nTrials) *nTrials = nt;
+    if (trialMs)
+        for (int k = 0; k < std::min(nt, maxTrials); ++k) trialMs[k] = (float)h->autotuneMs[k];
+    NSF_END(h)
+}
+
 int nsf_set_tolerance(nsf_device* h, double eps) {
     NSF_BEGIN(h)
     if (!(eps > 0)) throw bad_arg("tolerance must be positive");
@@ -648,6 +793,7 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
     if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
     if (innerTolerance > 0) h->innerTol = innerTolerance;
     h->solverMode = mode;
+    for (bool& off : h->mixedOff) off = false;
     if (mode == NSF_SOLVER_MIXED && h->sim.ready) {
         for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], h->stream);
         NSF_CUDA(cudaStreamSynchronize(h->stream));

@@ -279,11 +279,8 @@ __global__ void scale_kernel(int64_t n, double s, double* v) {
 
 static int blocks(int64_t n, int t) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + t - 1) / t, 152 * 64)); }
 
-// Builds every matrix of a mesh and the greedy element colouring; fills h->mats.  Returns the colour count.
-int assemble_all(nsf_device* h, double viscosity, double dt) {
-    MeshDev& m = h->mesh;
-    SimState& sim = h->sim;
-    cudaStream_t s = h->stream;
+// Builds every matrix of a mesh and the greedy element colouring into `mats`.  Returns the colour count.
+int assemble_instance(MeshDev& m, SimState& sim, Csr* mats, cudaStream_t s, double viscosity, double dt) {
     const int Nv = m.nNodes, P = m.nP, T = m.nEl;
     const int* el = m.hel.data();
     const std::vector<unsigned char>& bcV = sim.hbcV;
@@ -328,13 +325,13 @@ int assemble_all(nsf_device* h, double viscosity, double dt) {
     });
     HostCsr pG = build_pattern(2 * Nv, P, [&](int r, std::vector<int>& b) { nodesOf(r % Nv, 3, all, b, 0); });
 
-    upload_pattern(h->mats[NSF_VELOCITY_MASS], pM, s);
-    upload_pattern(h->mats[NSF_DIFFUSION], pD, s);
-    upload_pattern(h->mats[NSF_VELOCITY_LIFT], pWv, s);
-    upload_pattern(h->mats[NSF_PRESSURE_STIFFNESS], pK, s);
-    upload_pattern(h->mats[NSF_PRESSURE_LIFT], pWp, s);
-    upload_pattern(h->mats[NSF_VELOCITY_DIVERGENCE], pB, s);
-    upload_pattern(h->mats[NSF_PRESSURE_DIVERGENCE], pG, s);
+    upload_pattern(mats[NSF_VELOCITY_MASS], pM, s);
+    upload_pattern(mats[NSF_DIFFUSION], pD, s);
+    upload_pattern(mats[NSF_VELOCITY_LIFT], pWv, s);
+    upload_pattern(mats[NSF_PRESSURE_STIFFNESS], pK, s);
+    upload_pattern(mats[NSF_PRESSURE_LIFT], pWp, s);
+    upload_pattern(mats[NSF_VELOCITY_DIVERGENCE], pB, s);
+    upload_pattern(mats[NSF_PRESSURE_DIVERGENCE], pG, s);
 
     // greedy colouring in element order: no two elements of one colour share a node
     std::vector<unsigned long long> used(Nv, 0ull);
@@ -371,9 +368,9 @@ int assemble_all(nsf_device* h, double viscosity, double dt) {
     a.bcV = sim.bcV.get();
     a.bcP = sim.bcP.get();
     auto bind = [&](int slot, const int*& rp, const int*& col, double*& val) {
-        rp = h->mats[slot].rowptr.get();
-        col = h->mats[slot].col.get();
-        val = h->mats[slot].val.get();
+        rp = mats[slot].rowptr.get();
+        col = mats[slot].col.get();
+        val = mats[slot].val.get();
     };
     bind(NSF_VELOCITY_MASS, a.mRp, a.mCol, a.mVal);
     bind(NSF_DIFFUSION, a.dRp, a.dCol, a.dVal);
@@ -394,8 +391,8 @@ int assemble_all(nsf_device* h, double viscosity, double dt) {
     }
     bc_diagonal_kernel<<<blocks(Nv, 256), 256, 0, s>>>(Nv, sim.bcV.get(), a.dRp, a.dVal);
     bc_diagonal_kernel<<<blocks(P, 256), 256, 0, s>>>(P, sim.bcP.get(), a.kRp, a.kVal);
-    Csr& Bd = h->mats[NSF_VELOCITY_DIVERGENCE];
-    Csr& Gd = h->mats[NSF_PRESSURE_DIVERGENCE];
+    Csr& Bd = mats[NSF_VELOCITY_DIVERGENCE];
+    Csr& Gd = mats[NSF_PRESSURE_DIVERGENCE];
     scale_kernel<<<blocks(Bd.nnz, 256), 256, 0, s>>>(Bd.nnz, -(1.0 / dt), Bd.val.get());
     scale_kernel<<<blocks(Gd.nnz, 256), 256, 0, s>>>(Gd.nnz, -dt, Gd.val.get());
     NSF_CUDA(cudaGetLastError());

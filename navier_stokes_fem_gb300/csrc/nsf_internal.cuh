@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdarg>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -86,8 +87,8 @@ struct Csr {
 struct CgInfo {
     int iterations;      // inner iterations in total
     int status;          // nsf_status
-    int outer;           // refinement sweeps (mixed precision), 1 for the FP64 solver
-    int pad;
+    int outer;           // FP64 true-residual refreshes (mixed precision), 1 for the FP64 solver
+    int fallback;        // 1: the mixed solver stalled and finished with the FP64 method
     double rr;           // final ||r||^2 (recursive residual; FP64 true residual for the mixed solver)
     double bb;           // ||b||^2
 };
@@ -199,6 +200,32 @@ struct SimState {
     int nColours = 0;
 };
 
+// One mesh instance of the batched form: its mesh and tree, matrices, fields and CG workspace.
+struct Instance {
+    MeshDev mesh;
+    Csr mats[NSF_SLOT_COUNT];
+    SimState sim;
+    DevBuf<double> r, q, p0, p1;
+    DevBuf<float> r32, d32, q32, p32a, p32b;
+    DevBuf<double> partials;                 // 6 slots per CTA of the team
+    DevBuf<CgInfo> info;                     // ring of kStepInfoCap steps x 5 solves
+    DevBuf<int> stepCounter;
+    DevBuf<unsigned long long> teamNs;       // duration of the team's last step (autotuner input)
+    int blocks = 1;                          // team size (CTAs) in the current plan
+    double work = 1.0;                       // autotuner's work estimate
+};
+constexpr int kStepInfoCap = 64;
+
+// The persistent step kernel (nsf_step.cu)
+int step_kernel_capacity(int device);
+
+// Assembles every matrix of one mesh on the GPU (nsf_assembly.cu); returns the colour count.
+int assemble_instance(MeshDev& m, SimState& sim, Csr* mats, cudaStream_t s, double viscosity, double dt);
+// Upload, tree, BC data, assembly, lifts and initial fields of one instance (nsf_api.cu).
+void setup_instance(MeshDev& m, SimState& S, Csr* mats, cudaStream_t s, int nNodes, const float* xy, int nElements,
+                    const int* elements, int nPressure, int nU, const int* uNodes, const double* gu, const double* gv,
+                    int nPb, const int* pNodes, const double* gp, double viscosity, double dt);
+
 }  // namespace nsf
 
 // the opaque handle behind the C ABI
@@ -216,9 +243,10 @@ struct nsf_device {
     nsf::DevBuf<unsigned char> flush; // L2 eviction buffer (nsf_flush_l2)
     unsigned flushToggle = 0;
     double tol = 1e-8;
-    double innerTol = 1e-4;
+    double innerTol = 0.1;   // mixed precision: FP32 residual reduction between FP64 true residuals
     long long timeoutNs = 2000000000LL;
     int solverMode = NSF_SOLVER_FP64;
+    bool mixedOff[NSF_SLOT_COUNT] = {};   // systems whose mixed solve stalled once: solved in FP64 from then on
     // per-solve records (profiling of the persistent CG kernels)
     bool profile = false;
     std::vector<cudaEvent_t> evPool;
@@ -226,4 +254,24 @@ struct nsf_device {
     struct SolveRecord { int slot; int mode; int rows; int64_t nnz; cudaEvent_t a, b; int infoIndex; };
     std::vector<SolveRecord> records;
     int infoCursor = 0;
+    // batched form: instances, the launch plan and the captured step graph
+    std::vector<std::unique_ptr<nsf::Instance>> batch;
+    nsf::DevBuf<unsigned char> batchDesc;    // StepInstance array (nsf_step.cu)
+    nsf::DevBuf<int> batchBlockInst;
+    nsf::DevBuf<nsf::GridSync> batchSync;
+    int batchGrid = 0;
+    int batchCapacity = 0;                   // co-resident CTAs of the step kernel
+    bool batchReady = false;
+    cudaGraph_t batchGraph = nullptr;
+    cudaGraphExec_t batchGraphExec = nullptr;
+    int batchStepsDone = 0;
+    std::vector<int> autotuneLog;            // team sizes tried, flattened per round
+    std::vector<double> autotuneMs;          // step time of each round
 };
+
+namespace nsf {
+void batch_upload_plan(nsf_device* h);
+void batch_launch_step(nsf_device* h);
+void batch_autotune(nsf_device* h, int rounds);
+void batch_capture_graph(nsf_device* h);
+}  // namespace nsf

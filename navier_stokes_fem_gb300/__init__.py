@@ -475,15 +475,23 @@ class BatchedNavierStokes(GPUSimulationDevice):
         self._check(library().nsf_batch_step(self._h, int(n), it.ctypes.data_as(_v)))
         return it[: n * self.count * 5].reshape(n, self.count, 5)
 
+    def _index(self, index: int) -> int:
+        if not 0 <= int(index) < self.count:
+            raise NSFemError(5, f"instance index {index} out of range [0, {self.count})")
+        return int(index)
+
     def fields(self, index: int):
-        nv, npr = self.sizes[index]
+        nv, npr = self.sizes[self._index(index)]
         uv, p = np.zeros(2 * nv), np.zeros(npr)
         self._check(library().nsf_batch_get_fields(self._h, int(index), uv.ctypes.data_as(_v), p.ctypes.data_as(_v)))
         return uv, p
 
     def set_fields(self, index: int, uv, p):
+        nv, npr = self.sizes[self._index(index)]
         uv = np.ascontiguousarray(uv, np.float64)
         p = np.ascontiguousarray(p, np.float64)
+        if uv.size != 2 * nv or p.size != npr:
+            raise NSFemError(5, "field sizes do not match the instance")
         self._check(library().nsf_batch_set_fields(self._h, int(index), uv.ctypes.data_as(_v), p.ctypes.data_as(_v)))
 
     def plan(self):

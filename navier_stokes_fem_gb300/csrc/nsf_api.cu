@@ -186,6 +186,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.col = A.col.get();
     a.val = A.val.get();
     a.val32 = A.val32.get();
+    a.rowsum32 = A.rowsum32.get();
     a.b = b;
     a.x0 = x0;
     a.x = x;

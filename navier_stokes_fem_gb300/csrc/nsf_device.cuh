@@ -119,7 +119,12 @@ __device__ __forceinline__ void team_rows(int n, const Team& t, int& rb, int& re
 // warp).  Each lane then sums its own row in entry order with one fused multiply-add per non-zero - on GB300 the
 // FP64 pipe (about 2 DFMA per cycle per SM) is as tight as HBM, so no other FP64 work is done per non-zero.
 // gather(c) yields the vector entry of column c; epi(row, sum) runs on the lane owning `row`.
-template <typename TV, typename TA, typename Gather, typename Epi>
+// With Diff = true the product is taken in difference form, sum_j a_ij (x_j - x_i): the lane subtracts its own
+// row's entry before multiplying (the diagonal term vanishes), and epi adds rowsum_i * x_i.  For matrices whose
+// rows sum to (almost) zero - stiffness matrices - this removes the catastrophic cancellation of the plain sum on
+// smooth vectors, so an FP32 product stays accurate on the smallest eigenmodes; and because the rounded operator
+// keeps the exact row sums, its rounding error annihilates constants.
+template <typename TV, typename TA, bool Diff = false, typename Gather, typename Epi>
 __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const int* __restrict__ col,
                                           const TV* __restrict__ val, int rb, int re, TA* stage, Gather gather,
                                           Epi epi) {
@@ -135,6 +140,7 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
         const int sNext = __shfl_down_sync(0xffffffffu, s, 1);
         const int e = lane + 1 < nrows ? sNext : cEnd;
         const int cBeg = __shfl_sync(0xffffffffu, s, 0);
+        const TA self = (Diff && own) ? gather(row) : TA(0);
         TA acc = TA(0);
         for (int base = cBeg; base < cEnd; base += kStage) {
             const int cnt = min(kStage, cEnd - base);
@@ -158,7 +164,10 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
             __syncwarp();
             if (own) {
                 const int a0 = max(s, base), a1 = min(e, base + cnt);
-                for (int k = a0; k < a1; ++k) acc = fma(sv[k - base], sg[k - base], acc);
+                if (Diff)
+                    for (int k = a0; k < a1; ++k) acc = fma(sv[k - base], sg[k - base] - self, acc);
+                else
+                    for (int k = a0; k < a1; ++k) acc = fma(sv[k - base], sg[k - base], acc);
             }
             __syncwarp();
         }
@@ -381,14 +390,16 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             float* pc = pcur;
             const float* r32 = a.r32;
             double pq = 0;
-            warp_spmv<float, float>(a.rowptr, a.col, a.val32, rb, re, stage32,
-                                    [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                                    [&](int row, float acc) {
-                                        const float pi = fmaf(betaf, pp[row], r32[row]);
-                                        pc[row] = pi;
-                                        a.q32[row] = acc;
-                                        pq = fma((double)pi, (double)acc, pq);
-                                    });
+            // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv)
+            warp_spmv<float, float, true>(a.rowptr, a.col, a.val32, rb, re, stage32,
+                                          [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+                                          [&](int row, float acc) {
+                                              const float pi = fmaf(betaf, pp[row], r32[row]);
+                                              acc = fmaf(a.rowsum32[row], pi, acc);
+                                              pc[row] = pi;
+                                              a.q32[row] = acc;
+                                              pq = fma((double)pi, (double)acc, pq);
+                                          });
             pq = block_sum(pq, smem);
             if (threadIdx.x == 0) a.partials[t.rank] = pq;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }

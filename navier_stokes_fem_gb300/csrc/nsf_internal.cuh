@@ -79,6 +79,7 @@ struct Csr {
     DevBuf<int> rowptr, col;
     DevBuf<double> val;
     DevBuf<float> val32;
+    DevBuf<float> rowsum32;   // FP64 row sums rounded to FP32 (the difference-form FP32 product)
     bool has32 = false;
     bool valid() const { return rows > 0 && rowptr.ptr != nullptr; }
 };
@@ -107,6 +108,7 @@ struct CgArgs {
     const int* col;
     const double* val;
     const float* val32;
+    const float* rowsum32;   // row sums of the FP64 matrix, rounded once (mixed precision difference form)
     const double* b;
     const double* x0;
     double* x;

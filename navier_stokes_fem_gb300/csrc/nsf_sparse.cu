@@ -56,6 +56,16 @@ __global__ void to_fp32_kernel(int64_t n, const double* __restrict__ a, float* _
         b[i] = (float)a[i];
 }
 
+// FP64 row sums, rounded once to FP32: the diagonal term of the difference-form FP32 product
+__global__ void rowsum_kernel(int rows, const int* __restrict__ rowptr, const double* __restrict__ val,
+                              float* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k];
+        out[i] = (float)s;
+    }
+}
+
 static int grid_for(int64_t work, int threads) {
     int64_t g = (work + threads - 1) / threads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
@@ -87,6 +97,10 @@ void make_fp32_values(Csr& A, cudaStream_t s) {
     if (A.has32) return;
     A.val32.alloc((size_t)A.nnz);
     to_fp32_kernel<<<grid_for(A.nnz, 256), 256, 0, s>>>(A.nnz, A.val.get(), A.val32.get());
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+    A.rowsum32.alloc((size_t)A.rows);
+    rowsum_kernel<<<grid_for(A.rows, 256), 256, 0, s>>>(A.rows, A.rowptr.get(), A.val.get(), A.rowsum32.get());
     NSF_CUDA(cudaGetLastError());
     count_launch();
     A.has32 = true;

@@ -26,6 +26,7 @@ struct CsrView {
     const int* col;
     const double* val;
     const float* val32;
+    const float* rowsum32;
 };
 
 struct StepInstance {
@@ -60,6 +61,7 @@ __device__ __forceinline__ CgArgs solve_args(const StepInstance& I, const StepPa
     a.col = A.col;
     a.val = A.val;
     a.val32 = A.val32;
+    a.rowsum32 = A.rowsum32;
     a.r = I.r;
     a.q = I.q;
     a.pbuf0 = I.p0;
@@ -191,7 +193,9 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
 // ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
-static CsrView view(const Csr& A) { return CsrView{A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get()}; }
+static CsrView view(const Csr& A) {
+    return CsrView{A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.rowsum32.get()};
+}
 
 int step_kernel_capacity(int device) {
     int sms = 0, occ = 0;

@@ -289,7 +289,11 @@ def run_gpu(args):
     # roofline of the dominant kernel: the persistent CG solver, over every launch in the timed region
     bytes_total = 0.0
     for m_, n_, z_, i_, o_ in zip(prof["mode"], prof["rows"], prof["nnz"], prof["iterations"], prof["outer"]):
-        bytes_total += algorithmic_bytes(int(m_), int(n_), int(z_), int(i_), int(o_))
+        bytes_total += algorithmic_bytes(min(int(m_), 1), int(n_), int(z_), int(i_), int(o_))
+    mixed_stats = {"mixed_solves": int((prof["mode"] >= 1).sum()),
+                   "finished_in_fp64": int((prof["mode"] == 2).sum()),
+                   "mean_fp64_refreshes": round(float(prof["outer"][prof["mode"] >= 1].mean()), 2)
+                   if (prof["mode"] >= 1).any() else 0}
     cg_ms = float(np.sum(prof["ms"]))
     peak, peak_kind = peaks()
     achieved = bytes_total / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else 0.0
@@ -326,6 +330,7 @@ def run_gpu(args):
         "config": config_block(args, w, mesh, args.solver),
         "cg_iterations_per_step": its.mean(axis=0).round(1).tolist(),
         "cg_solves": ["diffusion u", "diffusion v", "pressure", "mass u", "mass v"],
+        "mixed_precision": mixed_stats if args.solver == "mixed" else None,
         "setup_s": round(setup_s, 3),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",

@@ -153,7 +153,8 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);
 int nsf_set_barrier_timeout(nsf_device* h, double seconds);
 /* Records CUDA events around every persistent CG launch while enabled (clears previous records). */
 int nsf_profile(nsf_device* h, int enable);
-/* Returns the number of records written (<= maxRecords). */
+/* Returns the number of records written (<= maxRecords).  mode: 0 FP64, 1 mixed, 2 mixed that stalled and finished
+ * with the FP64 method; outer: FP64 true-residual refreshes of a mixed solve. */
 int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* rows, int64_t* nnz, int* iterations,
                      int* outer, float* ms);
 /* op 0 records a start event on the handle's stream, op 1 a stop event and writes the elapsed ms. */

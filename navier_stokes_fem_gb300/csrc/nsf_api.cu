@@ -833,7 +833,7 @@ int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* r
             float t = 0;
             NSF_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
             if (slot) slot[i] = r.slot;
-            if (mode) mode[i] = r.mode;
+            if (mode) mode[i] = all[r.infoIndex].fallback ? 2 : r.mode;
             if (rows) rows[i] = r.rows;
             if (nnz) nnz[i] = r.nnz;
             if (iterations) iterations[i] = all[r.infoIndex].iterations;

@@ -10,6 +10,14 @@ constexpr int kWarps = kCgThreads / 32;
 constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 
+// TMA bulk-copy pipeline of the streamed SpMV: kPipe stages, each a contiguous slice of the CTA's column
+// indices and values (kStreamBytes per stage).  The dynamic shared memory of every CG kernel is kPipe stages
+// (the warp-chunked SpMV's staging area reuses the same bytes in other phases).
+constexpr int kPipe = 3;
+constexpr int kStreamBytes = 32768;
+constexpr int kDynSmem = kPipe * kStreamBytes;
+static_assert(kWarps * 2 * kStage * (int)sizeof(double) <= kDynSmem, "staging area must fit the stream buffers");
+
 // ---------------------------------------------------------------------------------------------------
 // memory-model and timing helpers
 // ---------------------------------------------------------------------------------------------------
@@ -175,6 +183,201 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
     }
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Streamed SpMV: the CTA's column indices and values arrive in shared memory through TMA bulk copies
+// (cp.async.bulk, completion on an mbarrier), kPipe stages in flight, so the matrix stream needs no registers
+// and no dependent loads; threads only read row pointers, gather the vector and sum from shared memory.
+// ---------------------------------------------------------------------------------------------------
+template <typename TV> __host__ __device__ constexpr int stream_entries() {
+    return (int)((kStreamBytes / (4 + sizeof(TV))) / 4) * 4;
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Per-CTA state of the copy pipeline; `seq` counts stages over the whole kernel so every buffer's mbarrier
+// phase is known without extra state.
+struct Stream {
+    unsigned long long* bar;   // kPipe mbarriers (shared)
+    unsigned char* buf;        // kPipe * kStreamBytes (dynamic shared)
+    int* ctl;                  // 2 shared ints: next stage's first row, abort
+    double* carry;             // 1 shared double: partial sum of a row that continues into the next stage
+    unsigned seq;
+    long long timeoutNs;
+
+    __device__ void init() {
+        if (threadIdx.x == 0) {
+            for (int i = 0; i < kPipe; ++i) mbar_init(bar + i, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        seq = 0;
+        __syncthreads();
+    }
+};
+
+// Shared memory of a CG kernel: `smem` (reduction slots), the copy pipeline `st` over the kDynSmem dynamic bytes,
+// and `stage`, the warp-chunked SpMV's staging area on the same bytes.  Launch with kDynSmem dynamic bytes.
+#define NSF_KERNEL_SHARED(timeout)                                                        \
+    extern __shared__ __align__(128) unsigned char nsf_dyn[];                              \
+    __shared__ double smem[33];                                                            \
+    __shared__ unsigned long long nsf_bars[kPipe];                                         \
+    __shared__ int nsf_ctl[2];                                                             \
+    __shared__ double nsf_carry[2];                                                        \
+    Stream st{nsf_bars, nsf_dyn, nsf_ctl, nsf_carry, 0u, (timeout)};                       \
+    st.init();                                                                             \
+    double* stage = reinterpret_cast<double*>(nsf_dyn)
+
+// Issue the copies of one stage: entries [c0, c1) of col and val (c0 a multiple of 4, c1 - c0 a multiple of 4).
+template <typename TV>
+__device__ __forceinline__ void stream_issue(Stream& st, unsigned slot, const int* col, const TV* val, int c0, int c1) {
+    constexpr int S = stream_entries<TV>();
+    unsigned char* base = st.buf + (size_t)slot * kStreamBytes;
+    const unsigned n = (unsigned)(c1 - c0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(st.bar + slot, n * (unsigned)(4 + sizeof(TV)));
+    bulk_g2s(base, col + c0, n * 4u, st.bar + slot);
+    bulk_g2s(base + (size_t)S * 4, val + c0, n * (unsigned)sizeof(TV), st.bar + slot);
+}
+
+// Rows [rb, re) of this CTA: epi(row, sum) for every row, sum = sum_j a_ij gather(j) (or the difference form with
+// Diff, see warp_spmv).  Returns false if a copy did not complete within the time limit.
+template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
+__device__ bool stream_spmv(Stream& st, const int* __restrict__ rowptr, const int* __restrict__ col,
+                            const TV* __restrict__ val, int nnzTotal, int rb, int re, Gather gather, Epi epi) {
+    constexpr int S = stream_entries<TV>();
+    if (rb >= re) return true;
+    const int E0 = rowptr[rb], E1 = rowptr[re];
+    const int base0 = E0 & ~3;
+    // Bulk copies need 16-byte aligned sources: with an unaligned col or val (a caller's sub-allocation) every
+    // entry is read directly.  Entries past the last multiple of 4 are always read directly.
+    const bool aligned = ((reinterpret_cast<unsigned long long>(col) | reinterpret_cast<unsigned long long>(val)) &
+                          15ULL) == 0;
+    const int copyLimit = aligned ? (nnzTotal & ~3) : 0;
+    const int nst = (E1 - base0 + S - 1) / S;
+    auto copy_range = [&](int s, int& c0, int& c1) {
+        c0 = base0 + s * S;
+        c1 = min(c0 + S, min((E1 + 3) & ~3, copyLimit));
+        if (c1 < c0) c1 = c0;
+    };
+    // the buffers were last written through the generic proxy (staging of other phases): order those writes
+    // before the copies that overwrite them
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    // prologue: stages 0 .. kPipe-2
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kPipe - 1 && s < nst; ++s) {
+            int c0, c1;
+            copy_range(s, c0, c1);
+            if (c1 > c0) stream_issue<TV>(st, (st.seq + s) % kPipe, col, val, c0, c1);
+            else mbar_expect_tx(st.bar + (st.seq + s) % kPipe, 0);
+        }
+        st.ctl[0] = rb;
+        st.ctl[1] = rb;   // stays put through a stage that no row touches (E0 == E1)
+        st.carry[0] = 0.0;
+    }
+    __syncthreads();
+    bool ok = true;
+    int s = 0;
+    for (; s < nst; ++s) {
+        const unsigned g = st.seq + s, slot = g % kPipe, parity = (g / kPipe) & 1;
+        if (threadIdx.x == 0 && s + kPipe - 1 < nst) {   // refill the buffer freed by stage s-1
+            int c0, c1;
+            copy_range(s + kPipe - 1, c0, c1);
+            const unsigned sl = (g + kPipe - 1) % kPipe;
+            if (c1 > c0) stream_issue<TV>(st, sl, col, val, c0, c1);
+            else mbar_expect_tx(st.bar + sl, 0);
+        }
+        // wait for this stage (bounded)
+        {
+            const long long t0 = global_ns();
+            while (!mbar_test(st.bar + slot, parity)) {
+                if (global_ns() - t0 > st.timeoutNs) { ok = false; break; }
+            }
+        }
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+        int c0, c1;
+        copy_range(s, c0, c1);
+        const int ws = max(E0, base0 + s * S), we = min(E1, base0 + (s + 1) * S);
+        const int* colS = reinterpret_cast<const int*>(st.buf + (size_t)slot * kStreamBytes);
+        const TV* valS = reinterpret_cast<const TV*>(st.buf + (size_t)slot * kStreamBytes + (size_t)S * 4);
+        const int first = st.ctl[0];
+        for (int r = first + (int)threadIdx.x; r < re; r += blockDim.x) {
+            const int rs = rowptr[r];
+            if (rs >= we) break;
+            const int rend = rowptr[r + 1];
+            const int a0 = max(rs, ws), a1 = min(rend, we);
+            const TA self = Diff ? gather(r) : TA(0);
+            TA acc = (r == first && rs < ws) ? (TA)st.carry[0] : TA(0);
+            for (int e = a0; e < a1; ++e) {
+                int c;
+                TV v;
+                if (e < c1) { c = colS[e - c0]; v = valS[e - c0]; }
+                else { c = col[e]; v = val[e]; }            // the last few entries of the matrix (alignment)
+                if (Diff) acc = fma(TA(v), gather(c) - self, acc);
+                else acc = fma(TA(v), gather(c), acc);
+            }
+            if (rend > we) {                  // continues in the next stage
+                st.carry[1] = (double)acc;
+                st.ctl[1] = r;
+            } else {
+                epi(r, acc);
+                if (rend == we) st.ctl[1] = r + 1;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st.ctl[0] = st.ctl[1];
+            st.carry[0] = st.carry[1];
+        }
+        // the next iteration's refill (thread 0) targets the buffer this stage used: everyone is done with it
+        __syncthreads();
+    }
+    if (!ok) {
+        // a copy did not land in time: before the CTA leaves, wait (bounded again) for the stages still in flight,
+        // s .. min(nst, s + kPipe) - 1, so that no copy writes into shared memory after the kernel ends
+        if (threadIdx.x == 0) {
+            const int last = min(nst, s + kPipe);
+            for (int k = s; k < last; ++k) {
+                const unsigned g = st.seq + k;
+                const long long t0 = global_ns();
+                while (!mbar_test(st.bar + g % kPipe, (g / kPipe) & 1))
+                    if (global_ns() - t0 > st.timeoutNs) break;
+            }
+        }
+        __syncthreads();
+        return false;
+    }
+    st.seq += (unsigned)nst;
+    {           // rows without entries after the last non-zero of the range (none in assembled matrices)
+        for (int r = st.ctl[0] + (int)threadIdx.x; r < re; r += blockDim.x)
+            if (rowptr[r] == E1) epi(r, TA(0));
+        __syncthreads();
+    }
+    return ok;
+}
+
 static __device__ void write_info(const Team& t, const CgArgs& a, int it, int status, int outer, double rr, double bb) {
     if (t.rank == 0 && threadIdx.x == 0) {
         a.info->iterations = it;
@@ -184,6 +387,21 @@ static __device__ void write_info(const Team& t, const CgArgs& a, int it, int st
         a.info->rr = rr;
         a.info->bb = bb;
     }
+}
+
+// A matrix copy that did not land in time: raise the team's abort word (its other CTAs leave at their next
+// barrier) and report the timeout status.
+static __device__ int stream_timeout(const Team& t, const CgArgs& a, int it, int outer, double rr, double bb) {
+    if (threadIdx.x == 0) atomicExch(&t.sync->abort, 1);
+    if (threadIdx.x == 0 && t.rank == 0) {
+        a.info->iterations = it;
+        a.info->status = NSF_ERR_BARRIER_TIMEOUT;
+        a.info->outer = outer;
+        a.info->fallback = 0;
+        a.info->rr = rr;
+        a.info->bb = bb;
+    }
+    return NSF_ERR_BARRIER_TIMEOUT;
 }
 
 // b for this block's rows: the given vector, or the fused right-hand side mask ? g : (B x_b) - lift, stored
@@ -203,8 +421,9 @@ static __device__ void build_rhs(const CgArgs& a, int rb, int re, double* stage)
 // FP64 persistent CG
 // partial regions: 0 = p.q, 1 = r.r, 2 = r0.r0, 3 = b.b
 // ---------------------------------------------------------------------------------------------------
-static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
+static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem, Stream& st) {
     const int G = t.size;
+    const int nnzTotal = a.rowptr[a.n];
     int rb, re;
     team_rows(a.n, t, rb, re);
     const double* b = a.bRowptr ? a.bOut : a.b;
@@ -236,13 +455,15 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     double* p = a.pbuf0;
     const int bs = blockDim.x;
     while (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
-        // phase A: q = A p, partial p.q
+        // phase A: q = A p (streamed matrix), partial p.q
         double pq = 0;
-        warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return p[c]; },
-                                  [&](int row, double acc) {
-                                      a.q[row] = acc;
-                                      pq = fma(p[row], acc, pq);
-                                  });
+        const bool copied = stream_spmv<double, double, false>(st, a.rowptr, a.col, a.val, nnzTotal, rb, re,
+                                                              [&](int c) { return p[c]; },
+                                                              [&](int row, double acc) {
+                                                                  a.q[row] = acc;
+                                                                  pq = fma(p[row], acc, pq);
+                                                              });
+        if (!copied) return stream_timeout(t, a, it, 1, rr, bb);
         pq = block_sum(pq, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(2)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
@@ -310,7 +531,8 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 // saves the third barrier of the FP64 kernel.
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
-static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
+static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, Stream& st) {
+    const int nnzTotal = a.rowptr[a.n];
     float* stage32 = reinterpret_cast<float*>(stage);
     const int G = t.size;
     int rb, re;
@@ -391,15 +613,16 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             const float* r32 = a.r32;
             double pq = 0;
             // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv)
-            warp_spmv<float, float, true>(a.rowptr, a.col, a.val32, rb, re, stage32,
-                                          [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                                          [&](int row, float acc) {
-                                              const float pi = fmaf(betaf, pp[row], r32[row]);
-                                              acc = fmaf(a.rowsum32[row], pi, acc);
-                                              pc[row] = pi;
-                                              a.q32[row] = acc;
-                                              pq = fma((double)pi, (double)acc, pq);
-                                          });
+            const bool copied = stream_spmv<float, float, true>(st, a.rowptr, a.col, a.val32, nnzTotal, rb, re,
+                                                                [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+                                                                [&](int row, float acc) {
+                                                                    const float pi = fmaf(betaf, pp[row], r32[row]);
+                                                                    acc = fmaf(a.rowsum32[row], pi, acc);
+                                                                    pc[row] = pi;
+                                                                    a.q32[row] = acc;
+                                                                    pq = fma((double)pi, (double)acc, pq);
+                                                                });
+            if (!copied) return stream_timeout(t, a, it, refresh, rr64, bb);
             pq = block_sum(pq, smem);
             if (threadIdx.x == 0) a.partials[t.rank] = pq;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
@@ -451,14 +674,14 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
         f.b = b;
         f.x0 = a.x;
         f.maxIt = a.maxIt - it;
-        const int st = team_cg_fp64(t, f, stage, smem);
-        if (st == NSF_ERR_BARRIER_TIMEOUT) return st;
+        const int fst = team_cg_fp64(t, f, stage, smem, st);
+        if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
             a.info->iterations += it;
             a.info->outer = refresh;
             a.info->fallback = 1;   // finished in FP64
         }
-        return st;
+        return fst;
     }
     write_info(t, a, it, status, refresh, rr64, bb);
     return status;

@@ -81,14 +81,13 @@ __device__ __forceinline__ CgArgs solve_args(const StepInstance& I, const StepPa
     return a;
 }
 
-__device__ __forceinline__ int run_cg(Team& t, const CgArgs& a, int mode, double* stage, double* smem) {
-    return mode == NSF_SOLVER_MIXED ? team_cg_mixed(t, a, stage, smem) : team_cg_fp64(t, a, stage, smem);
+__device__ __forceinline__ int run_cg(Team& t, const CgArgs& a, int mode, double* stage, double* smem, Stream& st) {
+    return mode == NSF_SOLVER_MIXED ? team_cg_mixed(t, a, stage, smem, st) : team_cg_fp64(t, a, stage, smem, st);
 }
 
 __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance* __restrict__ insts,
                                                              const int* __restrict__ blockInst, StepParams sp) {
-    __shared__ double smem[33];
-    __shared__ double stage[kWarps * 2 * kStage];
+    NSF_KERNEL_SHARED(sp.timeoutNs);
     const StepInstance& I = insts[blockInst[blockIdx.x]];
     Team t{I.sync, I.partials, I.nBlocks, (int)blockIdx.x - I.firstBlock, 0ULL, sp.timeoutNs};
     const long long t0 = global_ns();
@@ -143,7 +142,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.tmp + (size_t)ch * Nv;
         a.x = I.uv + (size_t)ch * Nv;
         a.info = info + ch;
-        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // pressure: Kp p = -(1/dt) Div u - lift, pinned nodes -> g; x0 = p
     {
@@ -160,7 +159,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.p;
         a.x = I.p;
         a.info = info + 2;
-        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // velocity correction: M du = (-dt Grad p) per component, x0 = u; the right-hand side is built from the
     // gradient rows of the component (row offset ch*Nv) inside the solve
@@ -175,7 +174,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.uv + (size_t)ch * Nv;
         a.x = I.tmp + (size_t)ch * Nv;
         a.info = info + 3 + ch;
-        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // u <- du + u with the Dirichlet values re-imposed (include/assembly.h:686-707), in place
     team_rows(Nv, t, rb, re);
@@ -200,7 +199,8 @@ static CsrView view(const Csr& A) {
 int step_kernel_capacity(int device) {
     int sms = 0, occ = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_kernel, kCgThreads, 0));
+    NSF_CUDA(cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_kernel, kCgThreads, kDynSmem));
     return sms * std::min(occ, 2);
 }
 
@@ -275,7 +275,7 @@ void batch_launch_step(nsf_device* h) {
     const StepInstance* desc = reinterpret_cast<const StepInstance*>(h->batchDesc.get());
     const int* bi = h->batchBlockInst.get();
     void* params[] = {(void*)&desc, (void*)&bi, (void*)&sp};
-    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)step_kernel, dim3(h->batchGrid), dim3(kCgThreads), params, 0,
+    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)step_kernel, dim3(h->batchGrid), dim3(kCgThreads), params, kDynSmem,
                                          h->stream));
     count_launch();
 }

@@ -174,7 +174,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     Csr& A = h->mats[slot];
     if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
     if (A.rows != A.cols) throw bad_arg("CG needs a square matrix");
-    if (mode == NSF_SOLVER_MIXED) make_fp32_values(A, h->stream);
+    prepare_matrix(A, mode == NSF_SOLVER_MIXED, h->stream);
     ensure_workspace(h, A.rows);
     CgWorkspace& ws = h->ws;
     const int infoIndex = h->infoCursor;
@@ -187,6 +187,10 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.val = A.val.get();
     a.val32 = A.val32.get();
     a.rowsum32 = A.rowsum32.get();
+    a.sellStart = A.sellStart.get();
+    a.sellCol = A.sellCol.get();
+    a.sellVal = A.sellVal.get();
+    a.sellVal32 = A.sellVal32.get();
     a.b = b;
     a.x0 = x0;
     a.x = x;
@@ -254,8 +258,7 @@ void upload_csr(nsf_device* h, int slot, int rows, int cols, int64_t nnz, const 
     A.rowptr.upload(rowptr, rows + 1, h->stream);
     A.col.upload(col, std::max<int64_t>(nnz, 0), h->stream);
     A.val.upload(val, std::max<int64_t>(nnz, 0), h->stream);
-    A.has32 = false;
-    A.val32.release();
+    A.values_changed();
     NSF_CUDA(cudaStreamSynchronize(h->stream));
 }
 
@@ -606,8 +609,8 @@ int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, con
     setup_instance(h->mesh, h->sim, h->mats, h->stream, nNodes, xy, nElements, elements, nPressure, nVelocityBC,
                    velocityBCNodes, bcU, bcV, nPressureBC, pressureBCNodes, bcP, viscosity, dt);
     ensure_workspace(h, std::max(nNodes, nPressure));
-    if (h->solverMode == NSF_SOLVER_MIXED)
-        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], h->stream);
+    for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS})
+        prepare_matrix(h->mats[slot], h->solverMode == NSF_SOLVER_MIXED, h->stream);
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     h->sim.ready = true;
     NSF_END(h)
@@ -689,8 +692,8 @@ int nsf_batch_add(nsf_device* h, int nNodes, const float* xy, int nElements, con
     in->stepCounter.zero(h->stream);
     in->teamNs.alloc(1);
     in->teamNs.zero(h->stream);
-    if (h->solverMode == NSF_SOLVER_MIXED)
-        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(in->mats[slot], h->stream);
+    for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS})
+        prepare_matrix(in->mats[slot], h->solverMode == NSF_SOLVER_MIXED, h->stream);
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     in->sim.ready = true;
     h->batch.push_back(std::move(in));
@@ -705,8 +708,8 @@ int nsf_batch_finalize(nsf_device* h, int autotuneRounds) {
     if ((int)h->batch.size() > h->batchCapacity)
         throw bad_arg("more instances than co-resident CTAs (" + std::to_string(h->batchCapacity) + ")");
     for (auto& in : h->batch)
-        if (h->solverMode == NSF_SOLVER_MIXED)
-            for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(in->mats[slot], h->stream);
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS})
+            prepare_matrix(in->mats[slot], h->solverMode == NSF_SOLVER_MIXED, h->stream);
     batch_autotune(h, std::max(0, autotuneRounds));
     batch_capture_graph(h);
     h->batchReady = true;
@@ -796,7 +799,7 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
     h->solverMode = mode;
     for (bool& off : h->mixedOff) off = false;
     if (mode == NSF_SOLVER_MIXED && h->sim.ready) {
-        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) make_fp32_values(h->mats[slot], h->stream);
+        for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) prepare_matrix(h->mats[slot], true, h->stream);
         NSF_CUDA(cudaStreamSynchronize(h->stream));
     }
     NSF_END(h)

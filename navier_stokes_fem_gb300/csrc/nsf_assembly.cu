@@ -137,8 +137,7 @@ static void upload_pattern(Csr& A, const HostCsr& p, cudaStream_t s) {
     A.col.upload(p.col.data(), p.col.size(), s);
     A.val.alloc(std::max<int64_t>(A.nnz, 1));
     A.val.zero(s);
-    A.has32 = false;
-    A.val32.release();
+    A.values_changed();
 }
 
 // ---------------------------------------------------------------------------------------------------

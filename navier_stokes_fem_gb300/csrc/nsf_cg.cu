@@ -31,35 +31,28 @@ namespace nsf {
 // single-solve kernels: the team is the whole cooperative grid
 // ---------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kCgThreads, 2) cg_fp64_kernel(CgArgs a) {
-    NSF_KERNEL_SHARED(a.timeoutNs);
+    NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_cg_fp64(t, a, stage, smem, st);
+    team_cg_fp64(t, a, stage, smem);
 }
 
 __global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_kernel(CgArgs a) {
-    NSF_KERNEL_SHARED(a.timeoutNs);
+    NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_cg_mixed(t, a, stage, smem, st);
+    team_cg_mixed(t, a, stage, smem);
 }
 
 // ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
-// Both CG kernels take kDynSmem bytes of dynamic shared memory (the copy pipeline), above the 48 KB default.
-void cg_set_smem_attributes() {
-    NSF_CUDA(cudaFuncSetAttribute(cg_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem));
-    NSF_CUDA(cudaFuncSetAttribute(cg_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem));
-}
-
 void cg_configure(CgWorkspace& ws, int device) {
-    cg_set_smem_attributes();
     int sms = 0, coop = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NSF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
     if (!coop) throw Error{NSF_ERR_NO_DEVICE, "device does not support cooperative launches"};
     int occ64 = 0, occMixed = 0;
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, kDynSmem));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, kDynSmem));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, 0));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, 0));
     const int perSm = std::min(2, std::min(occ64, occMixed));
     if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
     ws.grid = sms * perSm;
@@ -74,19 +67,18 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, cudaStream_t s) {
     CgArgs a = args;
     void* params[] = {&a};
     const void* fn = mode == NSF_SOLVER_MIXED ? (const void*)cg_mixed_kernel : (const void*)cg_fp64_kernel;
-    NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, kDynSmem, s));
+    NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
     count_launch();
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.
 int cg_fp64_grid(int device, int* block) {
-    cg_set_smem_attributes();
     int sms = 0, coop = 0, occ64 = 0, occMixed = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NSF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
     if (!coop) throw Error{NSF_ERR_NO_DEVICE, "device does not support cooperative launches"};
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, kDynSmem));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, kDynSmem));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, 0));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, 0));
     const int perSm = std::min(2, std::min(occ64, occMixed));
     if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
     *block = kCgThreads;
@@ -98,7 +90,7 @@ void cg_launch_fp64_raw(const CgArgs& args, int grid, int block, cudaStream_t s)
     NSF_CUDA(cudaMemsetAsync(args.sync, 0, sizeof(GridSync), s));
     CgArgs a = args;
     void* params[] = {&a};
-    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)cg_fp64_kernel, dim3(grid), dim3(block), params, kDynSmem, s));
+    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)cg_fp64_kernel, dim3(grid), dim3(block), params, 0, s));
     count_launch();
 }
 

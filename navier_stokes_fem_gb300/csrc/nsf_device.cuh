@@ -5,18 +5,16 @@
 
 namespace nsf {
 
-constexpr int kCgThreads = 512;
+constexpr int kCgThreads = 256;
 constexpr int kWarps = kCgThreads / 32;
 constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 
-// TMA bulk-copy pipeline of the streamed SpMV: kPipe stages, each a contiguous slice of the CTA's column
-// indices and values (kStreamBytes per stage).  The dynamic shared memory of every CG kernel is kPipe stages
-// (the warp-chunked SpMV's staging area reuses the same bytes in other phases).
-constexpr int kPipe = 3;
-constexpr int kStreamBytes = 32768;
-constexpr int kDynSmem = kPipe * kStreamBytes;
-static_assert(kWarps * 2 * kStage * (int)sizeof(double) <= kDynSmem, "staging area must fit the stream buffers");
+// Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area.
+#define NSF_KERNEL_SHARED()          \
+    __shared__ double smem[33];      \
+    __shared__ double stage[kWarps * 2 * kStage]
+
 
 // ---------------------------------------------------------------------------------------------------
 // memory-model and timing helpers
@@ -35,6 +33,8 @@ __device__ __forceinline__ long long global_ns() {
     return t;
 }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+// L2 load of data another block wrote before a barrier (never a stale L1 line)
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 
 // streaming loads for the matrix (read once per iteration; keep L2 for the gathered vectors)
 __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
@@ -99,24 +99,43 @@ static __device__ double block_sum(double v, double* smem) {
     return t;
 }
 
-// Sum of the per-block partials of one region, identical in every block and thread.
-static __device__ double grid_sum(const double* part, int G, double* smem) {
-    double v = 0;
-    if (threadIdx.x < 32) {
-        for (int i = threadIdx.x; i < G; i += 32) v += part[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) smem[32] = v;
-    }
-    __syncthreads();
-    v = smem[32];
-    __syncthreads();
-    return v;
+// hi + lo += a * b in double-float arithmetic (Dekker's exact product and Knuth's two-sum on FP32 operations):
+// about 44 significant bits for a per-thread partial dot product without touching the FP64 pipe, which on GB300
+// is narrower than the FP32 one by a factor of 64.  The _rn intrinsics keep the compiler from contracting them.
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(s, hi);
+    const float se = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(se, pe));
 }
 
-// Row-range of this CTA within its team: contiguous chunks keep each CTA's gathers local.
+// Sum of the per-block partials of one region, identical in every block and thread.  Every thread loads its
+// partials at once (one memory latency), then a fixed-order warp and block reduction.
+static __device__ double grid_sum(const double* part, int G, double* smem) {
+    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    double p[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) p[k] = tid + k * bs < G ? ld_cg(part + tid + k * bs) : 0.0;
+    double v = (p[0] + p[1]) + (p[2] + p[3]);
+    for (int i = tid + 4 * bs; i < G; i += bs) v += ld_cg(part + i);   // (teams wider than 4 blocks per thread)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) smem[16 + warp] = v;
+    __syncthreads();
+    double t = 0;
+    for (int w = 0; w < nw; ++w) t += smem[16 + w];
+    __syncthreads();
+    return t;
+}
+
+// Row-range of this CTA within its team: contiguous chunks keep each CTA's gathers local; chunks are whole
+// 32-row slices so that the SELL-32 product of a CTA covers exactly its rows.
 __device__ __forceinline__ void team_rows(int n, const Team& t, int& rb, int& re) {
-    const int chunk = (n + t.size - 1) / t.size;
+    const int slices = (n + 31) / 32;
+    const int chunk = ((slices + t.size - 1) / t.size) * 32;
     rb = min(n, t.rank * chunk);
     re = min(n, rb + chunk);
 }
@@ -184,198 +203,114 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Streamed SpMV: the CTA's column indices and values arrive in shared memory through TMA bulk copies
-// (cp.async.bulk, completion on an mbarrier), kPipe stages in flight, so the matrix stream needs no registers
-// and no dependent loads; threads only read row pointers, gather the vector and sum from shared memory.
+// SELL-32 product (the CG kernels' hot loop).  Rows are grouped in slices of 32; slice s stores its rows'
+// entries column-major, entry k of row 32s + lane at sliceStart[s] + 32k + lane, padded to the slice's longest
+// row with value 0 and the row's own column.  A warp owns a slice: every load of the matrix is one coalesced
+// 128-byte (FP32) or 256-byte (FP64) line, with no shared-memory staging and no block-wide synchronisation, and
+// each lane sums its row in CSR entry order with one fused multiply-add per entry (padding adds exact zeros),
+// so the result equals the CSR row sum bit for bit.  Up to kUnroll entries per lane have their matrix loads and
+// then their vector gathers in flight at once.  The matrix is read with evict-first loads so that the gathered
+// vectors stay in L2.
 // ---------------------------------------------------------------------------------------------------
-template <typename TV> __host__ __device__ constexpr int stream_entries() {
-    return (int)((kStreamBytes / (4 + sizeof(TV))) / 4) * 4;
-}
+constexpr int kSlice = 32;
+constexpr int kUnroll = 8;
 
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-// Per-CTA state of the copy pipeline; `seq` counts stages over the whole kernel so every buffer's mbarrier
-// phase is known without extra state.
-struct Stream {
-    unsigned long long* bar;   // kPipe mbarriers (shared)
-    unsigned char* buf;        // kPipe * kStreamBytes (dynamic shared)
-    int* ctl;                  // 2 shared ints: next stage's first row, abort
-    double* carry;             // 1 shared double: partial sum of a row that continues into the next stage
-    unsigned seq;
-    long long timeoutNs;
-
-    __device__ void init() {
-        if (threadIdx.x == 0) {
-            for (int i = 0; i < kPipe; ++i) mbar_init(bar + i, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        seq = 0;
-        __syncthreads();
-    }
-};
-
-// Shared memory of a CG kernel: `smem` (reduction slots), the copy pipeline `st` over the kDynSmem dynamic bytes,
-// and `stage`, the warp-chunked SpMV's staging area on the same bytes.  Launch with kDynSmem dynamic bytes.
-#define NSF_KERNEL_SHARED(timeout)                                                        \
-    extern __shared__ __align__(128) unsigned char nsf_dyn[];                              \
-    __shared__ double smem[33];                                                            \
-    __shared__ unsigned long long nsf_bars[kPipe];                                         \
-    __shared__ int nsf_ctl[2];                                                             \
-    __shared__ double nsf_carry[2];                                                        \
-    Stream st{nsf_bars, nsf_dyn, nsf_ctl, nsf_carry, 0u, (timeout)};                       \
-    st.init();                                                                             \
-    double* stage = reinterpret_cast<double*>(nsf_dyn)
-
-// Issue the copies of one stage: entries [c0, c1) of col and val (c0 a multiple of 4, c1 - c0 a multiple of 4).
+// Loads entries [k0, k0 + kUnroll) of a lane's row in a slice (column -1 past the slice width W).
 template <typename TV>
-__device__ __forceinline__ void stream_issue(Stream& st, unsigned slot, const int* col, const TV* val, int c0, int c1) {
-    constexpr int S = stream_entries<TV>();
-    unsigned char* base = st.buf + (size_t)slot * kStreamBytes;
-    const unsigned n = (unsigned)(c1 - c0);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(st.bar + slot, n * (unsigned)(4 + sizeof(TV)));
-    bulk_g2s(base, col + c0, n * 4u, st.bar + slot);
-    bulk_g2s(base + (size_t)S * 4, val + c0, n * (unsigned)sizeof(TV), st.bar + slot);
+__device__ __forceinline__ void sell_chunk(const int* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
+                                           int (&c)[kUnroll], TV (&v)[kUnroll]) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+        const bool in = k0 + u < W;
+        c[u] = in ? ld_stream(cp + (k0 + u) * kSlice) : -1;
+        v[u] = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
+    }
 }
 
-// Rows [rb, re) of this CTA: epi(row, sum) for every row, sum = sum_j a_ij gather(j) (or the difference form with
-// Diff, see warp_spmv).  Returns false if a copy did not complete within the time limit.
+// A warp walks its slices sFirst, sFirst + nw, ... with the next slice's first kUnroll matrix entries loaded
+// while the current slice's gathers are in flight, so a slice costs one memory latency, not two.  The slices'
+// start offsets are fetched 32 at a time, one per lane, and handed out by shuffles.
 template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
-__device__ bool stream_spmv(Stream& st, const int* __restrict__ rowptr, const int* __restrict__ col,
-                            const TV* __restrict__ val, int nnzTotal, int rb, int re, Gather gather, Epi epi) {
-    constexpr int S = stream_entries<TV>();
-    if (rb >= re) return true;
-    const int E0 = rowptr[rb], E1 = rowptr[re];
-    const int base0 = E0 & ~3;
-    // Bulk copies need 16-byte aligned sources: with an unaligned col or val (a caller's sub-allocation) every
-    // entry is read directly.  Entries past the last multiple of 4 are always read directly.
-    const bool aligned = ((reinterpret_cast<unsigned long long>(col) | reinterpret_cast<unsigned long long>(val)) &
-                          15ULL) == 0;
-    const int copyLimit = aligned ? (nnzTotal & ~3) : 0;
-    const int nst = (E1 - base0 + S - 1) / S;
-    auto copy_range = [&](int s, int& c0, int& c1) {
-        c0 = base0 + s * S;
-        c1 = min(c0 + S, min((E1 + 3) & ~3, copyLimit));
-        if (c1 < c0) c1 = c0;
+__device__ __forceinline__ void sell_spmv(const int* __restrict__ sliceStart, const int* __restrict__ col,
+                                          const TV* __restrict__ val, int rb, int re, Gather gather, Epi epi) {
+    if (rb >= re) return;   // (an empty range may start inside the last, partial slice)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int s1 = (re + kSlice - 1) / kSlice;
+    const int sFirst = rb / kSlice + warp;
+    if (sFirst >= s1) return;
+    const int count = (s1 - sFirst + nw - 1) / nw;
+    int mb = 0, me = 0;   // lane j: start and end of this warp's slice (block of 32) + j
+    auto meta_load = [&](int i0) {
+        const int idx = sFirst + (i0 + lane) * nw;
+        mb = idx < s1 ? sliceStart[idx] : 0;
+        me = idx < s1 ? sliceStart[idx + 1] : 0;
     };
-    // the buffers were last written through the generic proxy (staging of other phases): order those writes
-    // before the copies that overwrite them
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    // prologue: stages 0 .. kPipe-2
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kPipe - 1 && s < nst; ++s) {
-            int c0, c1;
-            copy_range(s, c0, c1);
-            if (c1 > c0) stream_issue<TV>(st, (st.seq + s) % kPipe, col, val, c0, c1);
-            else mbar_expect_tx(st.bar + (st.seq + s) % kPipe, 0);
+    meta_load(0);
+    int base = __shfl_sync(0xffffffffu, mb, 0);
+    int W = (__shfl_sync(0xffffffffu, me, 0) - base) / kSlice;
+    int c[kUnroll];
+    TV v[kUnroll];
+    sell_chunk<TV>(col + base + lane, val + base + lane, W, 0, c, v);
+    for (int i = 0; i < count; ++i) {
+        const int row = (sFirst + i * nw) * kSlice + lane;
+        const bool own = row < re;
+        const TA self = own ? gather(row) : TA(0);
+        TA g[kUnroll];
+        TV vk[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            g[u] = c[u] >= 0 ? gather(c[u]) : TA(0);
+            vk[u] = v[u];
         }
-        st.ctl[0] = rb;
-        st.ctl[1] = rb;   // stays put through a stage that no row touches (E0 == E1)
-        st.carry[0] = 0.0;
-    }
-    __syncthreads();
-    bool ok = true;
-    int s = 0;
-    for (; s < nst; ++s) {
-        const unsigned g = st.seq + s, slot = g % kPipe, parity = (g / kPipe) & 1;
-        if (threadIdx.x == 0 && s + kPipe - 1 < nst) {   // refill the buffer freed by stage s-1
-            int c0, c1;
-            copy_range(s + kPipe - 1, c0, c1);
-            const unsigned sl = (g + kPipe - 1) % kPipe;
-            if (c1 > c0) stream_issue<TV>(st, sl, col, val, c0, c1);
-            else mbar_expect_tx(st.bar + sl, 0);
+        // the next slice's first entries, in flight with this slice's gathers
+        int baseN = 0, WN = 0;
+        if (i + 1 < count) {
+            if (((i + 1) & 31) == 0) meta_load(i + 1);
+            baseN = __shfl_sync(0xffffffffu, mb, (i + 1) & 31);
+            WN = (__shfl_sync(0xffffffffu, me, (i + 1) & 31) - baseN) / kSlice;
         }
-        // wait for this stage (bounded)
-        {
-            const long long t0 = global_ns();
-            while (!mbar_test(st.bar + slot, parity)) {
-                if (global_ns() - t0 > st.timeoutNs) { ok = false; break; }
+        sell_chunk<TV>(col + baseN + lane, val + baseN + lane, WN, 0, c, v);
+        TA acc = TA(0);
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (u < W) {
+                if (Diff) acc = fma(TA(vk[u]), g[u] - self, acc);
+                else acc = fma(TA(vk[u]), g[u], acc);
             }
         }
-        if (__syncthreads_or(!ok)) { ok = false; break; }
-        int c0, c1;
-        copy_range(s, c0, c1);
-        const int ws = max(E0, base0 + s * S), we = min(E1, base0 + (s + 1) * S);
-        const int* colS = reinterpret_cast<const int*>(st.buf + (size_t)slot * kStreamBytes);
-        const TV* valS = reinterpret_cast<const TV*>(st.buf + (size_t)slot * kStreamBytes + (size_t)S * 4);
-        const int first = st.ctl[0];
-        for (int r = first + (int)threadIdx.x; r < re; r += blockDim.x) {
-            const int rs = rowptr[r];
-            if (rs >= we) break;
-            const int rend = rowptr[r + 1];
-            const int a0 = max(rs, ws), a1 = min(rend, we);
-            const TA self = Diff ? gather(r) : TA(0);
-            TA acc = (r == first && rs < ws) ? (TA)st.carry[0] : TA(0);
-            for (int e = a0; e < a1; ++e) {
-                int c;
-                TV v;
-                if (e < c1) { c = colS[e - c0]; v = valS[e - c0]; }
-                else { c = col[e]; v = val[e]; }            // the last few entries of the matrix (alignment)
-                if (Diff) acc = fma(TA(v), gather(c) - self, acc);
-                else acc = fma(TA(v), gather(c), acc);
-            }
-            if (rend > we) {                  // continues in the next stage
-                st.carry[1] = (double)acc;
-                st.ctl[1] = r;
-            } else {
-                epi(r, acc);
-                if (rend == we) st.ctl[1] = r + 1;
+        // rows longer than kUnroll entries (P2 matrices): the rest of the slice, chunk by chunk
+        for (int k0 = kUnroll; k0 < W; k0 += kUnroll) {
+            int c2[kUnroll];
+            TV v2[kUnroll];
+            sell_chunk<TV>(col + base + lane, val + base + lane, W, k0, c2, v2);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) g[u] = c2[u] >= 0 ? gather(c2[u]) : TA(0);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                if (c2[u] >= 0) {
+                    if (Diff) acc = fma(TA(v2[u]), g[u] - self, acc);
+                    else acc = fma(TA(v2[u]), g[u], acc);
+                }
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            st.ctl[0] = st.ctl[1];
-            st.carry[0] = st.carry[1];
-        }
-        // the next iteration's refill (thread 0) targets the buffer this stage used: everyone is done with it
-        __syncthreads();
+        if (own) epi(row, acc, self);
+        base = baseN;
+        W = WN;
     }
-    if (!ok) {
-        // a copy did not land in time: before the CTA leaves, wait (bounded again) for the stages still in flight,
-        // s .. min(nst, s + kPipe) - 1, so that no copy writes into shared memory after the kernel ends
-        if (threadIdx.x == 0) {
-            const int last = min(nst, s + kPipe);
-            for (int k = s; k < last; ++k) {
-                const unsigned g = st.seq + k;
-                const long long t0 = global_ns();
-                while (!mbar_test(st.bar + g % kPipe, (g / kPipe) & 1))
-                    if (global_ns() - t0 > st.timeoutNs) break;
-            }
-        }
-        __syncthreads();
-        return false;
+}
+
+// q = A p over the CTA's rows with epi(row, sum, p_row): the SELL-32 copy when the matrix has one, else the
+// warp-chunked CSR product (caller-owned CSR arrays, e.g. the allocation-free entry point).
+template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
+__device__ __forceinline__ void matrix_product(const int* sellStart, const int* sellCol, const TV* sellVal,
+                                               const int* rowptr, const int* col, const TV* val, int rb, int re,
+                                               TA* stage, Gather gather, Epi epi) {
+    if (sellStart) {
+        sell_spmv<TV, TA, Diff>(sellStart, sellCol, sellVal, rb, re, gather, epi);
+    } else {
+        warp_spmv<TV, TA, Diff>(rowptr, col, val, rb, re, stage, gather,
+                                [&](int row, TA acc) { epi(row, acc, gather(row)); });
     }
-    st.seq += (unsigned)nst;
-    {           // rows without entries after the last non-zero of the range (none in assembled matrices)
-        for (int r = st.ctl[0] + (int)threadIdx.x; r < re; r += blockDim.x)
-            if (rowptr[r] == E1) epi(r, TA(0));
-        __syncthreads();
-    }
-    return ok;
 }
 
 static __device__ void write_info(const Team& t, const CgArgs& a, int it, int status, int outer, double rr, double bb) {
@@ -387,21 +322,6 @@ static __device__ void write_info(const Team& t, const CgArgs& a, int it, int st
         a.info->rr = rr;
         a.info->bb = bb;
     }
-}
-
-// A matrix copy that did not land in time: raise the team's abort word (its other CTAs leave at their next
-// barrier) and report the timeout status.
-static __device__ int stream_timeout(const Team& t, const CgArgs& a, int it, int outer, double rr, double bb) {
-    if (threadIdx.x == 0) atomicExch(&t.sync->abort, 1);
-    if (threadIdx.x == 0 && t.rank == 0) {
-        a.info->iterations = it;
-        a.info->status = NSF_ERR_BARRIER_TIMEOUT;
-        a.info->outer = outer;
-        a.info->fallback = 0;
-        a.info->rr = rr;
-        a.info->bb = bb;
-    }
-    return NSF_ERR_BARRIER_TIMEOUT;
 }
 
 // b for this block's rows: the given vector, or the fused right-hand side mask ? g : (B x_b) - lift, stored
@@ -421,9 +341,8 @@ static __device__ void build_rhs(const CgArgs& a, int rb, int re, double* stage)
 // FP64 persistent CG
 // partial regions: 0 = p.q, 1 = r.r, 2 = r0.r0, 3 = b.b
 // ---------------------------------------------------------------------------------------------------
-static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem, Stream& st) {
+static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
     const int G = t.size;
-    const int nnzTotal = a.rowptr[a.n];
     int rb, re;
     team_rows(a.n, t, rb, re);
     const double* b = a.bRowptr ? a.bOut : a.b;
@@ -457,13 +376,12 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     while (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
         // phase A: q = A p (streamed matrix), partial p.q
         double pq = 0;
-        const bool copied = stream_spmv<double, double, false>(st, a.rowptr, a.col, a.val, nnzTotal, rb, re,
-                                                              [&](int c) { return p[c]; },
-                                                              [&](int row, double acc) {
-                                                                  a.q[row] = acc;
-                                                                  pq = fma(p[row], acc, pq);
-                                                              });
-        if (!copied) return stream_timeout(t, a, it, 1, rr, bb);
+        matrix_product<double, double, false>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+                                              [&](int c) { return p[c]; },
+                                              [&](int row, double acc, double pr) {
+                                                  a.q[row] = acc;
+                                                  pq = fma(pr, acc, pq);
+                                              });
         pq = block_sum(pq, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(2)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
@@ -531,8 +449,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 // saves the third barrier of the FP64 kernel.
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
-static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, Stream& st) {
-    const int nnzTotal = a.rowptr[a.n];
+static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
     float* stage32 = reinterpret_cast<float*>(stage);
     const int G = t.size;
     int rb, re;
@@ -611,25 +528,24 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             const float* pp = pprev;
             float* pc = pcur;
             const float* r32 = a.r32;
-            double pq = 0;
-            // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv)
-            const bool copied = stream_spmv<float, float, true>(st, a.rowptr, a.col, a.val32, nnzTotal, rb, re,
-                                                                [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                                                                [&](int row, float acc) {
-                                                                    const float pi = fmaf(betaf, pp[row], r32[row]);
-                                                                    acc = fmaf(a.rowsum32[row], pi, acc);
-                                                                    pc[row] = pi;
-                                                                    a.q32[row] = acc;
-                                                                    pq = fma((double)pi, (double)acc, pq);
-                                                                });
-            if (!copied) return stream_timeout(t, a, it, refresh, rr64, bb);
-            pq = block_sum(pq, smem);
+            // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
+            // p.q accumulates in double-float so that the FP64 pipe does no per-row work
+            float pqHi = 0.f, pqLo = 0.f;
+            matrix_product<float, float, true>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
+                                               stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+                                               [&](int row, float acc, float pi) {
+                                                   acc = fmaf(a.rowsum32[row], pi, acc);
+                                                   pc[row] = pi;
+                                                   a.q32[row] = acc;
+                                                   df_acc(pqHi, pqLo, pi, acc);
+                                               });
+            const double pq = block_sum((double)pqHi + (double)pqLo, smem);
             if (threadIdx.x == 0) a.partials[t.rank] = pq;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
             const double pqs = grid_sum(a.partials, G, smem);
             if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
             const float alphaf = (float)(rr / pqs);
-            double rrn = 0;
+            float rrHi = 0.f, rrLo = 0.f;
             for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += 4 * bs) {
                 float pi[4], qi[4], di[4], ri[4];
 #pragma unroll
@@ -644,11 +560,11 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
                         a.d32[i] = fmaf(alphaf, pi[u], di[u]);
                         const float rn = fmaf(-alphaf, qi[u], ri[u]);
                         a.r32[i] = rn;
-                        rrn = fma((double)rn, (double)rn, rrn);
+                        df_acc(rrHi, rrLo, rn, rn);
                     }
                 }
             }
-            rrn = block_sum(rrn, smem);
+            const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
             if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
             const double rrs = grid_sum(a.partials + G, G, smem);
@@ -674,7 +590,7 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
         f.b = b;
         f.x0 = a.x;
         f.maxIt = a.maxIt - it;
-        const int fst = team_cg_fp64(t, f, stage, smem, st);
+        const int fst = team_cg_fp64(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
             a.info->iterations += it;

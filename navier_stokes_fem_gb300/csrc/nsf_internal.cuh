@@ -81,6 +81,17 @@ struct Csr {
     DevBuf<float> val32;
     DevBuf<float> rowsum32;   // FP64 row sums rounded to FP32 (the difference-form FP32 product)
     bool has32 = false;
+    // SELL-32 copy for the CG kernels: slice s = rows [32s, 32s+32), entries column-major from sellStart[s]
+    int nSlices = 0;
+    DevBuf<int> sellStart, sellCol;
+    DevBuf<double> sellVal;
+    DevBuf<float> sellVal32;
+    bool hasSell = false, hasSell32 = false;
+    void values_changed() {
+        has32 = hasSell = hasSell32 = false;
+        val32.release();
+        sellVal32.release();
+    }
     bool valid() const { return rows > 0 && rowptr.ptr != nullptr; }
 };
 
@@ -109,6 +120,10 @@ struct CgArgs {
     const double* val;
     const float* val32;
     const float* rowsum32;   // row sums of the FP64 matrix, rounded once (mixed precision difference form)
+    const int* sellStart;    // SELL-32 copy (null: the CSR arrays are used)
+    const int* sellCol;
+    const double* sellVal;
+    const float* sellVal32;
     const double* b;
     const double* x0;
     double* x;
@@ -161,6 +176,8 @@ void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const un
 void axpy_bc_launch(int n, const double* a, double* y, const unsigned char* mask, const double* bcValue,
                     cudaStream_t s);
 void make_fp32_values(Csr& A, cudaStream_t s);
+// SELL-32 copy (FP64 values; with fp32 also the FP32 values and row sums) for the CG kernels; no-op when current
+void prepare_matrix(Csr& A, bool fp32, cudaStream_t s);
 
 // ------------------------------------------------------------------------------------------------
 // Mesh, point-location tree and simulation state

@@ -27,6 +27,10 @@ struct CsrView {
     const double* val;
     const float* val32;
     const float* rowsum32;
+    const int* sellStart;
+    const int* sellCol;
+    const double* sellVal;
+    const float* sellVal32;
 };
 
 struct StepInstance {
@@ -62,6 +66,10 @@ __device__ __forceinline__ CgArgs solve_args(const StepInstance& I, const StepPa
     a.val = A.val;
     a.val32 = A.val32;
     a.rowsum32 = A.rowsum32;
+    a.sellStart = A.sellStart;
+    a.sellCol = A.sellCol;
+    a.sellVal = A.sellVal;
+    a.sellVal32 = A.sellVal32;
     a.r = I.r;
     a.q = I.q;
     a.pbuf0 = I.p0;
@@ -81,13 +89,21 @@ __device__ __forceinline__ CgArgs solve_args(const StepInstance& I, const StepPa
     return a;
 }
 
-__device__ __forceinline__ int run_cg(Team& t, const CgArgs& a, int mode, double* stage, double* smem, Stream& st) {
-    return mode == NSF_SOLVER_MIXED ? team_cg_mixed(t, a, stage, smem, st) : team_cg_fp64(t, a, stage, smem, st);
+// One out-of-line copy of each solver serves the step's three solve sites (register allocation per solver, not
+// for six inlined copies at once).
+__device__ __noinline__ int step_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_cg_fp64(t, a, stage, smem);
+}
+__device__ __noinline__ int step_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_cg_mixed(t, a, stage, smem);
+}
+__device__ __forceinline__ int run_cg(Team& t, const CgArgs& a, int mode, double* stage, double* smem) {
+    return mode == NSF_SOLVER_MIXED ? step_cg_mixed(t, a, stage, smem) : step_cg_fp64(t, a, stage, smem);
 }
 
 __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance* __restrict__ insts,
                                                              const int* __restrict__ blockInst, StepParams sp) {
-    NSF_KERNEL_SHARED(sp.timeoutNs);
+    NSF_KERNEL_SHARED();
     const StepInstance& I = insts[blockInst[blockIdx.x]];
     Team t{I.sync, I.partials, I.nBlocks, (int)blockIdx.x - I.firstBlock, 0ULL, sp.timeoutNs};
     const long long t0 = global_ns();
@@ -142,7 +158,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.tmp + (size_t)ch * Nv;
         a.x = I.uv + (size_t)ch * Nv;
         a.info = info + ch;
-        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // pressure: Kp p = -(1/dt) Div u - lift, pinned nodes -> g; x0 = p
     {
@@ -159,7 +175,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.p;
         a.x = I.p;
         a.info = info + 2;
-        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // velocity correction: M du = (-dt Grad p) per component, x0 = u; the right-hand side is built from the
     // gradient rows of the component (row offset ch*Nv) inside the solve
@@ -174,7 +190,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.uv + (size_t)ch * Nv;
         a.x = I.tmp + (size_t)ch * Nv;
         a.info = info + 3 + ch;
-        if (run_cg(t, a, sp.mode, stage, smem, st) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // u <- du + u with the Dirichlet values re-imposed (include/assembly.h:686-707), in place
     team_rows(Nv, t, rb, re);
@@ -193,14 +209,14 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
 // host side
 // ---------------------------------------------------------------------------------------------------
 static CsrView view(const Csr& A) {
-    return CsrView{A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.rowsum32.get()};
+    return CsrView{A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.rowsum32.get(),
+                   A.hasSell ? A.sellStart.get() : nullptr, A.sellCol.get(), A.sellVal.get(), A.sellVal32.get()};
 }
 
 int step_kernel_capacity(int device) {
     int sms = 0, occ = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    NSF_CUDA(cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_kernel, kCgThreads, kDynSmem));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_kernel, kCgThreads, 0));
     return sms * std::min(occ, 2);
 }
 
@@ -275,7 +291,7 @@ void batch_launch_step(nsf_device* h) {
     const StepInstance* desc = reinterpret_cast<const StepInstance*>(h->batchDesc.get());
     const int* bi = h->batchBlockInst.get();
     void* params[] = {(void*)&desc, (void*)&bi, (void*)&sp};
-    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)step_kernel, dim3(h->batchGrid), dim3(kCgThreads), params, kDynSmem,
+    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)step_kernel, dim3(h->batchGrid), dim3(kCgThreads), params, 0,
                                          h->stream));
     count_launch();
 }

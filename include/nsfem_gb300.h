@@ -68,8 +68,17 @@ enum nsf_slot {
 
 /* CG variants */
 enum nsf_solver {
-    NSF_SOLVER_FP64 = 0,   /* persistent FP64 CG megakernel: the plain method */
-    NSF_SOLVER_MIXED = 1   /* FP32 matrix/vectors inside, FP64 dots and scalars, FP64 iterative refinement */
+    NSF_SOLVER_FP64 = 0,       /* persistent FP64 CG megakernel: the plain method */
+    NSF_SOLVER_MIXED = 1,      /* FP32 matrix/vectors inside, FP64 dots and scalars, FP64 iterative refinement */
+    NSF_SOLVER_PCG_MIXED = 2,  /* mixed precision with the slot's preconditioner (plain mixed CG if it has none) */
+    NSF_SOLVER_PCG_FP64 = 3    /* FP64 PCG with the slot's preconditioner (plain FP64 CG if it has none) */
+};
+
+/* preconditioner kinds (nsf_precond_kind) */
+enum nsf_precond {
+    NSF_PRECOND_NONE = 0,
+    NSF_PRECOND_IC0 = 1,       /* incomplete Cholesky on the multicolour pattern */
+    NSF_PRECOND_LEARNED = 2    /* factor values installed by nsf_precond_set (the learned preconditioner) */
 };
 
 /* ---- device (GPUSimulationDeviceManager::init + getDevice) ------------------------------------------- */
@@ -101,6 +110,25 @@ int nsf_conjugate_gradient_f32(nsf_device* h, int slot, const float* b, const fl
 /* Device-pointer form, asynchronous on the handle's stream except for the status read-back. */
 int nsf_conjugate_gradient_dev(nsf_device* h, int slot, const double* b_dev, const double* x0_dev, double* x_dev,
                                int maxIterations, double eps, int mode, int* iterations, double* relResidual);
+
+/* ---- preconditioners (IC0Preconditioner under USE_PRECONDITIONING, include/assembly.h:33-35, 1338-1344) -----
+ * M = L L^T in multicolour order: the slot's matrix graph is coloured greedily in row order, and L_ij (i != j)
+ * lives on the matrix pattern where colour(j) < colour(i).  A preconditioned solve (NSF_SOLVER_PCG_*) that has not
+ * converged after the slot's cap of iterations finishes with plain FP64 CG from its current iterate. */
+/* Builds the pattern; colours and the number of strictly lower entries may be NULL. */
+int nsf_precond_pattern(nsf_device* h, int slot, int* colours, int64_t* nnzLower);
+/* The pattern: rowptr[rows + 1] and col[nnzLower] of the strictly lower part, entries of a row ordered by
+ * (colour, column), and colour[rows]. */
+int nsf_precond_get_pattern(nsf_device* h, int slot, int* rowptr, int* col, unsigned char* colour);
+/* Incomplete Cholesky on the pattern, retried with a diagonal shift a_ii (1 + shift) on breakdown. */
+int nsf_precond_ic0(nsf_device* h, int slot, double* shiftUsed);
+/* Installs factor values (host arrays): lower[nnzLower] on the pattern and diag[rows] = L_ii > 0. */
+int nsf_precond_set(nsf_device* h, int slot, const double* lower, const double* diag);
+int nsf_precond_get(nsf_device* h, int slot, double* lower, double* diag);
+int nsf_precond_kind(nsf_device* h, int slot);
+int nsf_precond_clear(nsf_device* h, int slot);
+/* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
+int nsf_precond_cap(nsf_device* h, int slot, int maxIterations);
 
 /* ---- mesh, point location and advection (uploadKDTree; advect; KDTree::findElement) ------------------ */
 /* Uploads the mesh and builds the point-location tree on the GPU over triangle centroids. */
@@ -153,9 +181,10 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);
 int nsf_set_barrier_timeout(nsf_device* h, double seconds);
 /* Records CUDA events around every persistent CG launch while enabled (clears previous records). */
 int nsf_profile(nsf_device* h, int enable);
-/* Returns the number of records written (<= maxRecords).  mode: 0 FP64, 1 mixed, 2 mixed that stalled and finished
- * with the FP64 method; outer: FP64 true-residual refreshes of a mixed solve. */
-int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* rows, int64_t* nnz, int* iterations,
+/* Returns the number of records written (<= maxRecords).  mode: the nsf_solver that ran; fallback: 1 if the solve
+ * finished with plain FP64 CG (a stalled mixed solve, or a preconditioned one over its cap); outer: FP64
+ * true-residual refreshes of a mixed solve. */
+int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* fallback, int* rows, int64_t* nnz, int* iterations,
                      int* outer, float* ms);
 /* op 0 records a start event on the handle's stream, op 1 a stop event and writes the elapsed ms. */
 int nsf_timer(nsf_device* h, int op, float* ms);

@@ -36,7 +36,8 @@ STATUS = {0: "NSF_OK", 1: "NSF_ERR_CUDA", 2: "NSF_ERR_NOT_CONVERGED", 3: "NSF_ER
           4: "NSF_ERR_BARRIER_TIMEOUT", 5: "NSF_ERR_BAD_ARG", 6: "NSF_ERR_STATE", 7: "NSF_ERR_NO_DEVICE"}
 SLOT = {"pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
         "pressure_divergence": 4, "velocity_lift": 5, "pressure_lift": 6}
-SOLVER = {"fp64": 0, "mixed": 1}
+SOLVER = {"fp64": 0, "mixed": 1, "pcg_mixed": 2, "pcg_fp64": 3}
+PRECOND = {0: "none", 1: "ic0", 2: "learned"}
 
 
 class NSFemError(RuntimeError):
@@ -87,8 +88,16 @@ _SIGS = {
     "nsf_set_solver": (_i, [_v, _i, _d]),
     "nsf_set_barrier_timeout": (_i, [_v, _d]),
     "nsf_profile": (_i, [_v, _i]),
-    "nsf_profile_read": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.int32), _arr(np.int64),
-                              _arr(np.int32), _arr(np.int32), _arr(np.float32)]),
+    "nsf_profile_read": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.int32), _arr(np.int32),
+                              _arr(np.int64), _arr(np.int32), _arr(np.int32), _arr(np.float32)]),
+    "nsf_precond_pattern": (_i, [_v, _i, _P(_i), _P(_i64)]),
+    "nsf_precond_get_pattern": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.uint8)]),
+    "nsf_precond_ic0": (_i, [_v, _i, _P(_d)]),
+    "nsf_precond_set": (_i, [_v, _i, _arr(np.float64), _arr(np.float64)]),
+    "nsf_precond_get": (_i, [_v, _i, _arr(np.float64), _arr(np.float64)]),
+    "nsf_precond_kind": (_i, [_v, _i]),
+    "nsf_precond_clear": (_i, [_v, _i]),
+    "nsf_precond_cap": (_i, [_v, _i, _i]),
     "nsf_timer": (_i, [_v, _i, _P(_f)]),
     "nsf_host_alloc": (_i, [_v, _sz, _P(_v)]),
     "nsf_host_free": (_i, [_v, _v]),
@@ -343,14 +352,56 @@ class GPUSimulationDevice:
 
     def profile_read(self, max_records=100000):
         n = max_records
-        slot, mode, rows, it, outer = (np.zeros(n, np.int32) for _ in range(5))
+        slot, mode, fb, rows, it, outer = (np.zeros(n, np.int32) for _ in range(6))
         nnz = np.zeros(n, np.int64)
         ms = np.zeros(n, np.float32)
-        got = library().nsf_profile_read(self._h, n, slot, mode, rows, nnz, it, outer, ms)
+        got = library().nsf_profile_read(self._h, n, slot, mode, fb, rows, nnz, it, outer, ms)
         if got < 0:
             self._check(-got)
-        return {"slot": slot[:got], "mode": mode[:got], "rows": rows[:got], "nnz": nnz[:got], "iterations": it[:got],
-                "outer": outer[:got], "ms": ms[:got]}
+        return {"slot": slot[:got], "mode": mode[:got], "fallback": fb[:got], "rows": rows[:got], "nnz": nnz[:got],
+                "iterations": it[:got], "outer": outer[:got], "ms": ms[:got]}
+
+    # ---- preconditioners (M = L L^T on the multicolour pattern of the slot's matrix) ----
+    def precond_pattern(self, slot):
+        """(rowptr, col, colour) of the factor's strictly lower part; row entries ordered by (colour, column)."""
+        c, nnz = _i(), _i64()
+        self._check(library().nsf_precond_pattern(self._h, _slot(slot), ctypes.byref(c), ctypes.byref(nnz)))
+        rows, _, _ = self.matrix_shape(slot)
+        rp = np.zeros(rows + 1, np.int32)
+        col = np.zeros(max(nnz.value, 1), np.int32)
+        colour = np.zeros(rows, np.uint8)
+        self._check(library().nsf_precond_get_pattern(self._h, _slot(slot), rp, col, colour))
+        return rp, col[:nnz.value], colour
+
+    def precond_ic0(self, slot) -> float:
+        """Incomplete Cholesky factor on the pattern; returns the diagonal shift it needed."""
+        sh = _d()
+        self._check(library().nsf_precond_ic0(self._h, _slot(slot), ctypes.byref(sh)))
+        return sh.value
+
+    def precond_set(self, slot, lower, diag):
+        lower = np.ascontiguousarray(lower, np.float64)
+        self._check(library().nsf_precond_set(self._h, _slot(slot), lower if lower.size else np.zeros(1),
+                                              np.ascontiguousarray(diag, np.float64)))
+
+    def precond_get(self, slot):
+        rp, col, _ = self.precond_pattern(slot)
+        lower = np.zeros(max(col.size, 1))
+        diag = np.zeros(rp.size - 1)
+        self._check(library().nsf_precond_get(self._h, _slot(slot), lower, diag))
+        return lower[:col.size], diag
+
+    def precond_kind(self, slot) -> str:
+        k = library().nsf_precond_kind(self._h, _slot(slot))
+        if k < 0:
+            self._check(-k)
+        return PRECOND[k]
+
+    def precond_clear(self, slot):
+        self._check(library().nsf_precond_clear(self._h, _slot(slot)))
+
+    def precond_cap(self, slot, max_iterations):
+        self._check(library().nsf_precond_cap(self._h, _slot(slot), int(max_iterations)))
 
     def timer_start(self):
         self._check(library().nsf_timer(self._h, 0, None))

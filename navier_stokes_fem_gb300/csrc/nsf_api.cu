@@ -157,6 +157,10 @@ void ensure_workspace(nsf_device* h, int rows) {
     ws.q32.ensure(rows);
     ws.p32a.ensure(rows);
     ws.p32b.ensure(rows);
+    ws.w.ensure(rows);
+    ws.w32.ensure(rows);
+    ws.xp.ensure(rows);
+    ws.bp.ensure(rows);
 }
 
 cudaEvent_t pool_event(nsf_device* h) {
@@ -174,23 +178,29 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     Csr& A = h->mats[slot];
     if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
     if (A.rows != A.cols) throw bad_arg("CG needs a square matrix");
-    prepare_matrix(A, mode == NSF_SOLVER_MIXED, h->stream);
-    ensure_workspace(h, A.rows);
+    const bool pcg = mode == NSF_SOLVER_PCG_MIXED || mode == NSF_SOLVER_PCG_FP64;
+    if (pcg && (!h->factors[slot].ready || h->factors[slot].rows != A.rows))
+        mode = mode == NSF_SOLVER_PCG_MIXED ? NSF_SOLVER_MIXED : NSF_SOLVER_FP64;   // no factor: plain CG
+    const bool precond = mode == NSF_SOLVER_PCG_MIXED || mode == NSF_SOLVER_PCG_FP64;
+    // a preconditioned solve runs on the factor's colour-permuted copy of the matrix
+    Csr& S = precond ? h->factors[slot].Ap : A;
+    prepare_matrix(S, mode == NSF_SOLVER_MIXED || mode == NSF_SOLVER_PCG_MIXED, h->stream);
+    ensure_workspace(h, S.rows);
     CgWorkspace& ws = h->ws;
     const int infoIndex = h->infoCursor;
     h->infoCursor = (h->infoCursor + 1) % (int)ws.info.n;
     CgArgs a{};
     if (fused) a = *fused;
-    a.n = A.rows;
-    a.rowptr = A.rowptr.get();
-    a.col = A.col.get();
-    a.val = A.val.get();
-    a.val32 = A.val32.get();
-    a.rowsum32 = A.rowsum32.get();
-    a.sellStart = A.sellStart.get();
-    a.sellCol = A.sellCol.get();
-    a.sellVal = A.sellVal.get();
-    a.sellVal32 = A.sellVal32.get();
+    a.n = S.rows;
+    a.rowptr = S.rowptr.get();
+    a.col = S.col.get();
+    a.val = S.val.get();
+    a.val32 = S.val32.get();
+    a.rowsum32 = S.rowsum32.get();
+    a.sellStart = S.sellStart.get();
+    a.sellCol = S.sellCol.get();
+    a.sellVal = S.sellVal.get();
+    a.sellVal32 = S.sellVal32.get();
     a.b = b;
     a.x0 = x0;
     a.x = x;
@@ -207,6 +217,16 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.sync = ws.sync.get();
     a.info = ws.info.get() + infoIndex;
     a.maxIt = maxIt < 0 ? A.rows : maxIt;
+    if (precond) {
+        a.f = factor_view(h->factors[slot], ws);
+        // over the cap (the plain method's count) the solve falls back to plain FP64 CG with the caller's own
+        // budget; when the caller's budget is the tighter limit there is no fallback
+        const int cap = h->pcgCap[slot] > 0 ? h->pcgCap[slot] : A.rows;
+        a.fallbackMaxIt = cap < a.maxIt ? a.maxIt : 0;
+        a.maxIt = std::min(a.maxIt, cap);
+    }
+    if ((size_t)infoIndex >= h->infoMode.size()) h->infoMode.resize(ws.info.n, 0);
+    h->infoMode[infoIndex] = mode;
     a.tol2 = tol * tol;
     a.innerTol2 = h->innerTol * h->innerTol;
     a.maxOuter = 64;
@@ -259,6 +279,8 @@ void upload_csr(nsf_device* h, int slot, int rows, int cols, int64_t nnz, const 
     A.col.upload(col, std::max<int64_t>(nnz, 0), h->stream);
     A.val.upload(val, std::max<int64_t>(nnz, 0), h->stream);
     A.values_changed();
+    h->factors[slot] = Factor();
+    h->pcgOff[slot] = false;
     NSF_CUDA(cudaStreamSynchronize(h->stream));
 }
 
@@ -272,7 +294,14 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     MeshDev& m = h->mesh;
     const int Nv = m.nNodes;
     // mixed precision per system, unless that system already had to finish in FP64 (see run_steps)
-    auto mode = [&](int slot) { return h->solverMode == NSF_SOLVER_MIXED && !h->mixedOff[slot] ? NSF_SOLVER_MIXED : NSF_SOLVER_FP64; };
+    auto mode = [&](int slot) {
+        const bool pre = (h->solverMode == NSF_SOLVER_PCG_MIXED || h->solverMode == NSF_SOLVER_PCG_FP64) &&
+                         h->factors[slot].ready && !h->pcgOff[slot];
+        const bool mixed = (h->solverMode == NSF_SOLVER_MIXED || h->solverMode == NSF_SOLVER_PCG_MIXED) &&
+                           !h->mixedOff[slot];
+        if (pre) return mixed ? NSF_SOLVER_PCG_MIXED : NSF_SOLVER_PCG_FP64;
+        return mixed ? NSF_SOLVER_MIXED : NSF_SOLVER_FP64;
+    };
     cudaStream_t s = h->stream;
     double* uv = S.uv.get();
     double* tmp = S.tmp.get();
@@ -339,7 +368,13 @@ void run_steps(nsf_device* h, int nsteps, int* iterations) {
             for (int j = 0; j < 5; ++j) {
                 const CgInfo& info = all[idx[(size_t)5 * k + j]];
                 if (iterations) iterations[(size_t)5 * (done + k) + j] = info.iterations;
-                if (info.fallback) h->mixedOff[kSolveSlot[j]] = true;   // FP32 cannot resolve this system
+                if (info.fallback) {
+                    const int used = h->infoMode[idx[(size_t)5 * k + j]];
+                    if (used == NSF_SOLVER_PCG_MIXED || used == NSF_SOLVER_PCG_FP64)
+                        h->pcgOff[kSolveSlot[j]] = true;    // the factor did not pay: plain CG from now on
+                    else
+                        h->mixedOff[kSolveSlot[j]] = true;  // FP32 cannot resolve this system
+                }
                 if (info.status != NSF_OK)
                     throw Error{info.status, "step " + std::to_string(done + k + 1) + ", " + names[j] + " solve: " +
                                                  status_text(info.status) + " after " +
@@ -386,6 +421,7 @@ void nsf_destroy(nsf_device* h) {
         if (h->stream) cudaStreamSynchronize(h->stream);
         for (auto e : h->evPool) cudaEventDestroy(e);
         for (int i = 0; i < NSF_SLOT_COUNT; ++i) h->mats[i] = Csr();
+        for (int i = 0; i < NSF_SLOT_COUNT; ++i) h->factors[i] = Factor();
         for (int i = 0; i < 4; ++i) scratch(h, i).release();
         if (h->stream) cudaStreamDestroy(h->stream);
     }
@@ -487,7 +523,7 @@ int nsf_conjugate_gradient_dev(nsf_device* h, int slot, const double* b_dev, con
     NSF_BEGIN(h)
     check_slot(slot);
     if (!b_dev || !x0_dev || !x_dev) throw bad_arg("null vector");
-    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (mode < NSF_SOLVER_FP64 || mode > NSF_SOLVER_PCG_FP64) throw bad_arg("unknown solver mode");
     if (!(eps > 0)) throw bad_arg("eps must be positive");
     const int idx = launch_solve(h, slot, mode, b_dev, x0_dev, x_dev, maxIterations, eps, nullptr);
     const CgInfo info = read_info(h, idx);
@@ -504,7 +540,7 @@ int nsf_conjugate_gradient(nsf_device* h, int slot, const double* b, const doubl
     const Csr& A = h->mats[slot];
     if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot is empty"};
     if (!b || !x0 || !x) throw bad_arg("null vector");
-    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (mode < NSF_SOLVER_FP64 || mode > NSF_SOLVER_PCG_FP64) throw bad_arg("unknown solver mode");
     if (!(eps > 0)) throw bad_arg("eps must be positive");
     DevBuf<double>& db = scratch(h, 0);
     DevBuf<double>& dx0 = scratch(h, 1);
@@ -606,6 +642,10 @@ int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, con
                   const int* pressureBCNodes, const double* bcP, double viscosity, double dt) {
     NSF_BEGIN(h)
     h->sim.ready = false;
+    for (int i = 0; i < NSF_SLOT_COUNT; ++i) {
+        h->factors[i] = Factor();
+        h->pcgOff[i] = false;
+    }
     setup_instance(h->mesh, h->sim, h->mats, h->stream, nNodes, xy, nElements, elements, nPressure, nVelocityBC,
                    velocityBCNodes, bcU, bcV, nPressureBC, pressureBCNodes, bcP, viscosity, dt);
     ensure_workspace(h, std::max(nNodes, nPressure));
@@ -794,14 +834,108 @@ int nsf_set_tolerance(nsf_device* h, double eps) {
 
 int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
     NSF_BEGIN(h)
-    if (mode != NSF_SOLVER_FP64 && mode != NSF_SOLVER_MIXED) throw bad_arg("unknown solver mode");
+    if (mode < NSF_SOLVER_FP64 || mode > NSF_SOLVER_PCG_FP64) throw bad_arg("unknown solver mode");
     if (innerTolerance > 0) h->innerTol = innerTolerance;
     h->solverMode = mode;
     for (bool& off : h->mixedOff) off = false;
-    if (mode == NSF_SOLVER_MIXED && h->sim.ready) {
+    for (bool& off : h->pcgOff) off = false;
+    if ((mode == NSF_SOLVER_MIXED || mode == NSF_SOLVER_PCG_MIXED) && h->sim.ready) {
         for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) prepare_matrix(h->mats[slot], true, h->stream);
         NSF_CUDA(cudaStreamSynchronize(h->stream));
     }
+    NSF_END(h)
+}
+
+// ---- preconditioners -------------------------------------------------------------------------------
+static Factor& factor_for(nsf_device* h, int slot, bool needValues) {
+    check_slot(slot);
+    Factor& F = h->factors[slot];
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
+    if (F.rows != A.rows || !F.lRowptr.get()) factor_structure(F, A, h->stream);
+    if (needValues && !F.ready) throw Error{NSF_ERR_STATE, "slot " + std::to_string(slot) + " has no factor values"};
+    return F;
+}
+
+int nsf_precond_pattern(nsf_device* h, int slot, int* colours, int64_t* nnzLower) {
+    NSF_BEGIN(h)
+    Factor& F = factor_for(h, slot, false);
+    if (colours) *colours = F.colours;
+    if (nnzLower) *nnzLower = F.nnzL;
+    NSF_END(h)
+}
+
+int nsf_precond_get_pattern(nsf_device* h, int slot, int* rowptr, int* col, unsigned char* colour) {
+    NSF_BEGIN(h)
+    Factor& F = factor_for(h, slot, false);
+    if (rowptr)
+        NSF_CUDA(cudaMemcpyAsync(rowptr, F.lRowptr.get(), sizeof(int) * (F.rows + 1), cudaMemcpyDeviceToHost, h->stream));
+    if (col && F.nnzL)
+        NSF_CUDA(cudaMemcpyAsync(col, F.lCol.get(), sizeof(int) * F.nnzL, cudaMemcpyDeviceToHost, h->stream));
+    if (colour)
+        NSF_CUDA(cudaMemcpyAsync(colour, F.colourOf.get(), F.rows, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_precond_ic0(nsf_device* h, int slot, double* shiftUsed) {
+    NSF_BEGIN(h)
+    Factor& F = factor_for(h, slot, false);
+    const double sh = factor_ic0(F, h->mats[slot], h->stream);
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    h->pcgOff[slot] = false;
+    if (shiftUsed) *shiftUsed = sh;
+    NSF_END(h)
+}
+
+int nsf_precond_set(nsf_device* h, int slot, const double* lower, const double* diag) {
+    NSF_BEGIN(h)
+    if (!diag || (!lower && h->factors[slot].nnzL)) throw bad_arg("null array");
+    Factor& F = factor_for(h, slot, false);
+    if (F.nnzL && !lower) throw bad_arg("null array");
+    for (int i = 0; i < F.rows; ++i)
+        if (!(diag[i] > 0.0) || !std::isfinite(diag[i])) throw bad_arg("factor diagonal must be positive and finite");
+    for (int64_t k = 0; k < F.nnzL; ++k)
+        if (!std::isfinite(lower[k])) throw bad_arg("factor values must be finite");
+    if (F.nnzL) NSF_CUDA(cudaMemcpyAsync(F.lVal.get(), lower, sizeof(double) * F.nnzL, cudaMemcpyHostToDevice, h->stream));
+    NSF_CUDA(cudaMemcpyAsync(F.diag.get(), diag, sizeof(double) * F.rows, cudaMemcpyHostToDevice, h->stream));
+    factor_fill(F, h->stream);
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    F.kind = NSF_PRECOND_LEARNED;
+    F.shift = 0.0;
+    h->pcgOff[slot] = false;
+    NSF_END(h)
+}
+
+int nsf_precond_get(nsf_device* h, int slot, double* lower, double* diag) {
+    NSF_BEGIN(h)
+    Factor& F = factor_for(h, slot, true);
+    if (lower && F.nnzL)
+        NSF_CUDA(cudaMemcpyAsync(lower, F.lVal.get(), sizeof(double) * F.nnzL, cudaMemcpyDeviceToHost, h->stream));
+    if (diag) NSF_CUDA(cudaMemcpyAsync(diag, F.diag.get(), sizeof(double) * F.rows, cudaMemcpyDeviceToHost, h->stream));
+    NSF_CUDA(cudaStreamSynchronize(h->stream));
+    NSF_END(h)
+}
+
+int nsf_precond_kind(nsf_device* h, int slot) {
+    if (!h || slot < 0 || slot >= NSF_SLOT_COUNT) return -NSF_ERR_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    return h->factors[slot].ready ? h->factors[slot].kind : NSF_PRECOND_NONE;
+}
+
+int nsf_precond_clear(nsf_device* h, int slot) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    h->factors[slot] = Factor();
+    h->pcgOff[slot] = false;
+    NSF_END(h)
+}
+
+int nsf_precond_cap(nsf_device* h, int slot, int maxIterations) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    if (maxIterations < 0) throw bad_arg("cap must be >= 0");
+    h->pcgCap[slot] = maxIterations;
     NSF_END(h)
 }
 
@@ -821,7 +955,7 @@ int nsf_profile(nsf_device* h, int enable) {
     NSF_END(h)
 }
 
-int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* rows, int64_t* nnz, int* iterations,
+int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* fallback, int* rows, int64_t* nnz, int* iterations,
                      int* outer, float* ms) {
     if (!h) return -NSF_ERR_BAD_ARG;
     std::lock_guard<std::recursive_mutex> lk(h->mu);
@@ -836,7 +970,8 @@ int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* r
             float t = 0;
             NSF_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
             if (slot) slot[i] = r.slot;
-            if (mode) mode[i] = all[r.infoIndex].fallback ? 2 : r.mode;
+            if (mode) mode[i] = r.mode;
+            if (fallback) fallback[i] = all[r.infoIndex].fallback;
             if (rows) rows[i] = r.rows;
             if (nnz) nnz[i] = r.nnz;
             if (iterations) iterations[i] = all[r.infoIndex].iterations;

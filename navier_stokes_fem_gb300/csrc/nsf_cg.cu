@@ -23,7 +23,7 @@
 // The mixed-precision form runs CG with FP32 matrix values and FP32 vectors (FP64 dots and scalars) and refines
 // it with FP64 reliable updates: the true residual b - A x is recomputed with the FP64 matrix whenever the FP32
 // residual has dropped by a fixed factor, without restarting the recurrence.
-#include "nsf_device.cuh"
+#include "nsf_pcg_device.cuh"
 
 namespace nsf {
 
@@ -42,18 +42,39 @@ __global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_kernel(CgArgs a) {
     team_cg_mixed(t, a, stage, smem);
 }
 
+__global__ void __launch_bounds__(kCgThreads, 2) pcg_fp64_kernel(CgArgs a) {
+    NSF_KERNEL_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_fp64(t, a, stage, smem);
+}
+
+__global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_kernel(CgArgs a) {
+    NSF_KERNEL_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_mixed(t, a, stage, smem);
+}
+
 // ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
+// Co-resident CTAs per SM of every persistent solver kernel (the grid must fit all of them).
+static int cg_occupancy() {
+    int occ = 1 << 30;
+    for (const void* fn : {(const void*)cg_fp64_kernel, (const void*)cg_mixed_kernel, (const void*)pcg_fp64_kernel,
+                           (const void*)pcg_mixed_kernel}) {
+        int o = 0;
+        NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kCgThreads, 0));
+        occ = std::min(occ, o);
+    }
+    return occ;
+}
+
 void cg_configure(CgWorkspace& ws, int device) {
     int sms = 0, coop = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NSF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
     if (!coop) throw Error{NSF_ERR_NO_DEVICE, "device does not support cooperative launches"};
-    int occ64 = 0, occMixed = 0;
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, 0));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, 0));
-    const int perSm = std::min(2, std::min(occ64, occMixed));
+    const int perSm = std::min(2, cg_occupancy());
     if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
     ws.grid = sms * perSm;
     ws.block = kCgThreads;
@@ -66,20 +87,21 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, cudaStream_t s) {
     NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
     CgArgs a = args;
     void* params[] = {&a};
-    const void* fn = mode == NSF_SOLVER_MIXED ? (const void*)cg_mixed_kernel : (const void*)cg_fp64_kernel;
+    const void* fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel
+                     : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel
+                     : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel
+                                                    : (const void*)cg_fp64_kernel;
     NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
     count_launch();
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.
 int cg_fp64_grid(int device, int* block) {
-    int sms = 0, coop = 0, occ64 = 0, occMixed = 0;
+    int sms = 0, coop = 0;
     NSF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     NSF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
     if (!coop) throw Error{NSF_ERR_NO_DEVICE, "device does not support cooperative launches"};
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, cg_fp64_kernel, kCgThreads, 0));
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occMixed, cg_mixed_kernel, kCgThreads, 0));
-    const int perSm = std::min(2, std::min(occ64, occMixed));
+    const int perSm = std::min(2, cg_occupancy());
     if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
     *block = kCgThreads;
     return sms * perSm;

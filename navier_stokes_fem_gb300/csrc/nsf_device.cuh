@@ -9,6 +9,7 @@ constexpr int kCgThreads = 256;
 constexpr int kWarps = kCgThreads / 32;
 constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
+constexpr int kRows = 4;      // rows per thread with their loads in flight in the vector phases
 
 // Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area.
 #define NSF_KERNEL_SHARED()          \
@@ -215,88 +216,124 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
 constexpr int kSlice = 32;
 constexpr int kUnroll = 8;
 
-// Loads entries [k0, k0 + kUnroll) of a lane's row in a slice (column -1 past the slice width W).
-template <typename TV>
+// Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W).
+template <int U, typename TV>
 __device__ __forceinline__ void sell_chunk(const int* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
-                                           int (&c)[kUnroll], TV (&v)[kUnroll]) {
+                                           int (&c)[U], TV (&v)[U]) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
+    for (int u = 0; u < U; ++u) {
         const bool in = k0 + u < W;
         c[u] = in ? ld_stream(cp + (k0 + u) * kSlice) : -1;
         v[u] = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
     }
 }
 
-// A warp walks its slices sFirst, sFirst + nw, ... with the next slice's first kUnroll matrix entries loaded
-// while the current slice's gathers are in flight, so a slice costs one memory latency, not two.  The slices'
-// start offsets are fetched 32 at a time, one per lane, and handed out by shuffles.
-template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
-__device__ __forceinline__ void sell_spmv(const int* __restrict__ sliceStart, const int* __restrict__ col,
-                                          const TV* __restrict__ val, int rb, int re, Gather gather, Epi epi) {
+// A warp walks its slices sFirst, sFirst + nw, ... as NS independent streams (the warp's slice list cut in NS
+// consecutive parts), each with the next slice's first U matrix entries loaded while the current slice's gathers
+// are in flight: a step costs one memory latency and serves NS slices.  The slices' start offsets are fetched 32
+// at a time, one per lane, and handed out by shuffles.
+// pre(row) is evaluated when a slice starts (its loads overlap the slice's), and its value goes to epi(row, sum,
+// pre); with Diff it must be the row's own vector entry.  Rows [rb, re): rb a multiple of 32 unless rb == re.
+template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename Gather, typename Pre,
+          typename Epi>
+__device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, const int* __restrict__ col,
+                                          const TV* __restrict__ val, int rb, int re, Gather gather, Pre pre,
+                                          Epi epi) {
+    using PreT = decltype(pre(0));
     if (rb >= re) return;   // (an empty range may start inside the last, partial slice)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int s1 = (re + kSlice - 1) / kSlice;
     const int sFirst = rb / kSlice + warp;
     if (sFirst >= s1) return;
-    const int count = (s1 - sFirst + nw - 1) / nw;
-    int mb = 0, me = 0;   // lane j: start and end of this warp's slice (block of 32) + j
-    auto meta_load = [&](int i0) {
-        const int idx = sFirst + (i0 + lane) * nw;
-        mb = idx < s1 ? sliceStart[idx] : 0;
-        me = idx < s1 ? sliceStart[idx + 1] : 0;
+    const int count = (s1 - sFirst + nw - 1) / nw;   // this warp's slices
+    const int per = (count + NS - 1) / NS;           // per stream: stream q takes i in [q per, (q + 1) per)
+    int mb[NS], me[NS], base[NS], W[NS], c[NS][U];
+    TV v[NS][U];
+    auto meta_load = [&](int q, int i0) {   // lane j: start / end of stream q's slice i0 + j
+        const int idx = sFirst + (q * per + i0 + lane) * nw;
+        const bool in = idx < s1 && i0 + lane < per;
+        mb[q] = in ? sliceStart[idx] : 0;
+        me[q] = in ? sliceStart[idx + 1] : 0;
     };
-    meta_load(0);
-    int base = __shfl_sync(0xffffffffu, mb, 0);
-    int W = (__shfl_sync(0xffffffffu, me, 0) - base) / kSlice;
-    int c[kUnroll];
-    TV v[kUnroll];
-    sell_chunk<TV>(col + base + lane, val + base + lane, W, 0, c, v);
-    for (int i = 0; i < count; ++i) {
-        const int row = (sFirst + i * nw) * kSlice + lane;
-        const bool own = row < re;
-        const TA self = own ? gather(row) : TA(0);
-        TA g[kUnroll];
-        TV vk[kUnroll];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            g[u] = c[u] >= 0 ? gather(c[u]) : TA(0);
-            vk[u] = v[u];
-        }
-        // the next slice's first entries, in flight with this slice's gathers
-        int baseN = 0, WN = 0;
-        if (i + 1 < count) {
-            if (((i + 1) & 31) == 0) meta_load(i + 1);
-            baseN = __shfl_sync(0xffffffffu, mb, (i + 1) & 31);
-            WN = (__shfl_sync(0xffffffffu, me, (i + 1) & 31) - baseN) / kSlice;
-        }
-        sell_chunk<TV>(col + baseN + lane, val + baseN + lane, WN, 0, c, v);
-        TA acc = TA(0);
+    for (int q = 0; q < NS; ++q) {
+        meta_load(q, 0);
+        base[q] = __shfl_sync(0xffffffffu, mb[q], 0);
+        W[q] = (__shfl_sync(0xffffffffu, me[q], 0) - base[q]) / kSlice;
+        sell_chunk<U, TV>(col + base[q] + lane, val + base[q] + lane, W[q], 0, c[q], v[q]);
+    }
+    for (int k = 0; k < per; ++k) {
+        int row[NS], Wc[NS], bc[NS];
+        bool live[NS];
+        PreT pv[NS];
+        TA g[NS][U];
+        TV vk[NS][U];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            if (u < W) {
-                if (Diff) acc = fma(TA(vk[u]), g[u] - self, acc);
-                else acc = fma(TA(vk[u]), g[u], acc);
+        for (int q = 0; q < NS; ++q) {
+            const int i = q * per + k;
+            live[q] = i < count;
+            row[q] = (sFirst + i * nw) * kSlice + lane;
+            pv[q] = live[q] && row[q] < re ? pre(row[q]) : PreT{};
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                g[q][u] = c[q][u] >= 0 ? gather(c[q][u]) : TA(0);
+                vk[q][u] = v[q][u];
             }
         }
-        // rows longer than kUnroll entries (P2 matrices): the rest of the slice, chunk by chunk
-        for (int k0 = kUnroll; k0 < W; k0 += kUnroll) {
-            int c2[kUnroll];
-            TV v2[kUnroll];
-            sell_chunk<TV>(col + base + lane, val + base + lane, W, k0, c2, v2);
+        // the streams' next slices: first entries in flight with this step's gathers
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) g[u] = c2[u] >= 0 ? gather(c2[u]) : TA(0);
+        for (int q = 0; q < NS; ++q) {
+            Wc[q] = W[q];
+            bc[q] = base[q];
+            int baseN = 0, WN = 0;
+            if (k + 1 < per && q * per + k + 1 < count) {
+                if (((k + 1) & 31) == 0) meta_load(q, k + 1);
+                baseN = __shfl_sync(0xffffffffu, mb[q], (k + 1) & 31);
+                WN = (__shfl_sync(0xffffffffu, me[q], (k + 1) & 31) - baseN) / kSlice;
+            }
+            sell_chunk<U, TV>(col + baseN + lane, val + baseN + lane, WN, 0, c[q], v[q]);
+            base[q] = baseN;
+            W[q] = WN;
+        }
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                if (c2[u] >= 0) {
-                    if (Diff) acc = fma(TA(v2[u]), g[u] - self, acc);
-                    else acc = fma(TA(v2[u]), g[u], acc);
+        for (int q = 0; q < NS; ++q) {
+            if (!live[q]) continue;
+            TA self = TA(0);
+            if constexpr (Diff) self = pv[q];
+            TA acc = TA(0);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (u < Wc[q]) {
+                    if (Diff) acc = fma(TA(vk[q][u]), g[q][u] - self, acc);
+                    else acc = fma(TA(vk[q][u]), g[q][u], acc);
                 }
             }
+            // rows longer than U entries (P2 matrices): the rest of the slice, chunk by chunk
+            for (int k0 = U; k0 < Wc[q]; k0 += U) {
+                int c2[U];
+                TV v2[U];
+                TA g2[U];
+                sell_chunk<U, TV>(col + bc[q] + lane, val + bc[q] + lane, Wc[q], k0, c2, v2);
+#pragma unroll
+                for (int u = 0; u < U; ++u) g2[u] = c2[u] >= 0 ? gather(c2[u]) : TA(0);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (c2[u] >= 0) {
+                        if (Diff) acc = fma(TA(v2[u]), g2[u] - self, acc);
+                        else acc = fma(TA(v2[u]), g2[u], acc);
+                    }
+                }
+            }
+            if (row[q] < re) epi(row[q], acc, pv[q]);
         }
-        if (own) epi(row, acc, self);
-        base = baseN;
-        W = WN;
     }
+}
+
+// sum_j a_ij gather(j) (or its difference form) with epi(row, sum, gather(row)).
+template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
+__device__ __forceinline__ void sell_spmv(const int* __restrict__ sliceStart, const int* __restrict__ col,
+                                          const TV* __restrict__ val, int rb, int re, Gather gather, Epi epi) {
+    sell_rows<TV, TA, Diff>(sliceStart, col, val, rb, re, gather, gather, epi);
 }
 
 // q = A p over the CTA's rows with epi(row, sum, p_row): the SELL-32 copy when the matrix has one, else the
@@ -390,15 +427,15 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
         const double alpha = rr / pqs;
         // phase B: x += alpha p, r -= alpha q, partial r.r (four rows per thread in flight)
         double rrn = 0;
-        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += 4 * bs) {
-            double pi[4], qi[4], xi[4], ri[4];
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
+            double pi[kRows], qi[kRows], xi[kRows], ri[kRows];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kRows; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) { pi[u] = p[i]; qi[u] = a.q[i]; xi[u] = a.x[i]; ri[u] = a.r[i]; }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kRows; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) {
                     a.x[i] = fma(alpha, pi[u], xi[u]);
@@ -418,15 +455,15 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
         rr = rrs;
         if (rr <= target) { status = NSF_OK; break; }
         // phase C: p = r + beta p; the next product gathers p across blocks, hence the third barrier
-        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += 4 * bs) {
-            double pi[4], ri[4];
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
+            double pi[kRows], ri[kRows];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kRows; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) { pi[u] = p[i]; ri[u] = a.r[i]; }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kRows; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) p[i] = fma(beta, pi[u], ri[u]);
             }
@@ -546,15 +583,15 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
             const float alphaf = (float)(rr / pqs);
             float rrHi = 0.f, rrLo = 0.f;
-            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += 4 * bs) {
-                float pi[4], qi[4], di[4], ri[4];
+            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
+                float pi[kRows], qi[kRows], di[kRows], ri[kRows];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kRows; ++u) {
                     const int i = i0 + u * bs;
                     if (i < re) { pi[u] = pc[i]; qi[u] = a.q32[i]; di[u] = a.d32[i]; ri[u] = a.r32[i]; }
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kRows; ++u) {
                     const int i = i0 + u * bs;
                     if (i < re) {
                         a.d32[i] = fmaf(alphaf, pi[u], di[u]);

@@ -95,6 +95,55 @@ struct Csr {
     bool valid() const { return rows > 0 && rowptr.ptr != nullptr; }
 };
 
+// Preconditioner factor M = L L^T (incomplete Cholesky or learned), in multicolour order: rows are greedily
+// coloured so that no two neighbours share a colour, and "lower" means a neighbour of a smaller colour.  The
+// triangular solves then run colour by colour, every row of a colour in parallel.
+constexpr int kMaxColours = 16;
+
+struct FactorView {
+    int colours = 0;
+    int colourRow[kMaxColours + 1] = {};      // colour c = permuted rows [colourRow[c], colourRow[c+1]) (x 32)
+    int nNatural = 0;                         // rows of the caller's system
+    const int* perm = nullptr;                // permuted row -> caller's row (-1: padding row)
+    const int* loStart = nullptr;             // lower part (L_ij, colour j < colour i), SELL-32, permuted rows
+    const int* loCol = nullptr;
+    const double* loVal = nullptr;
+    const float* loVal32 = nullptr;
+    const int* upStart = nullptr;             // upper part (L_ji, colour j > colour i)
+    const int* upCol = nullptr;
+    const double* upVal = nullptr;
+    const float* upVal32 = nullptr;
+    const double* dinv = nullptr;             // 1 / L_ii per permuted row (1 on padding rows)
+    const float* dinv32 = nullptr;
+    double* w = nullptr;                      // work vector: forward-sweep result, then M^-1 r (in place)
+    float* w32 = nullptr;
+    double* xp = nullptr;                     // the iterate and right-hand side in permuted order
+    double* bp = nullptr;
+};
+
+// The factor of one matrix.  The preconditioned solve runs on the colour-permuted system P A P^T, whose colour
+// blocks are padded to whole 32-row slices (padding rows are identity rows with zero right-hand side), so every
+// colour phase of the sweeps is a contiguous, slice-aligned row range.
+struct Factor {
+    int rows = 0, colours = 0, nPerm = 0;
+    int64_t nnzL = 0;                          // strictly lower entries
+    int colourRow[kMaxColours + 1] = {};
+    DevBuf<unsigned char> colourOf;            // per caller row
+    DevBuf<int> lRowptr, lCol;                 // canonical CSR of the strictly lower part (caller's rows), entries by
+                                               // (colour, column)
+    DevBuf<int> aIndexL, aIndexDiag;           // positions of L's entries / the diagonal in the matrix's CSR values
+    DevBuf<double> lVal, diag;                 // factor values on the canonical pattern and L_ii
+    DevBuf<int> perm;                          // permuted row -> caller's row (-1 padding)
+    Csr Ap;                                    // P A P^T (padded), with its SELL copies
+    DevBuf<int> apFrom;                        // Ap value k = A.val[apFrom[k]] (-1: padding diagonal, 1.0)
+    DevBuf<int> loStart, loCol, loFrom, upStart, upCol, upFrom;
+    DevBuf<double> loVal, upVal, dinv;
+    DevBuf<float> loVal32, upVal32, dinv32;
+    int kind = 0;                              // NSF_PRECOND_NONE / IC0 / LEARNED
+    double shift = 0.0;                        // diagonal shift the incomplete factorisation needed
+    bool ready = false;
+};
+
 // One solve's outcome, written by the CG kernels (device) and read back by the host.
 struct CgInfo {
     int iterations;      // inner iterations in total
@@ -124,6 +173,7 @@ struct CgArgs {
     const int* sellCol;
     const double* sellVal;
     const float* sellVal32;
+    FactorView f;            // preconditioned solvers only
     const double* b;
     const double* x0;
     double* x;
@@ -140,6 +190,7 @@ struct CgArgs {
     GridSync* sync;
     CgInfo* info;
     int maxIt;
+    int fallbackMaxIt;       // preconditioned solvers: iteration budget of the plain-CG fallback (0: what is left)
     double tol2;
     double innerTol2;
     int maxOuter;
@@ -158,8 +209,8 @@ struct CgArgs {
 
 // the workspace shared by every solve on a handle (sized for the largest system)
 struct CgWorkspace {
-    DevBuf<double> r, q, p0, p1;
-    DevBuf<float> r32, d32, q32, p32a, p32b;
+    DevBuf<double> r, q, p0, p1, w, xp, bp;
+    DevBuf<float> r32, d32, q32, p32a, p32b, w32;
     DevBuf<double> partials;
     DevBuf<GridSync> sync;
     DevBuf<CgInfo> info;     // ring of infos (one per solve in a step)
@@ -178,6 +229,12 @@ void axpy_bc_launch(int n, const double* a, double* y, const unsigned char* mask
 void make_fp32_values(Csr& A, cudaStream_t s);
 // SELL-32 copy (FP64 values; with fp32 also the FP32 values and row sums) for the CG kernels; no-op when current
 void prepare_matrix(Csr& A, bool fp32, cudaStream_t s);
+
+// preconditioner factors (nsf_precond.cu)
+void factor_structure(Factor& F, const Csr& A, cudaStream_t s);
+double factor_ic0(Factor& F, const Csr& A, cudaStream_t s);
+void factor_fill(Factor& F, cudaStream_t s);
+FactorView factor_view(const Factor& F, CgWorkspace& ws);
 
 // ------------------------------------------------------------------------------------------------
 // Mesh, point-location tree and simulation state
@@ -266,6 +323,9 @@ struct nsf_device {
     long long timeoutNs = 2000000000LL;
     int solverMode = NSF_SOLVER_FP64;
     bool mixedOff[NSF_SLOT_COUNT] = {};   // systems whose mixed solve stalled once: solved in FP64 from then on
+    nsf::Factor factors[NSF_SLOT_COUNT];  // preconditioners
+    int pcgCap[NSF_SLOT_COUNT] = {};      // iteration cap of a preconditioned solve (0: rows)
+    bool pcgOff[NSF_SLOT_COUNT] = {};     // systems whose preconditioned solve fell back: plain CG from then on
     // per-solve records (profiling of the persistent CG kernels)
     bool profile = false;
     std::vector<cudaEvent_t> evPool;
@@ -273,6 +333,7 @@ struct nsf_device {
     struct SolveRecord { int slot; int mode; int rows; int64_t nnz; cudaEvent_t a, b; int infoIndex; };
     std::vector<SolveRecord> records;
     int infoCursor = 0;
+    std::vector<int> infoMode;               // solver mode each info slot's solve ran with
     // batched form: instances, the launch plan and the captured step graph
     std::vector<std::unique_ptr<nsf::Instance>> batch;
     nsf::DevBuf<unsigned char> batchDesc;    // StepInstance array (nsf_step.cu)

@@ -1,0 +1,484 @@
+// Preconditioned conjugate gradients with a multicolour incomplete-Cholesky-shaped factor M = L L^T (the
+// reference's IC0Preconditioner path, include/assembly.h:33-35 and 1338-1344, and the learned factor).
+//
+// Rows are coloured so that neighbours never share a colour; L_ij (i != j) is non-zero only when colour(j) <
+// colour(i).  M^-1 r is then two sweeps of colour phases, every row of a colour independent of the others:
+//     forward,  c = 0 .. C-1:   y_i = (r_i - sum_{colour j < c} L_ij y_j) / L_ii
+//     backward, c = C-1 .. 0:   z_i = (y_i - sum_{colour j > c} L_ji z_j) / L_ii
+// Colour 0 of the forward sweep needs no neighbour, so it is fused into the phase that produces r; the backward
+// step of the last colour is z_i = y_i / L_ii and is fused into that colour's forward phase.  A solve with C
+// colours therefore spends 2C - 2 team barriers per iteration on the sweeps.  The factor's rows are stored as
+// SELL-32 slices over per-colour row lists, so a colour phase streams contiguous, coalesced slices.
+#pragma once
+#include "nsf_device.cuh"
+
+namespace nsf {
+
+// this CTA's share [r0, r1) of the rows [c0, c1) of one colour block (both multiples of 32), in whole slices
+__device__ __forceinline__ void team_block(int c0, int c1, const Team& t, int& r0, int& r1) {
+    const int chunk = ((c1 - c0) / kSlice + t.size - 1) / t.size * kSlice;
+    r0 = min(c1, c0 + t.rank * chunk);
+    r1 = min(c1, r0 + chunk);
+}
+
+// values a sweep row needs besides its sum, loaded when its slice starts
+template <typename TA> struct SweepRow {
+    TA src;   // r_i (forward) or y_i (backward)
+    TA d;     // 1 / L_ii
+    TA r;     // r_i (backward: the r.z term)
+};
+
+// Accumulator of r.z: FP64 for the FP64 solver, double-float for the mixed one.
+template <typename TA> struct DotAcc;
+template <> struct DotAcc<double> {
+    double v = 0.0;
+    __device__ void add(double a, double b) { v = fma(a, b, v); }
+    __device__ double value() const { return v; }
+};
+template <> struct DotAcc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ void add(float a, float b) { df_acc(hi, lo, a, b); }
+    __device__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Colour-0 rows of the forward sweep (permuted rows [0, colourRow[1])), fused into the phase that writes r_i:
+// y_i = r_i / L_ii (and, with a single colour, z_i = y_i / L_ii with its r.z term).
+template <typename TA>
+__device__ __forceinline__ void colour0_row(const FactorView& F, TA* w, const TA* dinv, int row, TA ri,
+                                            DotAcc<TA>& rz) {
+    if (row >= F.colourRow[1]) return;
+    const TA d = dinv[row];
+    TA y = ri * d;
+    if (F.colours == 1) {
+        y *= d;
+        rz.add(ri, y);
+    }
+    w[row] = y;
+}
+
+// colour0_row with 1 / L_ii already loaded (d; only read for colour-0 rows)
+template <typename TA>
+__device__ __forceinline__ void colour0_store(const FactorView& F, TA* w, int row, TA ri, TA d, DotAcc<TA>& rz) {
+    if (row >= F.colourRow[1]) return;
+    TA y = ri * d;
+    if (F.colours == 1) {
+        y *= d;
+        rz.add(ri, y);
+    }
+    w[row] = y;
+}
+
+// Forward colours 1..C-1 and backward colours C-2..0 of M^-1 r (colour 0 already done), then the grid-wide r.z.
+// Each colour phase is the pipelined SELL-32 product over the colour's rows of L (or L^T).  `rz` holds this
+// thread's r.z terms so far.  Returns false on a barrier timeout.
+template <typename TV, typename TA>
+__device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, const TV* loVal, const TV* upVal,
+                               const TA* dinv, DotAcc<TA>& rz, double* smem, int& where, double& rzOut) {
+    const FactorView& F = a.f;
+    const int C = F.colours;
+    for (int c = 1; c < C; ++c) {
+        int r0, r1;
+        team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
+        const bool last = c == C - 1;
+        sell_rows<TV, TA, false, 1, 4>(F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
+                                 [&](int i) { return SweepRow<TA>{r[i], dinv[i], TA(0)}; },
+                                 [&](int i, TA acc, const SweepRow<TA>& q) {
+                                     TA y = (q.src - acc) * q.d;
+                                     if (last) {   // backward step of the last colour: z_i = y_i / L_ii
+                                         y *= q.d;
+                                         rz.add(q.src, y);
+                                     }
+                                     w[i] = y;
+                                 });
+        if (!t.barrier(where++)) return false;
+    }
+    for (int c = C - 2; c >= 0; --c) {
+        int r0, r1;
+        team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
+        sell_rows<TV, TA, false, 1, 4>(F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
+                                 [&](int i) { return SweepRow<TA>{w[i], dinv[i], r[i]}; },
+                                 [&](int i, TA acc, const SweepRow<TA>& q) {
+                                     const TA z = (q.src - acc) * q.d;
+                                     rz.add(q.r, z);
+                                     w[i] = z;
+                                 });
+        if (c > 0 && !t.barrier(where++)) return false;
+    }
+    const double part = block_sum(rz.value(), smem);
+    if (threadIdx.x == 0) a.partials[4 * t.size + t.rank] = part;
+    if (!t.barrier(where++)) return false;
+    rzOut = grid_sum(a.partials + 4 * t.size, t.size, smem);
+    return true;
+}
+
+// The preconditioned solve runs on the colour-permuted system.  In: (the fused right-hand side is built in the
+// caller's order, then) b and x0 are gathered into permuted order; out: x is scattered back.  Returns the args of
+// the permuted solve (n = padded size, b = x0 = x = the permuted vectors), or false on a barrier timeout.
+static __device__ bool permute_in(Team& t, const CgArgs& a, double* stage, CgArgs& p, int& where) {
+    const FactorView& F = a.f;
+    int rb, re;
+    team_rows(F.nNatural, t, rb, re);
+    build_rhs(a, rb, re, stage);
+    if (a.bRowptr && !t.barrier(where++)) return false;
+    const double* b = a.bRowptr ? a.bOut : a.b;
+    team_rows(a.n, t, rb, re);
+    for (int i = rb + (int)threadIdx.x; i < re; i += blockDim.x) {
+        const int o = F.perm[i];
+        F.bp[i] = o >= 0 ? b[o] : 0.0;
+        F.xp[i] = o >= 0 ? a.x0[o] : 0.0;
+    }
+    if (!t.barrier(where++)) return false;
+    p = a;
+    p.bRowptr = nullptr;
+    p.b = F.bp;
+    p.x0 = F.xp;
+    p.x = F.xp;
+    return true;
+}
+
+static __device__ void permute_out(Team& t, const CgArgs& a) {
+    const FactorView& F = a.f;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    for (int i = rb + (int)threadIdx.x; i < re; i += blockDim.x) {
+        const int o = F.perm[i];
+        if (o >= 0) a.x[o] = F.xp[i];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// FP64 PCG.  partial regions: 0 = p.q, 1 = r.r, 2 = r0.r0, 3 = b.b, 4 = r.z
+// ---------------------------------------------------------------------------------------------------
+static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, double* smem) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    const double* b = a.bRowptr ? a.bOut : a.b;
+    double* w = F.w;
+    int where = 200;
+
+    build_rhs(a, rb, re, stage);
+    double rrp = 0, bbp = 0;
+    DotAcc<double> rz0;
+    warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.x0[c]; },
+                              [&](int row, double acc) {
+                                  const double bi = b[row];
+                                  const double ri = bi - acc;
+                                  a.r[row] = ri;
+                                  if (a.x != a.x0) a.x[row] = a.x0[row];
+                                  rrp = fma(ri, ri, rrp);
+                                  bbp = fma(bi, bi, bbp);
+                                  colour0_row<double>(F, w, F.dinv, row, ri, rz0);
+                              });
+    rrp = block_sum(rrp, smem);
+    bbp = block_sum(bbp, smem);
+    if (threadIdx.x == 0) { a.partials[2 * G + t.rank] = rrp; a.partials[3 * G + t.rank] = bbp; }
+    if (!t.barrier(where++)) { write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 1, 0, 0); return NSF_ERR_BARRIER_TIMEOUT; }
+    double rr = grid_sum(a.partials + 2 * G, G, smem);
+    const double bb = grid_sum(a.partials + 3 * G, G, smem);
+    const double target = bb > 0 ? a.tol2 * bb : a.tol2 * rr;
+    int it = 0, status = NSF_ERR_NOT_CONVERGED;
+    if (!(rr == rr) || !(bb == bb) || isinf(rr) || isinf(bb)) status = NSF_ERR_BREAKDOWN;
+    else if (rr <= target) status = NSF_OK;
+    double rz = 0, beta = 0;
+    if (status == NSF_ERR_NOT_CONVERGED) {
+        if (!precond_sweeps<double, double>(t, a, a.r, w, F.loVal, F.upVal, F.dinv, rz0, smem, where, rz)) {
+            write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb);
+            return NSF_ERR_BARRIER_TIMEOUT;
+        }
+        if (!(rz > 0.0) || isinf(rz)) status = NSF_ERR_BREAKDOWN;
+    }
+    double* p = a.pbuf0;
+    while (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
+        // p = z + beta p
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
+            double pi[kRows], wi[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    pi[u] = beta == 0.0 ? 0.0 : p[i];
+                    wi[u] = w[i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) p[i] = beta == 0.0 ? wi[u] : fma(beta, pi[u], wi[u]);
+            }
+        }
+        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+        // q = A p, p.q
+        double pq = 0;
+        matrix_product<double, double, false>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+                                              [&](int c) { return p[c]; },
+                                              [&](int row, double acc, double pr) {
+                                                  a.q[row] = acc;
+                                                  pq = fma(pr, acc, pq);
+                                              });
+        pq = block_sum(pq, smem);
+        if (threadIdx.x == 0) a.partials[t.rank] = pq;
+        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+        const double pqs = grid_sum(a.partials, G, smem);
+        if (!(pqs > 0.0) || isinf(pqs)) { status = NSF_ERR_BREAKDOWN; break; }
+        const double alpha = rz / pqs;
+        // x += alpha p, r -= alpha q, r.r, colour-0 rows of the forward sweep
+        double rrn = 0;
+        DotAcc<double> rzp;
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
+            double pi[kRows], qi[kRows], xi[kRows], ri[kRows], di[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    pi[u] = p[i];
+                    qi[u] = a.q[i];
+                    xi[u] = a.x[i];
+                    ri[u] = a.r[i];
+                    di[u] = i < F.colourRow[1] ? F.dinv[i] : 0.0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    a.x[i] = fma(alpha, pi[u], xi[u]);
+                    const double rn = fma(-alpha, qi[u], ri[u]);
+                    a.r[i] = rn;
+                    rrn = fma(rn, rn, rrn);
+                    colour0_store<double>(F, w, i, rn, di[u], rzp);
+                }
+            }
+        }
+        rrn = block_sum(rrn, smem);
+        if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
+        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+        rr = grid_sum(a.partials + G, G, smem);
+        ++it;
+        if (!(rr == rr) || isinf(rr)) { status = NSF_ERR_BREAKDOWN; break; }
+        if (rr <= target) { status = NSF_OK; break; }
+        double rzn = 0;
+        if (!precond_sweeps<double, double>(t, a, a.r, w, F.loVal, F.upVal, F.dinv, rzp, smem, where, rzn)) {
+            write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb);
+            return NSF_ERR_BARRIER_TIMEOUT;
+        }
+        if (!(rzn > 0.0) || isinf(rzn)) { status = NSF_ERR_BREAKDOWN; break; }
+        beta = rzn / rz;
+        rz = rzn;
+    }
+    if (status == NSF_ERR_NOT_CONVERGED && a.fallbackMaxIt > 0) {
+        // over the cap: plain FP64 CG from the current iterate (x is complete after the last barrier)
+        CgArgs f = a;
+        f.bRowptr = nullptr;
+        f.b = b;
+        f.x0 = a.x;
+        f.maxIt = a.fallbackMaxIt;
+        const int fst = team_cg_fp64(t, f, stage, smem);
+        if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
+        if (t.rank == 0 && threadIdx.x == 0) {
+            a.info->iterations += it;
+            a.info->fallback = 1;
+        }
+        return fst;
+    }
+    write_info(t, a, it, status, 1, rr, bb);
+    return status;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Mixed-precision PCG: the mixed CG of nsf_device.cuh (FP32 matrix, vectors and factor; FP64 dots, scalars,
+// true residuals) with z = M^-1 r applied in FP32 after every update of r.  The search direction is formed on the
+// fly in the product, p_j = z_j + beta p_prev_j.  If the recurrence stalls, or the preconditioned method needs
+// more iterations than the caller allows (the plain method's count), the solve finishes with plain FP64 CG.
+// partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r.z
+// ---------------------------------------------------------------------------------------------------
+static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, double* smem) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    const double* b = a.bRowptr ? a.bOut : a.b;
+    float* w = F.w32;
+
+    build_rhs(a, rb, re, stage);
+    if (a.x != a.x0)
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] = a.x0[i];
+
+    int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 300, stalls = 0;
+    double rr64 = 0, bb = 0, target = 0, rz = 0, beta = 0.0, rrBest = INFINITY;
+    float* pprev = a.p32a;
+    float* pcur = a.p32b;
+    bool first = true, resetP = true, timedOut = false;
+    while (true) {
+        // true residual r = b - A64 x, r32 = (float) r, d32 = 0, colour 0 of the forward sweep
+        const double* xs = first ? a.x0 : a.x;
+        double rrp = 0, bbp = 0;
+        DotAcc<float> rzp;
+        warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xs[c]; },
+                                  [&](int row, double acc) {
+                                      const double bi = b[row];
+                                      const double ri = bi - acc;
+                                      const float r32 = (float)ri;
+                                      a.r32[row] = r32;
+                                      a.d32[row] = 0.0f;
+                                      if (resetP) pprev[row] = 0.0f;   // restart: p = z (beta = 0)
+                                      rrp = fma(ri, ri, rrp);
+                                      bbp = fma(bi, bi, bbp);
+                                      colour0_row<float>(F, w, F.dinv32, row, r32, rzp);
+                                  });
+        rrp = block_sum(rrp, smem);
+        bbp = block_sum(bbp, smem);
+        if (threadIdx.x == 0) {
+            a.partials[2 * G + t.rank] = rrp;
+            a.partials[3 * G + t.rank] = bbp;
+        }
+        if (!t.barrier(where++)) { timedOut = true; break; }
+        rr64 = grid_sum(a.partials + 2 * G, G, smem);
+        if (first) {
+            bb = grid_sum(a.partials + 3 * G, G, smem);
+            target = bb > 0 ? a.tol2 * bb : a.tol2 * rr64;
+        }
+        if (!(rr64 == rr64) || isinf(rr64)) { status = NSF_ERR_BREAKDOWN; break; }
+        if (rr64 <= target) { status = NSF_OK; break; }
+        if (it >= a.maxIt || refresh >= a.maxOuter) break;
+        if (refresh > 0 && rr64 > 0.81 * rrBest) {   // stagnation guard (see team_cg_mixed)
+            if (++stalls >= 3) break;
+        } else {
+            stalls = 0;
+        }
+        rrBest = fmin(rrBest, rr64);
+        double rzT = 0;
+        if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT)) {
+            timedOut = true;
+            break;
+        }
+        if (!(rzT > 0.0) || isinf(rzT)) { status = NSF_ERR_BREAKDOWN; break; }
+        // every refresh restarts the preconditioned recurrence (p = z): on the ill-conditioned pressure systems an
+        // FP32 preconditioned recurrence carried across refreshes converged up to 2x slower than restarted cycles
+        beta = 0.0;
+        resetP = true;
+        rz = rzT;
+        const double rrRef = rr64;
+        const int itRef = it;
+        ++refresh;
+        first = false;
+
+        bool innerBreakdown = false;
+        while (it < a.maxIt) {
+            const float betaf = (float)beta;
+            const float* pp = pprev;
+            float* pc = pcur;
+            float pqHi = 0.f, pqLo = 0.f;
+            matrix_product<float, float, true>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
+                                               reinterpret_cast<float*>(stage),
+                                               [&](int c) { return fmaf(betaf, pp[c], w[c]); },
+                                               [&](int row, float acc, float pi) {
+                                                   acc = fmaf(a.rowsum32[row], pi, acc);
+                                                   pc[row] = pi;
+                                                   a.q32[row] = acc;
+                                                   df_acc(pqHi, pqLo, pi, acc);
+                                               });
+            const double pq = block_sum((double)pqHi + (double)pqLo, smem);
+            if (threadIdx.x == 0) a.partials[t.rank] = pq;
+            if (!t.barrier(where++)) { timedOut = true; break; }
+            const double pqs = grid_sum(a.partials, G, smem);
+            if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
+            const float alphaf = (float)(rz / pqs);
+            float rrHi = 0.f, rrLo = 0.f;
+            DotAcc<float> rzn;
+            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
+                float pi[kRows], qi[kRows], di[kRows], ri[kRows], vi[kRows];
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const int i = i0 + u * bs;
+                    if (i < re) {
+                        pi[u] = pc[i];
+                        qi[u] = a.q32[i];
+                        di[u] = a.d32[i];
+                        ri[u] = a.r32[i];
+                        vi[u] = i < F.colourRow[1] ? F.dinv32[i] : 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const int i = i0 + u * bs;
+                    if (i < re) {
+                        a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                        const float rn = fmaf(-alphaf, qi[u], ri[u]);
+                        a.r32[i] = rn;
+                        df_acc(rrHi, rrLo, rn, rn);
+                        colour0_store<float>(F, w, i, rn, vi[u], rzn);
+                    }
+                }
+            }
+            const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
+            if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
+            if (!t.barrier(where++)) { timedOut = true; break; }
+            const double rrs = grid_sum(a.partials + G, G, smem);
+            ++it;
+            { float* tmp = pprev; pprev = pcur; pcur = tmp; }
+            if (!(rrs == rrs) || isinf(rrs)) { innerBreakdown = true; break; }
+            if (rrs <= a.innerTol2 * rrRef || rrs <= target) break;   // time for a true residual
+            if (it - itRef >= kMaxInnerBetweenRefresh) break;
+            double rzs = 0;
+            if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzn, smem, where, rzs)) {
+                timedOut = true;
+                break;
+            }
+            if (!(rzs > 0.0) || isinf(rzs)) { innerBreakdown = true; break; }
+            beta = rzs / rz;
+            rz = rzs;
+        }
+        if (timedOut) break;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
+        if (!t.barrier(where++)) { timedOut = true; break; }
+        if (innerBreakdown) resetP = true;
+    }
+    if (timedOut) {
+        write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb);
+        return NSF_ERR_BARRIER_TIMEOUT;
+    }
+    if (status == NSF_ERR_NOT_CONVERGED && (a.fallbackMaxIt > 0 || it < a.maxIt)) {
+        // plain FP64 CG from the current iterate, with the plain method's own iteration budget
+        CgArgs f = a;
+        f.bRowptr = nullptr;
+        f.b = b;
+        f.x0 = a.x;
+        f.maxIt = a.fallbackMaxIt > 0 ? a.fallbackMaxIt : a.maxIt - it;
+        const int fst = team_cg_fp64(t, f, stage, smem);
+        if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
+        if (t.rank == 0 && threadIdx.x == 0) {
+            a.info->iterations += it;
+            a.info->outer = refresh;
+            a.info->fallback = 1;
+        }
+        return fst;
+    }
+    write_info(t, a, it, status, refresh, rr64, bb);
+    return status;
+}
+
+// Preconditioned solves of the caller's system: permute in, solve the colour-permuted system, permute out.
+template <typename Body>
+__device__ int team_pcg(Team& t, const CgArgs& a, double* stage, double* smem, Body body) {
+    int where = 190;
+    CgArgs p;
+    if (!permute_in(t, a, stage, p, where)) {
+        write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
+        return NSF_ERR_BARRIER_TIMEOUT;
+    }
+    const int st = body(t, p, stage, smem);
+    if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
+    return st;
+}
+
+static __device__ int team_pcg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_pcg(t, a, stage, smem, pcg_fp64_body);
+}
+
+static __device__ int team_pcg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_pcg(t, a, stage, smem, pcg_mixed_body);
+}
+
+}  // namespace nsf

@@ -82,6 +82,16 @@ def lib():
         L.orc_set_tolerance.argtypes = [_p, _d]
         L.orc_point_in_triangle.restype = _i
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
+        _u8ptr = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+        L.orc_mc_colour.restype = _i
+        L.orc_mc_colour.argtypes = [_i, _lptr, _iptr, _u8ptr]
+        L.orc_mc_lower.restype = ctypes.c_int64
+        L.orc_mc_lower.argtypes = [_i, _lptr, _iptr, _u8ptr, _p, _p, _p, _p]
+        L.orc_ic0.restype = _i
+        L.orc_ic0.argtypes = [_i, _i, _u8ptr, _lptr, _iptr, _lptr, _lptr, _dptr, _d, _dptr, _dptr]
+        L.orc_pcg.restype = _i
+        L.orc_pcg.argtypes = [_i, _lptr, _iptr, _dptr, _i, _u8ptr, _lptr, _iptr, _dptr, _dptr, _dptr, _dptr, _dptr,
+                              _i, _d, ctypes.POINTER(_i), ctypes.POINTER(_d)]
         _LIB = L
     return _LIB
 
@@ -354,6 +364,61 @@ class ReferenceTree:
         out = np.zeros(4, np.float32)
         ref_lib().ref_grid_bbox(self._h, out)
         return out
+
+
+# ---------------------------------------------------------------------------------------------------
+# Multicolour IC(0) preconditioner and PCG (precond_oracle.cpp)
+# ---------------------------------------------------------------------------------------------------
+class McFactor:
+    """Multicolour pattern of a CSR matrix (scipy), its IC(0) values, and PCG with M = L L^T."""
+
+    def __init__(self, A):
+        A = A.tocsr()
+        A.sort_indices()
+        self.A = A
+        self.n = A.shape[0]
+        self.rp = np.ascontiguousarray(A.indptr, np.int64)
+        self.ci = np.ascontiguousarray(A.indices, np.int32)
+        self.av = np.ascontiguousarray(A.data, np.float64)
+        L = lib()
+        self.colour = np.zeros(self.n, np.uint8)
+        self.colours = L.orc_mc_colour(self.n, self.rp, self.ci, self.colour)
+        nnz = L.orc_mc_lower(self.n, self.rp, self.ci, self.colour, None, None, None, None)
+        self.lrp = np.zeros(self.n + 1, np.int64)
+        self.lci = np.zeros(max(nnz, 1), np.int32)
+        self.aidx = np.zeros(max(nnz, 1), np.int64)
+        self.adiag = np.full(self.n, -1, np.int64)
+        L.orc_mc_lower(self.n, self.rp, self.ci, self.colour, self.lrp.ctypes.data, self.lci.ctypes.data,
+                       self.aidx.ctypes.data, self.adiag.ctypes.data)
+        self.nnz_lower = int(nnz)
+        self.lval = np.zeros(max(nnz, 1))
+        self.diag = np.ones(self.n)
+        self.shift = 0.0
+
+    def ic0(self):
+        """IC(0) values; on breakdown retried with a diagonal shift of 1e-3, 1e-2, ... (as the GPU path does)."""
+        shift = 0.0
+        for _ in range(8):
+            failed = lib().orc_ic0(self.n, self.colours, self.colour, self.lrp, self.lci, self.aidx, self.adiag,
+                                   self.av, shift, self.lval, self.diag)
+            if not failed:
+                self.shift = shift
+                return shift
+            shift = 1e-3 if shift == 0.0 else shift * 10
+        raise RuntimeError("IC(0) broke down")
+
+    def set(self, lower, diag):
+        self.lval[: self.nnz_lower] = lower
+        self.diag[:] = diag
+
+    def pcg(self, b, x0, max_iter=-1, tol=1e-8):
+        x = np.zeros(self.n)
+        it, rel = _i(), _d()
+        st = lib().orc_pcg(self.n, self.rp, self.ci, self.av, self.colours, self.colour, self.lrp, self.lci,
+                           self.lval, self.diag, np.ascontiguousarray(b, np.float64),
+                           np.ascontiguousarray(x0, np.float64), x, int(max_iter), float(tol), ctypes.byref(it),
+                           ctypes.byref(rel))
+        return x, it.value, rel.value, st
 
 
 def set_threads(n: int) -> None:

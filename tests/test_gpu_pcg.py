@@ -1,0 +1,147 @@
+"""Preconditioned CG on the GPU: the multicolour pattern and IC(0) factor against the oracle's, FP64 PCG
+against the oracle's PCG, mixed-precision PCG to the FP64 residual, installed (learned-path) factors, the
+fallback to plain CG over the iteration cap, and whole steps with the pressure solve preconditioned."""
+import numpy as np
+import pytest
+
+import navier_stokes_fem_gb300 as nsf
+import oracle
+from navier_stokes_fem_gb300 import mesh as M
+from tests._meshes import rel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-8
+NAMES = ["pressure_stiffness", "diffusion"]
+
+
+@pytest.fixture(scope="module")
+def system():
+    m = M.cavity(32)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    d = nsf.GPUSimulationDevice(0)
+    for name in ("pressure_stiffness", "diffusion", "velocity_mass"):
+        rp, col, val, shape = o.matrix(name)
+        d.upload_matrix(name, rp.astype(np.int32), col, val, shape)
+    yield d, o
+    d.close()
+
+
+def _relres(o, name, x, b):
+    A = o.scipy_matrix(name)
+    return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_pattern_and_ic0_match_oracle(system, name):
+    d, o = system
+    rp, col, colour = d.precond_pattern(name)
+    F = oracle.McFactor(o.scipy_matrix(name))
+    assert np.array_equal(colour, F.colour)
+    assert np.array_equal(rp, F.lrp) and np.array_equal(col, F.lci[:F.nnz_lower])
+    assert d.precond_ic0(name) == F.ic0()
+    lower, diag = d.precond_get(name)
+    assert np.abs(lower - F.lval[:F.nnz_lower]).max() <= 1e-12 * np.abs(F.lval).max()
+    assert np.abs(diag - F.diag).max() <= 1e-12 * np.abs(F.diag).max()
+    assert d.precond_kind(name) == "ic0"
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp64_pcg_matches_oracle_pcg(system, name):
+    d, o = system
+    d.precond_ic0(name)
+    n = d.matrix_shape(name)[0]
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal(n)
+    x0 = 0.1 * rng.standard_normal(n)
+    x, it, rr = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_fp64")
+    F = oracle.McFactor(o.scipy_matrix(name))
+    F.ic0()
+    xr, itr, _, st = F.pcg(b, x0, tol=TOL)
+    assert st == 0
+    assert abs(it - itr) <= max(2, itr // 50)
+    assert _relres(o, name, x, b) < 1.5 * TOL
+    assert rel(x, xr) < 1e-6
+    _, it_plain, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="fp64")
+    assert it < it_plain
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_mixed_pcg_reaches_fp64_residual(system, name):
+    d, o = system
+    d.precond_ic0(name)
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(6).standard_normal(n)
+    x, it, rr = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_mixed")
+    xr, st, itr, _ = o.cg(name, b, np.zeros(n), tol=TOL)
+    assert _relres(o, name, x, b) < 1.5 * TOL           # the FP64 true residual drives the refinement loop
+    assert rel(x, xr) < 1e-6
+    assert it < itr
+
+
+def test_installed_factor_is_used_as_given(system):
+    """nsf_precond_set is the learned preconditioner's entry point: IC(0) values installed through it must give
+    the IC(0) solve, and the identity factor must give plain CG."""
+    d, o = system
+    name = "pressure_stiffness"
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(7).standard_normal(n)
+    d.precond_ic0(name)
+    _, it_ic0, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
+    lower, diag = d.precond_get(name)
+    d.precond_clear(name)
+    assert d.precond_kind(name) == "none"
+    d.precond_set(name, lower, diag)
+    assert d.precond_kind(name) == "learned"
+    _, it_set, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
+    assert it_set == it_ic0
+    d.precond_set(name, np.zeros_like(lower), np.ones(n))
+    _, it_id, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
+    _, it_plain, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="fp64")
+    assert abs(it_id - it_plain) <= 1
+    with pytest.raises(nsf.NSFemError):
+        d.precond_set(name, lower, -diag)
+    d.precond_ic0(name)
+
+
+@pytest.mark.parametrize("solver", ["pcg_fp64", "pcg_mixed"])
+def test_over_the_cap_falls_back_to_plain_cg(system, solver):
+    d, o = system
+    name = "pressure_stiffness"
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(8).standard_normal(n)
+    d.precond_ic0(name)
+    d.precond_cap(name, 3)
+    d.profile(True)
+    x, it, rr = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver=solver)
+    prof = d.profile_read()
+    d.profile(False)
+    d.precond_cap(name, 0)
+    assert prof["fallback"][-1] == 1
+    assert _relres(o, name, x, b) < 1.5 * TOL
+
+
+@pytest.mark.parametrize("solver", ["pcg_fp64", "pcg_mixed"])
+def test_steps_with_preconditioned_pressure_match_oracle(solver):
+    """Solvers that stop at the same 1e-8 relative residual differ by ~cond(A) * 1e-8 in the solution, so the
+    preconditioned runs are held against the discrete solution (the oracle driven to 1e-13): within 1e-3, and of
+    the same size as the plain FP64 path's own error."""
+    m = M.cavity(24)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    o.set_tolerance(1e-13)
+    st, rit = o.step(10)
+    assert st == 0
+    ruv, rp = o.fields()
+
+    def run(solver, precondition):
+        sim = nsf.NavierStokesAssembly(m, 0.01, 0.01, solver=solver)
+        if precondition:
+            sim.precond_ic0("pressure_stiffness")
+        it = sim.step(10)
+        uv, p = sim.fields()
+        sim.close()
+        return max(rel(uv, ruv), rel(p, rp)), it
+
+    err, it = run(solver, True)
+    err_plain, it_plain = run("fp64", False)
+    assert err < 1e-3 and err < 10 * err_plain + 1e-7
+    assert it[:, 2].sum() < 0.7 * it_plain[:, 2].sum()     # the pressure solves need far fewer iterations

@@ -130,6 +130,36 @@ int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
 int nsf_precond_cap(nsf_device* h, int slot, int maxIterations);
 
+/* ---- the learned preconditioner ----------------------------------------------------------------------
+ * An edge-based message-passing network over the factor pattern's graph outputs L (M = L L^T) for a system
+ * matrix; trained on the GPU (forward, backward and Adam kernels; BF16 tensor-core layers with FP32 accumulation)
+ * on pairs (A, x, b) the plain method produced, with loss ||L^ L^T x^ - b^||^2 / ||b^||^2 on the diagonally scaled
+ * system.  The learner is bound to a device handle and uses its stream. */
+typedef struct nsf_learner nsf_learner;
+int nsf_learn_create(nsf_device* h, uint64_t seed, nsf_learner** out);
+void nsf_learn_destroy(nsf_learner* L);
+const char* nsf_learn_last_error(const nsf_learner* L);
+int nsf_learn_param_count(nsf_learner* L, int64_t* count);
+int nsf_learn_get_params(nsf_learner* L, float* theta);
+/* Replaces the parameters (and resets the Adam state). */
+int nsf_learn_set_params(nsf_learner* L, const float* theta);
+/* Stores a training system: the slot's current matrix (its graph and features) with a solution x of A x = b. */
+int nsf_learn_add_system(nsf_learner* L, int slot, const double* x, const double* b, int* index);
+int nsf_learn_clear_systems(nsf_learner* L);
+int nsf_learn_system_size(nsf_learner* L, int index, int* nodes, int64_t* edges);
+/* The network's scaled factor on a stored system: lower[edges] (factor pattern order), diag[nodes]. */
+int nsf_learn_forward(nsf_learner* L, int index, float* lower, float* diag);
+/* Loss of a stored system and its gradient with respect to the parameters. */
+int nsf_learn_loss_grad(nsf_learner* L, int index, double* loss, float* grad);
+/* `steps` Adam steps, each on the mean gradient of `batch` systems drawn from the store; losses[steps] or NULL. */
+int nsf_learn_train(nsf_learner* L, int steps, int batch, double lr, uint64_t seed, float* losses);
+/* Runs the network on the slot's matrix and installs its factor as the slot's preconditioner. */
+int nsf_learn_apply(nsf_learner* L, int slot);
+/* One tensor-core dense layer on host arrays: Y[rows x N] = epilogue(X[rows x K] W[K x N] + bias), X and W
+ * rounded to BF16, FP32 accumulation; epilogue 0 none, 1 ReLU; K and N multiples of 16 up to 128. */
+int nsf_tc_dense(nsf_device* h, int rows, int K, int N, const float* X, const float* W, const float* bias,
+                 int epilogue, float* Y);
+
 /* ---- mesh, point location and advection (uploadKDTree; advect; KDTree::findElement) ------------------ */
 /* Uploads the mesh and builds the point-location tree on the GPU over triangle centroids. */
 int nsf_upload_mesh(nsf_device* h, int nNodes, const float* xy, int nElements, const int* elements, int nPressure);

@@ -98,6 +98,20 @@ _SIGS = {
     "nsf_precond_kind": (_i, [_v, _i]),
     "nsf_precond_clear": (_i, [_v, _i]),
     "nsf_precond_cap": (_i, [_v, _i, _i]),
+    "nsf_tc_dense": (_i, [_v, _i, _i, _i, _arr(np.float32), _arr(np.float32), _v, _i, _arr(np.float32)]),
+    "nsf_learn_create": (_i, [_v, ctypes.c_uint64, _P(_v)]),
+    "nsf_learn_destroy": (None, [_v]),
+    "nsf_learn_last_error": (ctypes.c_char_p, [_v]),
+    "nsf_learn_param_count": (_i, [_v, _P(_i64)]),
+    "nsf_learn_get_params": (_i, [_v, _arr(np.float32)]),
+    "nsf_learn_set_params": (_i, [_v, _arr(np.float32)]),
+    "nsf_learn_add_system": (_i, [_v, _i, _arr(np.float64), _arr(np.float64), _P(_i)]),
+    "nsf_learn_clear_systems": (_i, [_v]),
+    "nsf_learn_system_size": (_i, [_v, _i, _P(_i), _P(_i64)]),
+    "nsf_learn_forward": (_i, [_v, _i, _arr(np.float32), _arr(np.float32)]),
+    "nsf_learn_loss_grad": (_i, [_v, _i, _P(_d), _arr(np.float32)]),
+    "nsf_learn_train": (_i, [_v, _i, _i, _d, ctypes.c_uint64, _v]),
+    "nsf_learn_apply": (_i, [_v, _i]),
     "nsf_timer": (_i, [_v, _i, _P(_f)]),
     "nsf_host_alloc": (_i, [_v, _sz, _P(_v)]),
     "nsf_host_free": (_i, [_v, _v]),
@@ -427,6 +441,99 @@ class GPUSimulationDevice:
         buf = (ctypes.c_byte * max(nbytes, 1)).from_address(p.value)
         arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
         return arr
+
+
+class Learner:
+    """The learned preconditioner (nsf_learn_*): a message-passing network that outputs the factor L of a slot's
+    matrix, trained on the GPU on (matrix, solution, right-hand side) triples of the plain method."""
+
+    def __init__(self, device: "GPUSimulationDevice", seed: int = 0):
+        self.device = device
+        h = _v()
+        st = library().nsf_learn_create(device._h, ctypes.c_uint64(seed), ctypes.byref(h))
+        if st != 0:
+            raise NSFemError(st, library().nsf_last_error(device._h).decode())
+        self._h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise NSFemError(st, library().nsf_learn_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().nsf_learn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def param_count(self) -> int:
+        n = _i64()
+        self._check(library().nsf_learn_param_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def params(self):
+        th = np.zeros(self.param_count, np.float32)
+        self._check(library().nsf_learn_get_params(self._h, th))
+        return th
+
+    def set_params(self, theta):
+        self._check(library().nsf_learn_set_params(self._h, np.ascontiguousarray(theta, np.float32)))
+
+    def add_system(self, slot, x, b) -> int:
+        idx = _i()
+        self._check(library().nsf_learn_add_system(self._h, _slot(slot), np.ascontiguousarray(x, np.float64),
+                                                   np.ascontiguousarray(b, np.float64), ctypes.byref(idx)))
+        return idx.value
+
+    def clear_systems(self):
+        self._check(library().nsf_learn_clear_systems(self._h))
+
+    def system_size(self, index):
+        n, m = _i(), _i64()
+        self._check(library().nsf_learn_system_size(self._h, int(index), ctypes.byref(n), ctypes.byref(m)))
+        return n.value, m.value
+
+    def forward(self, index):
+        """(L^ off-diagonal values in the factor pattern's order, L^ diagonal) of a stored system."""
+        n, m = self.system_size(index)
+        lower, diag = np.zeros(max(m, 1), np.float32), np.zeros(n, np.float32)
+        self._check(library().nsf_learn_forward(self._h, int(index), lower, diag))
+        return lower[:m], diag
+
+    def loss_grad(self, index):
+        loss = _d()
+        g = np.zeros(self.param_count, np.float32)
+        self._check(library().nsf_learn_loss_grad(self._h, int(index), ctypes.byref(loss), g))
+        return loss.value, g
+
+    def train(self, steps, batch=1, lr=1e-3, seed=0):
+        losses = np.zeros(max(steps, 1), np.float32)
+        self._check(library().nsf_learn_train(self._h, int(steps), int(batch), float(lr), ctypes.c_uint64(seed),
+                                              losses.ctypes.data_as(_v)))
+        return losses[:steps]
+
+    def apply(self, slot):
+        """Installs the network's factor for the slot's current matrix (preconditioner kind "learned")."""
+        self._check(library().nsf_learn_apply(self._h, _slot(slot)))
+
+
+def tc_dense(device, X, W, bias=None, relu=False):
+    """One tensor-core dense layer (BF16 operands, FP32 accumulation): relu?(X W + bias)."""
+    X = np.ascontiguousarray(X, np.float32)
+    W = np.ascontiguousarray(W, np.float32)
+    rows, K = X.shape
+    N = W.shape[1]
+    Y = np.zeros((rows, N), np.float32)
+    b = None if bias is None else np.ascontiguousarray(bias, np.float32)
+    st = library().nsf_tc_dense(device._h, rows, K, N, X.reshape(-1), W.reshape(-1),
+                                b.ctypes.data_as(_v) if b is not None else None, 1 if relu else 0, Y.reshape(-1))
+    device._check(st)
+    return Y
 
 
 class NavierStokesAssembly(GPUSimulationDevice):

@@ -105,6 +105,16 @@ void setup_instance(MeshDev& m, SimState& S, Csr* mats, cudaStream_t s, int nNod
     NSF_CUDA(cudaStreamSynchronize(s));
 }
 
+Factor& factor_for(nsf_device* h, int slot, bool needValues) {
+    if (slot < 0 || slot >= NSF_SLOT_COUNT) throw bad_arg("matrix slot out of range");
+    Factor& F = h->factors[slot];
+    const Csr& A = h->mats[slot];
+    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
+    if (F.rows != A.rows || !F.lRowptr.get()) factor_structure(F, A, h->stream);
+    if (needValues && !F.ready) throw Error{NSF_ERR_STATE, "slot " + std::to_string(slot) + " has no factor values"};
+    return F;
+}
+
 }  // namespace nsf
 
 std::atomic<long long> nsf::g_launches{0};
@@ -847,16 +857,6 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
 }
 
 // ---- preconditioners -------------------------------------------------------------------------------
-static Factor& factor_for(nsf_device* h, int slot, bool needValues) {
-    check_slot(slot);
-    Factor& F = h->factors[slot];
-    const Csr& A = h->mats[slot];
-    if (!A.valid()) throw Error{NSF_ERR_STATE, "matrix slot " + std::to_string(slot) + " is empty"};
-    if (F.rows != A.rows || !F.lRowptr.get()) factor_structure(F, A, h->stream);
-    if (needValues && !F.ready) throw Error{NSF_ERR_STATE, "slot " + std::to_string(slot) + " has no factor values"};
-    return F;
-}
-
 int nsf_precond_pattern(nsf_device* h, int slot, int* colours, int64_t* nnzLower) {
     NSF_BEGIN(h)
     Factor& F = factor_for(h, slot, false);

@@ -350,6 +350,8 @@ struct nsf_device {
 };
 
 namespace nsf {
+// the slot's factor with its pattern built (values too when needValues); nsf_api.cu
+Factor& factor_for(nsf_device* h, int slot, bool needValues);
 void batch_upload_plan(nsf_device* h);
 void batch_launch_step(nsf_device* h);
 void batch_autotune(nsf_device* h, int rounds);

@@ -1,0 +1,188 @@
+// Dense layers of the learned preconditioner on the tensor cores: Y = epilogue(X W^T) with X gathered row by row
+// from up to three FP32 sources (edge features plus the two end nodes' features, say), rounded to BF16 in shared
+// memory, W in BF16, FP32 accumulation in tensor memory.
+//
+// One CTA of 128 threads owns a 128-row tile at a time (persistent over tiles).  The threads stage the tile in the
+// canonical no-swizzle K-major layout, one thread issues K / 16 tcgen05.mma (M = 128, N <= 128, K = 16) into TMEM
+// and commits them to an mbarrier, then each warp reads its 32 TMEM lanes (= 32 rows) back with tcgen05.ld for the
+// fused epilogue (bias, ReLU, ReLU-mask for the backward pass, residual).  Every wait is bounded; on a time-out the
+// kernel raises the error word, waits (bounded) for its MMAs, frees TMEM and leaves.
+#include <algorithm>
+#include <vector>
+
+#include "nsf_internal.cuh"
+#include "nsf_tc.cuh"
+#include "nsf_learn.h"
+
+namespace nsf {
+
+namespace {
+constexpr int kTcThreads = 128;
+constexpr int kTcM = 128;
+
+__device__ __forceinline__ float seg_value(const TcArgs& g, int row, int k) {
+    int s = 0;
+    while (s + 1 < g.nseg && k >= g.seg[s].width) {
+        k -= g.seg[s].width;
+        ++s;
+    }
+    const TcSeg& sg = g.seg[s];
+    const int src = sg.index ? sg.index[row] : row;
+    return src >= 0 ? sg.base[(size_t)src * sg.width + k] : 0.0f;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kTcThreads, 1) tc_dense_kernel(TcArgs g) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmemBase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int K = g.K, N = g.N;
+    __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(sm);
+    __nv_bfloat16* sB = reinterpret_cast<__nv_bfloat16*>(sm + (size_t)kTcM * K * 2);
+    const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : 128u);
+    if (warp == 0) tc::tmem_alloc(&tmemBase, ncols);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    for (int e = tid; e < N * K; e += kTcThreads) {
+        const int n = e / K, k = e - n * K;
+        sB[tc::core_offset(n, k, K)] = g.B[e];
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmemBase;
+    const uint32_t idesc = tc::idesc_bf16(kTcM, N);
+    const uint32_t aBase = tc::smem_u32(sA), bBase = tc::smem_u32(sB);
+    const uint32_t sbo = (uint32_t)K * 16u;   // 8-row groups of a K-wide tile
+    const int tiles = (g.rows + kTcM - 1) / kTcM;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int r0 = tile * kTcM;
+        for (int e = tid; e < kTcM * K; e += kTcThreads) {
+            const int r = e / K, k = e - r * K;
+            const float v = r0 + r < g.rows ? seg_value(g, r0 + r, k) : 0.0f;
+            sA[tc::core_offset(r, k, K)] = __float2bfloat16_rn(v);
+        }
+        tc::fence_proxy_async();   // generic-proxy stores -> visible to the tensor core (async proxy)
+        tc::fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after();
+            for (int s = 0; s < K / 16; ++s)
+                tc::mma_bf16(tmem, tc::smem_desc(aBase + s * 256u, 128u, sbo), tc::smem_desc(bBase + s * 256u, 128u, sbo),
+                             idesc, s > 0);
+            tc::mma_commit(&mbar);
+        }
+        if (!tc::mbar_wait(&mbar, phase, g.timeoutNs)) ok = false;
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        phase ^= 1u;
+        tc::fence_after();
+        const int row = r0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            float v[32];
+            tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (row < g.rows) {
+                float* y = g.Y + (size_t)row * N + c0;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    float a = v[j];
+                    if (g.bias) a += g.bias[c0 + j];
+                    switch (g.epi) {
+                        case TC_EPI_RELU:
+                            if (g.Ypre) g.Ypre[(size_t)row * N + c0 + j] = a;
+                            a = fmaxf(a, 0.0f);
+                            break;
+                        case TC_EPI_RELU_MASK:   // backward through a ReLU: keep where the pre-activation was > 0
+                            a = g.aux[(size_t)row * N + c0 + j] > 0.0f ? a : 0.0f;
+                            break;
+                        default:
+                            break;
+                    }
+                    if (g.resid) a += g.resid[(size_t)row * N + c0 + j];
+                    y[j] = a;
+                }
+            }
+        }
+        tc::fence_before();
+        __syncthreads();   // TMEM and the A tile are reused by the next tile
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(g.error, 1);
+        tc::mbar_wait(&mbar, phase, g.timeoutNs);   // the MMAs in flight, if any (bounded again)
+        __syncthreads();
+    }
+    tc::fence_after();
+    if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
+// Y[rows x N] = epilogue(X W^T) with X the concatenated segments (K columns) and W given as N x K BF16 rows.
+void tc_dense(const TcArgs& a, cudaStream_t s, int sms) {
+    if (a.K % 16 || a.K <= 0 || a.K > 128 || a.N % 16 || a.N <= 0 || a.N > 128) throw bad_arg("dense layer shape");
+    if (a.rows <= 0) return;
+    int w = 0;
+    for (int i = 0; i < a.nseg; ++i) w += a.seg[i].width;
+    if (w != a.K) throw bad_arg("segment widths must add up to K");
+    const size_t smem = (size_t)kTcM * a.K * 2 + (size_t)a.N * a.K * 2;
+    static bool attr = false;
+    if (!attr) {
+        NSF_CUDA(cudaFuncSetAttribute(tc_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        attr = true;
+    }
+    const int tiles = (a.rows + kTcM - 1) / kTcM;
+    tc_dense_kernel<<<std::min(tiles, std::max(sms, 1)), kTcThreads, smem, s>>>(a);
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+}  // namespace nsf
+
+// ---------------------------------------------------------------------------------------------------
+// C entry point: one dense layer on host arrays (the tensor-core path's known-answer check)
+// ---------------------------------------------------------------------------------------------------
+extern "C" int nsf_tc_dense(nsf_device* h, int rows, int K, int N, const float* X, const float* W,
+                            const float* bias, int epilogue, float* Y) {
+    if (!h || !X || !W || !Y || rows <= 0) return NSF_ERR_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    try {
+        NSF_CUDA(cudaSetDevice(h->device));
+        if (epilogue != nsf::TC_EPI_NONE && epilogue != nsf::TC_EPI_RELU) throw nsf::bad_arg("epilogue: 0 or 1");
+        std::vector<__nv_bfloat16> B((size_t)N * K);
+        for (int k = 0; k < K; ++k)
+            for (int o = 0; o < N; ++o) B[(size_t)o * K + k] = __float2bfloat16_rn(W[(size_t)k * N + o]);
+        nsf::DevBuf<float> x, y, b;
+        nsf::DevBuf<__nv_bfloat16> w;
+        nsf::DevBuf<int> err;
+        x.upload(X, (size_t)rows * K, h->stream);
+        w.upload(B.data(), B.size(), h->stream);
+        if (bias) b.upload(bias, (size_t)N, h->stream);
+        y.alloc((size_t)rows * N);
+        err.alloc(1);
+        err.zero(h->stream);
+        nsf::TcArgs a{};
+        a.seg[0] = {x.get(), nullptr, K};
+        a.nseg = 1;
+        a.rows = rows;
+        a.K = K;
+        a.B = w.get();
+        a.N = N;
+        a.bias = bias ? b.get() : nullptr;
+        a.epi = epilogue;
+        a.Y = y.get();
+        a.error = err.get();
+        a.timeoutNs = h->timeoutNs;
+        nsf::tc_dense(a, h->stream, h->smCount);
+        int e = 0;
+        NSF_CUDA(cudaMemcpyAsync(Y, y.get(), sizeof(float) * rows * N, cudaMemcpyDeviceToHost, h->stream));
+        NSF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        if (e) throw nsf::Error{NSF_ERR_BARRIER_TIMEOUT, "tensor-core layer timed out"};
+        return NSF_OK;
+    } catch (const nsf::Error& e) {
+        h->lastError = e.msg;
+        return e.status;
+    }
+}

@@ -229,6 +229,12 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.maxIt = maxIt < 0 ? A.rows : maxIt;
     if (precond) {
         a.f = factor_view(h->factors[slot], ws);
+        a.f.natB = b;          // the solve itself runs on the permuted copies
+        a.f.natX0 = x0;
+        a.f.natX = x;
+        a.b = ws.bp.get();
+        a.x0 = ws.xp.get();
+        a.x = ws.xp.get();
         // over the cap (the plain method's count) the solve falls back to plain FP64 CG with the caller's own
         // budget; when the caller's budget is the tighter limit there is no fallback
         const int cap = h->pcgCap[slot] > 0 ? h->pcgCap[slot] : A.rows;

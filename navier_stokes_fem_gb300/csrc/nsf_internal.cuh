@@ -119,6 +119,9 @@ struct FactorView {
     float* w32 = nullptr;
     double* xp = nullptr;                     // the iterate and right-hand side in permuted order
     double* bp = nullptr;
+    const double* natB = nullptr;             // the caller's right-hand side, initial guess and solution
+    const double* natX0 = nullptr;
+    double* natX = nullptr;
 };
 
 // The factor of one matrix.  The preconditioned solve runs on the colour-permuted system P A P^T, whose colour

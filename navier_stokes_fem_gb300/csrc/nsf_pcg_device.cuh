@@ -80,7 +80,7 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
         const bool last = c == C - 1;
-        sell_rows<TV, TA, false, 1, 4>(F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
+        sell_rows<TV, TA, false, sizeof(TA) == 4 ? 2 : 1, 4>(F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
                                  [&](int i) { return SweepRow<TA>{r[i], dinv[i], TA(0)}; },
                                  [&](int i, TA acc, const SweepRow<TA>& q) {
                                      TA y = (q.src - acc) * q.d;
@@ -95,7 +95,7 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
     for (int c = C - 2; c >= 0; --c) {
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
-        sell_rows<TV, TA, false, 1, 4>(F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
+        sell_rows<TV, TA, false, sizeof(TA) == 4 ? 2 : 1, 4>(F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
                                  [&](int i) { return SweepRow<TA>{w[i], dinv[i], r[i]}; },
                                  [&](int i, TA acc, const SweepRow<TA>& q) {
                                      const TA z = (q.src - acc) * q.d;
@@ -111,29 +111,24 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
     return true;
 }
 
-// The preconditioned solve runs on the colour-permuted system.  In: (the fused right-hand side is built in the
-// caller's order, then) b and x0 are gathered into permuted order; out: x is scattered back.  Returns the args of
-// the permuted solve (n = padded size, b = x0 = x = the permuted vectors), or false on a barrier timeout.
-static __device__ bool permute_in(Team& t, const CgArgs& a, double* stage, CgArgs& p, int& where) {
+// The preconditioned solve runs on the colour-permuted system: a.n is the padded size and a.b, a.x0 and a.x are
+// the permuted vectors (F.bp, F.xp); the caller's vectors are F.natB / F.natX0 / F.natX.  In: (the fused
+// right-hand side is built in the caller's order, then) b and x0 are gathered into permuted order; out: x is
+// scattered back.  Returns false on a barrier timeout.
+static __device__ bool permute_in(Team& t, const CgArgs& a, double* stage, int& where) {
     const FactorView& F = a.f;
     int rb, re;
     team_rows(F.nNatural, t, rb, re);
     build_rhs(a, rb, re, stage);
     if (a.bRowptr && !t.barrier(where++)) return false;
-    const double* b = a.bRowptr ? a.bOut : a.b;
+    const double* b = a.bRowptr ? a.bOut : F.natB;
     team_rows(a.n, t, rb, re);
     for (int i = rb + (int)threadIdx.x; i < re; i += blockDim.x) {
         const int o = F.perm[i];
         F.bp[i] = o >= 0 ? b[o] : 0.0;
-        F.xp[i] = o >= 0 ? a.x0[o] : 0.0;
+        F.xp[i] = o >= 0 ? F.natX0[o] : 0.0;
     }
-    if (!t.barrier(where++)) return false;
-    p = a;
-    p.bRowptr = nullptr;
-    p.b = F.bp;
-    p.x0 = F.xp;
-    p.x = F.xp;
-    return true;
+    return t.barrier(where++);
 }
 
 static __device__ void permute_out(Team& t, const CgArgs& a) {
@@ -142,7 +137,7 @@ static __device__ void permute_out(Team& t, const CgArgs& a) {
     team_rows(a.n, t, rb, re);
     for (int i = rb + (int)threadIdx.x; i < re; i += blockDim.x) {
         const int o = F.perm[i];
-        if (o >= 0) a.x[o] = F.xp[i];
+        if (o >= 0) F.natX[o] = F.xp[i];
     }
 }
 
@@ -154,11 +149,10 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
     const int G = t.size, bs = blockDim.x;
     int rb, re;
     team_rows(a.n, t, rb, re);
-    const double* b = a.bRowptr ? a.bOut : a.b;
+    const double* b = a.b;   // permuted right-hand side (permute_in)
     double* w = F.w;
     int where = 200;
 
-    build_rhs(a, rb, re, stage);
     double rrp = 0, bbp = 0;
     DotAcc<double> rz0;
     warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.x0[c]; },
@@ -298,12 +292,8 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
     const int G = t.size, bs = blockDim.x;
     int rb, re;
     team_rows(a.n, t, rb, re);
-    const double* b = a.bRowptr ? a.bOut : a.b;
+    const double* b = a.b;   // permuted right-hand side (permute_in); x0 == x
     float* w = F.w32;
-
-    build_rhs(a, rb, re, stage);
-    if (a.x != a.x0)
-        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] = a.x0[i];
 
     int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 300, stalls = 0;
     double rr64 = 0, bb = 0, target = 0, rz = 0, beta = 0.0, rrBest = INFINITY;
@@ -460,25 +450,28 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
 }
 
 // Preconditioned solves of the caller's system: permute in, solve the colour-permuted system, permute out.
-template <typename Body>
-__device__ int team_pcg(Team& t, const CgArgs& a, double* stage, double* smem, Body body) {
+// (The solve works on the kernel's own argument block: the permuted vectors are passed in it, so no copy of the
+// arguments lands in local memory.)
+static __device__ int team_pcg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
     int where = 190;
-    CgArgs p;
-    if (!permute_in(t, a, stage, p, where)) {
+    if (!permute_in(t, a, stage, where)) {
         write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
         return NSF_ERR_BARRIER_TIMEOUT;
     }
-    const int st = body(t, p, stage, smem);
+    const int st = pcg_fp64_body(t, a, stage, smem);
     if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
     return st;
 }
 
-static __device__ int team_pcg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
-    return team_pcg(t, a, stage, smem, pcg_fp64_body);
-}
-
 static __device__ int team_pcg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
-    return team_pcg(t, a, stage, smem, pcg_mixed_body);
+    int where = 190;
+    if (!permute_in(t, a, stage, where)) {
+        write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
+        return NSF_ERR_BARRIER_TIMEOUT;
+    }
+    const int st = pcg_mixed_body(t, a, stage, smem);
+    if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
+    return st;
 }
 
 }  // namespace nsf

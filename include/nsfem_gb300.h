@@ -153,8 +153,9 @@ int nsf_learn_forward(nsf_learner* L, int index, float* lower, float* diag);
 int nsf_learn_loss_grad(nsf_learner* L, int index, double* loss, float* grad);
 /* `steps` Adam steps, each on the mean gradient of `batch` systems drawn from the store; losses[steps] or NULL. */
 int nsf_learn_train(nsf_learner* L, int steps, int batch, double lr, uint64_t seed, float* losses);
-/* Runs the network on the slot's matrix and installs its factor as the slot's preconditioner. */
-int nsf_learn_apply(nsf_learner* L, int slot);
+/* Runs the network on the slot's matrix of `target` (NULL: the learner's own handle; same GPU) and installs its
+ * factor as that slot's preconditioner. */
+int nsf_learn_apply(nsf_learner* L, nsf_device* target, int slot);
 /* One tensor-core dense layer on host arrays: Y[rows x N] = epilogue(X[rows x K] W[K x N] + bias), X and W
  * rounded to BF16, FP32 accumulation; epilogue 0 none, 1 ReLU; K and N multiples of 16 up to 128. */
 int nsf_tc_dense(nsf_device* h, int rows, int K, int N, const float* X, const float* W, const float* bias,

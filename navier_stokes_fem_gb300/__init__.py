@@ -111,7 +111,7 @@ _SIGS = {
     "nsf_learn_forward": (_i, [_v, _i, _arr(np.float32), _arr(np.float32)]),
     "nsf_learn_loss_grad": (_i, [_v, _i, _P(_d), _arr(np.float32)]),
     "nsf_learn_train": (_i, [_v, _i, _i, _d, ctypes.c_uint64, _v]),
-    "nsf_learn_apply": (_i, [_v, _i]),
+    "nsf_learn_apply": (_i, [_v, _v, _i]),
     "nsf_timer": (_i, [_v, _i, _P(_f)]),
     "nsf_host_alloc": (_i, [_v, _sz, _P(_v)]),
     "nsf_host_free": (_i, [_v, _v]),
@@ -517,9 +517,10 @@ class Learner:
                                               losses.ctypes.data_as(_v)))
         return losses[:steps]
 
-    def apply(self, slot):
-        """Installs the network's factor for the slot's current matrix (preconditioner kind "learned")."""
-        self._check(library().nsf_learn_apply(self._h, _slot(slot)))
+    def apply(self, slot, device: "GPUSimulationDevice" = None):
+        """Installs the network's factor for the slot's current matrix (preconditioner kind "learned") on `device`
+        (default: the learner's own device handle; it must be on the same GPU)."""
+        self._check(library().nsf_learn_apply(self._h, device._h if device is not None else None, _slot(slot)))
 
 
 def tc_dense(device, X, W, bias=None, relu=False):

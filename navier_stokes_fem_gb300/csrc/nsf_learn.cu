@@ -981,12 +981,16 @@ int nsf_learn_train(nsf_learner* L, int steps, int batch, double lr, uint64_t se
     LEARN_END(L)
 }
 
-// Runs the network on the slot's current matrix and installs L as the slot's preconditioner (kind LEARNED).
-int nsf_learn_apply(nsf_learner* L, int slot) {
+// Runs the network on the slot's current matrix (of `target`, or of the learner's own handle when null) and
+// installs L as that slot's preconditioner (kind LEARNED).  Both handles must live on the same GPU.
+int nsf_learn_apply(nsf_learner* L, nsf_device* target, int slot) {
     LEARN_BEGIN(L)
-    std::unique_ptr<LSystem> S = build_system(L->h, slot, nullptr, nullptr);
+    nsf_device* T = target ? target : L->h;
+    if (T->device != L->h->device) throw bad_arg("the target handle is on another GPU");
+    std::lock_guard<std::recursive_mutex> lkT(T->mu);
+    std::unique_ptr<LSystem> S = build_system(T, slot, nullptr, nullptr);   // synchronises T's stream
     Learner(L).forward(*S);
-    Factor& F = factor_for(L->h, slot, false);
+    Factor& F = factor_for(T, slot, false);
     factor_from_net_kernel<<<grid_for((int64_t)S->m + S->n, 256), 256, 0, L->h->stream>>>(
         S->n, S->m, S->c.get(), S->sqrtD.get(), L->tape.lower.get(), L->tape.diag.get(), F.lVal.get(), F.diag.get());
     NSF_CUDA(cudaGetLastError());
@@ -996,7 +1000,7 @@ int nsf_learn_apply(nsf_learner* L, int slot) {
     NSF_CUDA(cudaStreamSynchronize(L->h->stream));
     F.kind = NSF_PRECOND_LEARNED;
     F.shift = 0.0;
-    L->h->pcgOff[slot] = false;
+    T->pcgOff[slot] = false;
     LEARN_END(L)
 }
 

@@ -296,7 +296,7 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
     float* w = F.w32;
 
     int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 300, stalls = 0;
-    double rr64 = 0, bb = 0, target = 0, rz = 0, beta = 0.0, rrBest = INFINITY;
+    double rr64 = 0, bb = 0, target = 0, rz = 0, beta = 0.0, rrBest = INFINITY, rrCycle = INFINITY;
     float* pprev = a.p32a;
     float* pcur = a.p32b;
     bool first = true, resetP = true, timedOut = false;
@@ -344,11 +344,15 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
             break;
         }
         if (!(rzT > 0.0) || isinf(rzT)) { status = NSF_ERR_BREAKDOWN; break; }
-        // every refresh restarts the preconditioned recurrence (p = z): on the ill-conditioned pressure systems an
-        // FP32 preconditioned recurrence carried across refreshes converged up to 2x slower than restarted cycles
-        beta = 0.0;
-        resetP = true;
+        // Continue the recurrence from the refreshed residual (beta' = r.z / r_prev.z_prev), unless the cycle just
+        // ended has drifted: its FP32 recursive residual fell by innerTol^2 but the true one by less than a quarter.
+        // Then restart it (p = z).  Carried recurrences converged fastest on the large pressure systems once the flow
+        // had settled, but in the first steps of a cavity they drifted and took up to 5x the iterations.
+        const bool drifted = refresh > 0 && rr64 > 0.25 * rrCycle;
+        beta = (resetP || drifted) ? 0.0 : rzT / rz;
+        resetP = false;
         rz = rzT;
+        rrCycle = rr64;
         const double rrRef = rr64;
         const int itRef = it;
         ++refresh;

@@ -72,12 +72,13 @@ __global__ void ap_values_kernel(int64_t nnz, const int* __restrict__ from, cons
 // already use the most distinct colours (ties: more neighbours, then the lower row index) with the smallest colour
 // none of them uses.  On the triangulated grids of this solver it finds 3 colours where first-fit in row order
 // needs 4, and every colour is one sweep phase.  Deterministic; the oracle restates it with the same tie rule.
-int dsatur_colour(int n, const std::vector<int>& rp, const std::vector<int>& ci, std::vector<unsigned char>& colour) {
+int dsatur_colour(int n, const std::vector<int>& rp, const std::vector<int>& ci, const std::vector<double>& av,
+                  std::vector<unsigned char>& colour) {
     colour.assign((size_t)n, 255);
     std::vector<unsigned> used((size_t)n, 0);      // colours among coloured neighbours (bit mask)
     std::vector<int> deg((size_t)n, 0);
     for (int i = 0; i < n; ++i)
-        for (int k = rp[i]; k < rp[i + 1]; ++k) deg[i] += ci[k] != i;
+        for (int k = rp[i]; k < rp[i + 1]; ++k) deg[i] += ci[k] != i && av[k] != 0.0;
     // max-heap of (saturation, degree, -row) with lazy deletion
     using Key = std::tuple<int, int, int>;
     std::priority_queue<Key> heap;
@@ -95,7 +96,7 @@ int dsatur_colour(int n, const std::vector<int>& rp, const std::vector<int>& ci,
         colours = std::max(colours, c + 1);
         for (int k = rp[i]; k < rp[i + 1]; ++k) {
             const int j = ci[k];
-            if (j == i || colour[j] != 255 || (used[j] >> c & 1u)) continue;
+            if (j == i || av[k] == 0.0 || colour[j] != 255 || (used[j] >> c & 1u)) continue;
             used[j] |= 1u << c;
             heap.push(Key{__builtin_popcount(used[j]), deg[j], -j});
         }
@@ -110,13 +111,18 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
     if (!A.valid() || A.rows != A.cols) throw bad_arg("preconditioner needs a square matrix");
     const int n = A.rows;
     std::vector<int> rp((size_t)n + 1), ci((size_t)A.nnz);
+    std::vector<double> av((size_t)A.nnz);
     NSF_CUDA(cudaMemcpyAsync(rp.data(), A.rowptr.get(), sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s));
-    if (A.nnz) NSF_CUDA(cudaMemcpyAsync(ci.data(), A.col.get(), sizeof(int) * ci.size(), cudaMemcpyDeviceToHost, s));
+    if (A.nnz) {
+        NSF_CUDA(cudaMemcpyAsync(ci.data(), A.col.get(), sizeof(int) * ci.size(), cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaMemcpyAsync(av.data(), A.val.get(), sizeof(double) * av.size(), cudaMemcpyDeviceToHost, s));
+    }
     NSF_CUDA(cudaStreamSynchronize(s));
 
-    // colouring (DSatur, see dsatur_colour)
+    // colouring of the graph of the non-zero entries (DSatur, see dsatur_colour); exact zeros of the assembled
+    // pattern couple nothing, so neighbours through them may share a colour and carry no factor entry
     std::vector<unsigned char> colour;
-    const int colours = dsatur_colour(n, rp, ci, colour);
+    const int colours = dsatur_colour(n, rp, ci, av, colour);
 
     // canonical strictly-lower pattern: neighbours of a smaller colour, ordered by (colour, column)
     std::vector<int> lrp((size_t)n + 1, 0), lci, aIdx, aDiag((size_t)n, -1);
@@ -128,7 +134,7 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
         for (int k = rp[i]; k < rp[i + 1]; ++k) {
             const int j = ci[k];
             if (j == i) aDiag[i] = k;
-            else if (colour[j] < colour[i]) row.push_back({j, k});
+            else if (av[k] != 0.0 && colour[j] < colour[i]) row.push_back({j, k});
         }
         if (aDiag[i] < 0) throw Error{NSF_ERR_BAD_ARG, "row " + std::to_string(i) + " has no diagonal entry"};
         std::sort(row.begin(), row.end(), [&](const std::pair<int, int>& a, const std::pair<int, int>& b) {

@@ -111,13 +111,23 @@ void make_fp32_values(Csr& A, cudaStream_t s) {
 // ---------------------------------------------------------------------------------------------------
 // SELL-32 copy of a CSR matrix (the layout the CG kernels stream; see sell_spmv in nsf_device.cuh)
 // ---------------------------------------------------------------------------------------------------
-__global__ void sell_width_kernel(int rows, int nSlices, const int* __restrict__ rowptr,
-                                  long long* __restrict__ width) {
+// Entries kept in the SELL copies: every non-zero and the diagonal.  Exact zeros of the assembled pattern (the
+// diagonal couplings of right-angled P1 triangles, eliminated Dirichlet couplings: about a quarter of a structured
+// pressure matrix) contribute +0 to every row sum, so leaving them out changes no product for finite vectors.
+__device__ __forceinline__ bool sell_keep(const double* val, const int* col, int k, int row) {
+    return val[k] != 0.0 || col[k] == row;
+}
+
+__global__ void sell_width_kernel(int rows, int nSlices, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                  const double* __restrict__ val, long long* __restrict__ width) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nSlices; s += gridDim.x * blockDim.x) {
         int w = 0;
         for (int l = 0; l < 32; ++l) {
             const int r = s * 32 + l;
-            if (r < rows) w = max(w, rowptr[r + 1] - rowptr[r]);
+            if (r >= rows) continue;
+            int c = 0;
+            for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) c += sell_keep(val, col, k, r);
+            w = max(w, c);
         }
         width[s] = (long long)w * 32;
     }
@@ -127,24 +137,27 @@ __global__ void narrow_kernel(int n, const long long* __restrict__ in, int* __re
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (int)in[i];
 }
 
-// One thread per (slice, lane): the row's entries in CSR order, then padding (value 0, the row's own column).
+// One thread per (slice, lane): the row's kept entries in CSR order (kept by their FP64 value), then padding
+// (value 0, the row's own column).
 template <typename T>
 __global__ void sell_fill_kernel(int rows, int nSlices, const int* __restrict__ rowptr, const int* __restrict__ col,
-                                 const T* __restrict__ val, const int* __restrict__ start, int* __restrict__ scol,
-                                 T* __restrict__ sval) {
+                                 const double* __restrict__ keepVal, const T* __restrict__ val,
+                                 const int* __restrict__ start, int* __restrict__ scol, T* __restrict__ sval) {
     const long long total = (long long)nSlices * 32;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
         const int r = (int)i, s = r / 32, lane = r % 32;
         const int base = start[s], W = (start[s + 1] - base) / 32;
-        const int b = r < rows ? rowptr[r] : 0;
-        const int len = r < rows ? rowptr[r + 1] - b : 0;
+        const int e = r < rows ? rowptr[r + 1] : 0;
+        int q = r < rows ? rowptr[r] : 0;
         const int self = r < rows ? r : 0;
         for (int k = 0; k < W; ++k) {
+            while (q < e && !sell_keep(keepVal, col, q, r)) ++q;
             const int idx = base + k * 32 + lane;
-            const bool in = k < len;
-            if (scol) scol[idx] = in ? col[b + k] : self;
-            sval[idx] = in ? val[b + k] : T(0);
+            const bool in = q < e;
+            if (scol) scol[idx] = in ? col[q] : self;
+            sval[idx] = in ? val[q] : T(0);
+            if (in) ++q;
         }
     }
 }
@@ -156,7 +169,8 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
         DevBuf<long long> width, start64;
         width.alloc((size_t)A.nSlices);
         start64.alloc((size_t)A.nSlices + 1);
-        sell_width_kernel<<<grid_for(A.nSlices, 256), 256, 0, s>>>(A.rows, A.nSlices, A.rowptr.get(), width.get());
+        sell_width_kernel<<<grid_for(A.nSlices, 256), 256, 0, s>>>(A.rows, A.nSlices, A.rowptr.get(), A.col.get(),
+                                                                  A.val.get(), width.get());
         NSF_CUDA(cudaGetLastError());
         count_launch();
         NSF_CUDA(cudaMemsetAsync(start64.get(), 0, sizeof(long long), s));
@@ -169,6 +183,7 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
         NSF_CUDA(cudaMemcpyAsync(&total, start64.get() + A.nSlices, sizeof(long long), cudaMemcpyDeviceToHost, s));
         NSF_CUDA(cudaStreamSynchronize(s));
         if (total > INT32_MAX) throw Error{NSF_ERR_BAD_ARG, "padded matrix exceeds 2^31-1 entries"};
+        // (total may be below nnz: exact zeros are left out)
         A.sellStart.alloc((size_t)A.nSlices + 1);
         narrow_kernel<<<grid_for(A.nSlices + 1, 256), 256, 0, s>>>(A.nSlices + 1, start64.get(), A.sellStart.get());
         NSF_CUDA(cudaGetLastError());
@@ -176,8 +191,8 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
         A.sellCol.alloc((size_t)std::max(total, 1LL));
         A.sellVal.alloc((size_t)std::max(total, 1LL));
         sell_fill_kernel<double><<<grid_for((int64_t)A.nSlices * 32, 256), 256, 0, s>>>(
-            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.sellStart.get(), A.sellCol.get(),
-            A.sellVal.get());
+            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val.get(), A.sellStart.get(),
+            A.sellCol.get(), A.sellVal.get());
         NSF_CUDA(cudaGetLastError());
         count_launch();
         NSF_CUDA(cudaStreamSynchronize(s));   // width / start64 / tmp are released on return
@@ -186,7 +201,7 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
     if (fp32 && !A.hasSell32) {
         A.sellVal32.alloc(A.sellVal.n);
         sell_fill_kernel<float><<<grid_for((int64_t)A.nSlices * 32, 256), 256, 0, s>>>(
-            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val32.get(), A.sellStart.get(), nullptr,
+            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.sellStart.get(), nullptr,
             A.sellVal32.get());
         NSF_CUDA(cudaGetLastError());
         count_launch();

@@ -84,9 +84,9 @@ def lib():
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
         _u8ptr = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
         L.orc_mc_colour.restype = _i
-        L.orc_mc_colour.argtypes = [_i, _lptr, _iptr, _u8ptr]
+        L.orc_mc_colour.argtypes = [_i, _lptr, _iptr, _dptr, _u8ptr]
         L.orc_mc_lower.restype = ctypes.c_int64
-        L.orc_mc_lower.argtypes = [_i, _lptr, _iptr, _u8ptr, _p, _p, _p, _p]
+        L.orc_mc_lower.argtypes = [_i, _lptr, _iptr, _dptr, _u8ptr, _p, _p, _p, _p]
         L.orc_ic0.restype = _i
         L.orc_ic0.argtypes = [_i, _i, _u8ptr, _lptr, _iptr, _lptr, _lptr, _dptr, _d, _dptr, _dptr]
         L.orc_pcg.restype = _i
@@ -382,13 +382,13 @@ class McFactor:
         self.av = np.ascontiguousarray(A.data, np.float64)
         L = lib()
         self.colour = np.zeros(self.n, np.uint8)
-        self.colours = L.orc_mc_colour(self.n, self.rp, self.ci, self.colour)
-        nnz = L.orc_mc_lower(self.n, self.rp, self.ci, self.colour, None, None, None, None)
+        self.colours = L.orc_mc_colour(self.n, self.rp, self.ci, self.av, self.colour)
+        nnz = L.orc_mc_lower(self.n, self.rp, self.ci, self.av, self.colour, None, None, None, None)
         self.lrp = np.zeros(self.n + 1, np.int64)
         self.lci = np.zeros(max(nnz, 1), np.int32)
         self.aidx = np.zeros(max(nnz, 1), np.int64)
         self.adiag = np.full(self.n, -1, np.int64)
-        L.orc_mc_lower(self.n, self.rp, self.ci, self.colour, self.lrp.ctypes.data, self.lci.ctypes.data,
+        L.orc_mc_lower(self.n, self.rp, self.ci, self.av, self.colour, self.lrp.ctypes.data, self.lci.ctypes.data,
                        self.aidx.ctypes.data, self.adiag.ctypes.data)
         self.nnz_lower = int(nnz)
         self.lval = np.zeros(max(nnz, 1))

@@ -19,14 +19,14 @@
 
 extern "C" {
 
-// DSatur colouring (Brelaz 1979), as the GPU path colours: repeatedly colour the uncoloured row whose coloured
-// neighbours use the most distinct colours (ties: more neighbours, then the lower row index) with the smallest
-// colour none of them uses.  Returns the number of colours (or -1 above 32).
-int orc_mc_colour(int n, const int64_t* rp, const int* ci, unsigned char* colour) {
+// DSatur colouring (Brelaz 1979) of the graph of the non-zero entries, as the GPU path colours: repeatedly colour
+// the uncoloured row whose coloured neighbours use the most distinct colours (ties: more neighbours, then the lower
+// row index) with the smallest colour none of them uses.  Returns the number of colours (or -1 above 32).
+int orc_mc_colour(int n, const int64_t* rp, const int* ci, const double* av, unsigned char* colour) {
     std::vector<int> c((size_t)n, -1), deg((size_t)n, 0);
     std::vector<unsigned> used((size_t)n, 0);
     for (int i = 0; i < n; ++i)
-        for (int64_t k = rp[i]; k < rp[i + 1]; ++k) deg[i] += ci[k] != i;
+        for (int64_t k = rp[i]; k < rp[i + 1]; ++k) deg[i] += ci[k] != i && av[k] != 0.0;
     std::priority_queue<std::tuple<int, int, int>> heap;
     for (int i = 0; i < n; ++i) heap.push(std::make_tuple(0, deg[i], -i));
     int colours = 0;
@@ -45,7 +45,7 @@ int orc_mc_colour(int n, const int64_t* rp, const int* ci, unsigned char* colour
         colours = std::max(colours, k + 1);
         for (int64_t e = rp[i]; e < rp[i + 1]; ++e) {
             const int j = ci[e];
-            if (j == i || c[j] >= 0 || (used[j] >> k & 1u)) continue;
+            if (j == i || av[e] == 0.0 || c[j] >= 0 || (used[j] >> k & 1u)) continue;
             used[j] |= 1u << k;
             int sj = 0;
             for (unsigned m = used[j]; m; m &= m - 1) ++sj;
@@ -55,10 +55,10 @@ int orc_mc_colour(int n, const int64_t* rp, const int* ci, unsigned char* colour
     return colours;
 }
 
-// Strictly lower pattern: row i's neighbours j with colour(j) < colour(i), ordered by (colour(j), j).  With
+// Strictly lower pattern: row i's non-zero neighbours j with colour(j) < colour(i), ordered by (colour(j), j).  With
 // lrp == nullptr only the count is returned.  aIdx/aDiag: positions in the matrix's value array.
-int64_t orc_mc_lower(int n, const int64_t* rp, const int* ci, const unsigned char* colour, int64_t* lrp, int* lci,
-                     int64_t* aIdx, int64_t* aDiag) {
+int64_t orc_mc_lower(int n, const int64_t* rp, const int* ci, const double* av, const unsigned char* colour,
+                     int64_t* lrp, int* lci, int64_t* aIdx, int64_t* aDiag) {
     int64_t count = 0;
     std::vector<std::pair<int, int64_t>> row;
     if (lrp) lrp[0] = 0;
@@ -68,7 +68,7 @@ int64_t orc_mc_lower(int n, const int64_t* rp, const int* ci, const unsigned cha
             const int j = ci[k];
             if (j == i) {
                 if (aDiag) aDiag[i] = k;
-            } else if (colour[j] < colour[i]) {
+            } else if (av[k] != 0.0 && colour[j] < colour[i]) {
                 row.push_back({j, k});
             }
         }

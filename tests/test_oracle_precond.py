@@ -17,10 +17,10 @@ def _system(n=24, name="pressure_stiffness"):
 def test_colouring_is_proper_and_pattern_is_lower():
     A = _system()
     F = oracle.McFactor(A)
-    rows, cols = A.nonzero()
+    rows, cols = A.nonzero()                                           # (the non-zero entries only)
     off = rows != cols
-    assert (F.colour[rows[off]] != F.colour[cols[off]]).all()          # neighbours never share a colour
-    assert F.colours <= 4                                              # P1 triangulated grid: small palette
+    assert (F.colour[rows[off]] != F.colour[cols[off]]).all()          # coupled rows never share a colour
+    assert F.colours <= 3                                              # P1 triangulated grid: small palette
     for i in range(A.shape[0]):
         js = F.lci[F.lrp[i]:F.lrp[i + 1]]
         assert (F.colour[js] < F.colour[i]).all()

@@ -2,7 +2,11 @@
 """Benchmark of the per-time-step hot path: ms per operator-split time step and CG iterations per solve at a
 1e-8 relative residual, on one GB300 (N GPUs run N independent replicas; the path does not shard).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--solver fp64|mixed] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--solver S] [--precond P] [--impl reference]
+
+The default line is the metric's method on the 2048 x 2048 cavity: mixed-precision PCG with the learned
+preconditioner (trained on the GPU during set-up, untimed), with the plain FP64 CG megakernel timed on the same
+workload in the same run ("plain_fp64_cg").
 
 A step is one pass of the hot path over the resident fields: advection, two diffusion solves, the pressure solve,
 the gradient product and two mass solves (NavierStokesAssembly::semiLagrangianSolve's loop body,
@@ -41,7 +45,7 @@ WORKLOADS = {
     # the batched form: 64 cavities, n ~ U{16..256}, nu log-U[1e-3,1e-1], lid U[0.5,2], dt = 0.25 h / lid
     "batched64": dict(kind="batched", count=64, seed=20261203, n_lo=16, n_hi=256, nu=None, dt=None),
 }
-DEFAULT_WORKLOAD = "channel1024x256"
+DEFAULT_WORKLOAD = "cavity2048"
 L2_BYTES = 129 << 20
 
 
@@ -297,18 +301,21 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def run_gpu(args):
-    world, rank, local, pg = dist_setup()
-    import navier_stokes_fem_gb300 as nsf
+def pcg_bytes(mixed, n, nz, nzl, its, outer):
+    """Minimal DRAM bytes of one preconditioned solve (int32 indices): per iteration the product with the
+    non-zeros of A and both triangular sweeps over the factor's nzl strictly lower entries (values + indices),
+    plus about 15 vector passes (product gathers and outputs, the x/r update, the sweeps' right-hand sides,
+    inverse diagonals and in-place results).  The mixed form moves FP32 values and vectors and adds an FP64
+    residual per refresh."""
+    v = 4 if mixed else 8
+    it_bytes = (v + 4) * (nz + 2 * nzl) + 4 * (n + 1) + 15 * v * n
+    refresh = 12 * nz + 4 * (n + 1) + 28 * n
+    return (outer + 1) * refresh + its * it_bytes
 
-    w = WORKLOADS[args.workload]
-    mesh = make_mesh(w)
-    t0 = time.perf_counter()
-    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
-                                   inner_tolerance=args.inner_tol)
-    if args.precond == "ic0":
-        sim.precond_ic0("pressure_stiffness")
-    setup_s = time.perf_counter() - t0
+
+def time_arm(sim, args, pg):
+    """Warm-up steps, then args.steps timed steps (CUDA events on the library's stream, L2 flushed in between)
+    with every persistent solve recorded; returns the measurements."""
     for _ in range(args.warmup):
         sim.flush_l2(256 << 20)
         sim.step(1)
@@ -331,20 +338,77 @@ def run_gpu(args):
     clk = clocks.stop()
     prof = sim.profile_read()
     sim.profile(False)
-    ms = max_over_ranks(pg, ms_total / args.steps)
+    return {"ms": max_over_ranks(pg, ms_total / args.steps), "its": np.asarray(its), "prof": prof,
+            "launches": launches, "clocks": clk}
 
-    # roofline of the dominant kernel: the persistent CG solver, over every launch in the timed region
-    bytes_total = 0.0
-    for m_, n_, z_, i_, o_ in zip(prof["mode"], prof["rows"], prof["nnz"], prof["iterations"], prof["outer"]):
-        bytes_total += algorithmic_bytes(1 if int(m_) in (1, 2) else 0, int(n_), int(z_), int(i_), int(o_))
-    mixed = (prof["mode"] == 1) | (prof["mode"] == 2)
-    mixed_stats = {"mixed_solves": int(mixed.sum()),
-                   "finished_in_fp64": int((prof["fallback"] == 1).sum()),
-                   "mean_fp64_refreshes": round(float(prof["outer"][mixed].mean()), 2) if mixed.any() else 0}
-    cg_ms = float(np.sum(prof["ms"]))
+
+def nonzeros(sim, slot):
+    rp, col, val, shape = sim.download_matrix(slot)
+    return int(np.count_nonzero(val))
+
+
+def roofline(sim, arm, args):
+    """Algorithmic bytes over every persistent solve of the timed steps / their summed kernel time."""
+    prof = arm["prof"]
+    nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
+    nzl = {}
+    for slot in (0, 1, 2):
+        if sim.precond_kind(slot) != "none":
+            nzl[slot] = int(sim.precond_pattern(slot)[1].size)
+    names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel", 2: "pcg_mixed_kernel", 3: "pcg_fp64_kernel"}
+    bytes_by, ms_by = {}, {}
+    for sl, m_, n_, i_, o_, t_ in zip(prof["slot"], prof["mode"], prof["rows"], prof["iterations"], prof["outer"],
+                                      prof["ms"]):
+        m_, sl = int(m_), int(sl)
+        if m_ in (2, 3):
+            b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_))
+        else:
+            b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_))
+        bytes_by[names[m_]] = bytes_by.get(names[m_], 0.0) + b
+        ms_by[names[m_]] = ms_by.get(names[m_], 0.0) + float(t_)
+    top = max(ms_by, key=ms_by.get)
     peak, peak_kind = peaks()
-    achieved = bytes_total / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else 0.0
-    n_launch = len(prof["ms"])
+    achieved = bytes_by[top] / (ms_by[top] * 1e-3) / 1e9 if ms_by[top] > 0 else 0.0
+    launches = int(sum(1 for m_ in prof["mode"] if names[int(m_)] == top))
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs", "kernel": top,
+            "launches": launches, "kernel_ms_per_step": round(ms_by[top] / args.steps, 3),
+            "kernel_share_of_solver_time": round(ms_by[top] / max(sum(ms_by.values()), 1e-9), 3),
+            "algorithmic_bytes_per_launch": round(bytes_by[top] / max(launches, 1)), "traffic": None}
+
+
+def run_gpu(args):
+    world, rank, local, pg = dist_setup()
+    import navier_stokes_fem_gb300 as nsf
+
+    w = WORKLOADS[args.workload]
+    mesh = make_mesh(w)
+    t0 = time.perf_counter()
+    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
+                                   inner_tolerance=args.inner_tol)
+    setup_s = time.perf_counter() - t0
+    learned = None
+    t0 = time.perf_counter()
+    if args.precond == "ic0":
+        sim.precond_ic0("pressure_stiffness")
+    elif args.precond == "learned":
+        from navier_stokes_fem_gb300 import learn
+
+        trainer = nsf.GPUSimulationDevice(local)
+        learner, learned = learn.train(trainer, seed=args.seed, steps=args.train_steps)
+        t1 = time.perf_counter()
+        learner.apply("pressure_stiffness", sim)
+        learned["apply_s"] = round(time.perf_counter() - t1, 3)
+        learner.close()
+        trainer.close()
+    precond_s = time.perf_counter() - t0
+    arm = time_arm(sim, args, pg)
+    ms, its, clk, launches = arm["ms"], arm["its"], arm["clocks"], arm["launches"]
+    roof = roofline(sim, arm, args)
+    prof = arm["prof"]
+    mixed = (prof["mode"] == 1) | (prof["mode"] == 2)
+    mixed_stats = {"mixed_solves": int(mixed.sum()), "finished_in_fp64": int((prof["fallback"] == 1).sum()),
+                   "mean_fp64_refreshes": round(float(prof["outer"][mixed].mean()), 2) if mixed.any() else 0}
 
     # end to end through the C ABI: host fields copied in and out around every step (pinned buffers)
     uv, p = sim.fields()
@@ -361,30 +425,39 @@ def run_gpu(args):
         p_in, p_out = p_out, p_in
     e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / e2e_steps)
     field_bytes = int(uv.nbytes + p.nbytes)
+    sim.close()
+
+    # the plain FP64 CG megakernel on the same workload and steps, in the same process (the comparison the metric
+    # names); its own warm-up steps are not timed
+    plain = None
+    if args.compare and not (args.solver == "fp64" and args.precond == "none"):
+        ref = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver="fp64")
+        parm = time_arm(ref, args, pg)
+        ref.close()
+        plain = {"ms_per_step": round(parm["ms"], 3), "cg_iterations_per_step": parm["its"].mean(axis=0).round(1).tolist(),
+                 "speedup": round(parm["ms"] / ms, 3), "clocks": parm["clocks"]}
 
     base = None
-    sim.close()
     if rank == 0 and not args.no_cpu_baseline:
-        base = cpu_baseline(mesh, w, args.cpu_steps, iterations_per_step=np.asarray(its).mean(axis=0))
+        base = cpu_baseline(mesh, w, args.cpu_steps, iterations_per_step=(plain["cg_iterations_per_step"] if plain
+                                                                           else its.mean(axis=0)))
     if rank != 0:
         return
-    its = np.asarray(its)
+    solver = args.solver + ("" if args.precond == "none" else f" + {args.precond} preconditioner")
     line = {
         "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.solver == "fp64" else "f32+f64",
+        "vs_baseline": None, "dtype": "f64" if args.solver in ("fp64", "pcg_fp64") else "f32+f64",
         "data": "synthetic (seeded structured mesh; inputs resident in HBM, L2 flushed between steps)",
-        "config": config_block(args, w, mesh, args.solver),
+        "config": config_block(args, w, mesh, solver),
         "cg_iterations_per_step": its.mean(axis=0).round(1).tolist(),
         "cg_solves": ["diffusion u", "diffusion v", "pressure", "mass u", "mass v"],
-        "mixed_precision": mixed_stats if args.solver == "mixed" else None,
+        "plain_fp64_cg": plain,
+        "mixed_precision": mixed_stats if args.solver in ("mixed", "pcg_mixed") else None,
+        "learned_preconditioner": learned,
         "setup_s": round(setup_s, 3),
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-                     "kernel": "cg_fp64_kernel" if args.solver == "fp64" else "cg_mixed_kernel",
-                     "launches": n_launch, "kernel_ms_per_step": round(cg_ms / args.steps, 3),
-                     "algorithmic_bytes_per_launch": round(bytes_total / max(n_launch, 1)),
-                     "traffic": None},
+        "preconditioner_setup_s": round(precond_s, 3),
+        "roofline": roof,
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": field_bytes,
                 "d2h_bytes_per_step": field_bytes, "steps": e2e_steps},
         "gpu_launches": int(launches),
@@ -518,6 +591,12 @@ def run_cg_probe(args):
     sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], solver=args.solver, inner_tolerance=args.inner_tol)
     if args.precond == "ic0":
         sim.precond_ic0("pressure_stiffness")
+    elif args.precond == "learned":
+        from navier_stokes_fem_gb300 import learn
+
+        trainer = nsf.GPUSimulationDevice(0)
+        learner, _ = learn.train(trainer, seed=args.seed, steps=args.train_steps)
+        learner.apply("pressure_stiffness", sim)
     b = np.random.default_rng(0).standard_normal(mesh.n_pressure)
     for _ in range(2):
         x, it, rr, st = sim.conjugate_gradient("pressure_stiffness", b, np.zeros_like(b), max_iterations=args.cg_probe,
@@ -529,12 +608,17 @@ def run_cg_probe(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--solver", default="fp64", choices=["fp64", "mixed", "pcg_mixed", "pcg_fp64"])
-    ap.add_argument("--precond", default="none", choices=["none", "ic0"])
+    ap.add_argument("--solver", default=None, choices=["fp64", "mixed", "pcg_mixed", "pcg_fp64"],
+                    help="default: pcg_mixed with the learned preconditioner (the metric's method)")
+    ap.add_argument("--precond", default=None, choices=["none", "ic0", "learned"])
+    ap.add_argument("--train-steps", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="skip the plain FP64 CG run on the same workload")
     ap.add_argument("--inner-tol", type=float, default=-1.0)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -542,6 +626,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.solver is None:
+        if WORKLOADS[args.workload]["kind"] == "batched":
+            args.solver = "mixed"        # (the batched step kernel runs the unpreconditioned solvers)
+        else:
+            args.solver = "pcg_mixed" if args.precond in (None, "learned") else "fp64"
+    if args.precond is None:
+        args.precond = "learned" if args.solver in ("pcg_mixed", "pcg_fp64") else "none"
     if args.cg_probe:
         run_cg_probe(args)
     elif args.impl == "reference":

@@ -112,9 +112,11 @@ int nsf_conjugate_gradient_dev(nsf_device* h, int slot, const double* b_dev, con
                                int maxIterations, double eps, int mode, int* iterations, double* relResidual);
 
 /* ---- preconditioners (IC0Preconditioner under USE_PRECONDITIONING, include/assembly.h:33-35, 1338-1344) -----
- * M = L L^T in multicolour order: the slot's matrix graph is coloured greedily in row order, and L_ij (i != j)
- * lives on the matrix pattern where colour(j) < colour(i).  A preconditioned solve (NSF_SOLVER_PCG_*) that has not
- * converged after the slot's cap of iterations finishes with plain FP64 CG from its current iterate. */
+ * M = L L^T in multicolour order: the graph of the slot's non-zero entries is coloured by DSatur (most distinct
+ * neighbour colours first; ties: more neighbours, then the lower row), and L_ij (i != j) lives on the non-zeros
+ * where colour(j) < colour(i).  The solve runs on the colour-permuted matrix.  A preconditioned solve
+ * (NSF_SOLVER_PCG_*) that has not converged after the slot's cap of iterations finishes with plain FP64 CG from
+ * its current iterate, within the caller's own iteration budget. */
 /* Builds the pattern; colours and the number of strictly lower entries may be NULL. */
 int nsf_precond_pattern(nsf_device* h, int slot, int* colours, int64_t* nnzLower);
 /* The pattern: rowptr[rows + 1] and col[nnzLower] of the strictly lower part, entries of a row ordered by

@@ -253,7 +253,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
         e1 = pool_event(h);
         NSF_CUDA(cudaEventRecord(e0, h->stream));
     }
-    cg_launch(ws, a, mode, h->stream);
+    cg_launch(ws, a, mode, S.maxWidth > kSellChunk, h->stream);
     if (h->profile) {
         NSF_CUDA(cudaEventRecord(e1, h->stream));
         h->records.push_back({slot, mode, A.rows, A.nnz, e0, e1, infoIndex});
@@ -326,10 +326,14 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     // diffusion solves, u then v (include/assembly.h:1529-1545, 489-558): rhs = M u_adv - lift, g on Dirichlet rows
     for (int ch = 0; ch < 2; ++ch) {
         CgArgs f{};
-        const Csr& M = h->mats[NSF_VELOCITY_MASS];
+        Csr& M = h->mats[NSF_VELOCITY_MASS];
+        prepare_matrix(M, false, s);
         f.bRowptr = M.rowptr.get();
         f.bCol = M.col.get();
         f.bVal = M.val.get();
+        f.bSellStart = M.sellStart.get();
+        f.bSellCol = M.sellCol.get();
+        f.bSellVal = M.sellVal.get();
         f.bX = tmp + (size_t)ch * Nv;
         f.lift = S.liftV[ch].get();
         f.bcMask = S.bcV.get();
@@ -341,10 +345,14 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     // pressure projection (include/assembly.h:560-712): rhs_p = -(1/dt) Div u - lift, pinned nodes -> g
     {
         CgArgs f{};
-        const Csr& Bd = h->mats[NSF_VELOCITY_DIVERGENCE];
+        Csr& Bd = h->mats[NSF_VELOCITY_DIVERGENCE];
+        prepare_matrix(Bd, false, s);
         f.bRowptr = Bd.rowptr.get();
         f.bCol = Bd.col.get();
         f.bVal = Bd.val.get();
+        f.bSellStart = Bd.sellStart.get();
+        f.bSellCol = Bd.sellCol.get();
+        f.bSellVal = Bd.sellVal.get();
         f.bX = uv;
         f.lift = S.liftP.get();
         f.bcMask = S.bcP.get();
@@ -667,6 +675,7 @@ int nsf_sim_setup(nsf_device* h, int nNodes, const float* xy, int nElements, con
     ensure_workspace(h, std::max(nNodes, nPressure));
     for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS})
         prepare_matrix(h->mats[slot], h->solverMode == NSF_SOLVER_MIXED, h->stream);
+    prepare_matrix(h->mats[NSF_VELOCITY_DIVERGENCE], false, h->stream);   // the pressure right-hand side's product
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     h->sim.ready = true;
     NSF_END(h)

@@ -30,28 +30,34 @@ namespace nsf {
 // ---------------------------------------------------------------------------------------------------
 // single-solve kernels: the team is the whole cooperative grid
 // ---------------------------------------------------------------------------------------------------
+// Wide = true: the pipelined product for matrices with slices wider than kSellChunk entries per row (P2 systems);
+// each kernel is instantiated for both so that the narrow systems keep their own register allocation.
+template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) cg_fp64_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_cg_fp64(t, a, stage, smem);
+    team_cg_fp64<Wide>(t, a, stage, smem);
 }
 
+template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_cg_mixed(t, a, stage, smem);
+    team_cg_mixed<Wide>(t, a, stage, smem);
 }
 
+template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) pcg_fp64_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_fp64(t, a, stage, smem);
+    team_pcg_fp64<Wide>(t, a, stage, smem);
 }
 
+template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed(t, a, stage, smem);
+    team_pcg_mixed<Wide>(t, a, stage, smem);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -60,8 +66,10 @@ __global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_kernel(CgArgs a) {
 // Co-resident CTAs per SM of every persistent solver kernel (the grid must fit all of them).
 static int cg_occupancy() {
     int occ = 1 << 30;
-    for (const void* fn : {(const void*)cg_fp64_kernel, (const void*)cg_mixed_kernel, (const void*)pcg_fp64_kernel,
-                           (const void*)pcg_mixed_kernel}) {
+    for (const void* fn : {(const void*)cg_fp64_kernel<false>, (const void*)cg_mixed_kernel<false>,
+                           (const void*)pcg_fp64_kernel<false>, (const void*)pcg_mixed_kernel<false>,
+                           (const void*)cg_fp64_kernel<true>, (const void*)cg_mixed_kernel<true>,
+                           (const void*)pcg_fp64_kernel<true>, (const void*)pcg_mixed_kernel<true>}) {
         int o = 0;
         NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kCgThreads, 0));
         occ = std::min(occ, o);
@@ -83,14 +91,21 @@ void cg_configure(CgWorkspace& ws, int device) {
     ws.info.alloc(4096);
 }
 
-void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, cudaStream_t s) {
+void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStream_t s) {
     NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
     CgArgs a = args;
     void* params[] = {&a};
-    const void* fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel
-                     : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel
-                     : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel
-                                                    : (const void*)cg_fp64_kernel;
+    const void* fn;
+    if (wide)
+        fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel<true>
+             : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel<true>
+             : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel<true>
+                                            : (const void*)cg_fp64_kernel<true>;
+    else
+        fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel<false>
+             : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel<false>
+             : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel<false>
+                                            : (const void*)cg_fp64_kernel<false>;
     NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
     count_launch();
 }
@@ -112,7 +127,7 @@ void cg_launch_fp64_raw(const CgArgs& args, int grid, int block, cudaStream_t s)
     NSF_CUDA(cudaMemsetAsync(args.sync, 0, sizeof(GridSync), s));
     CgArgs a = args;
     void* params[] = {&a};
-    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)cg_fp64_kernel, dim3(grid), dim3(block), params, 0, s));
+    NSF_CUDA(cudaLaunchCooperativeKernel((const void*)cg_fp64_kernel<false>, dim3(grid), dim3(block), params, 0, s));
     count_launch();
 }
 

@@ -214,7 +214,7 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
 // vectors stay in L2.
 // ---------------------------------------------------------------------------------------------------
 constexpr int kSlice = 32;
-constexpr int kUnroll = 8;
+constexpr int kUnroll = kSellChunk;
 
 // Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W).
 template <int U, typename TV>
@@ -329,21 +329,139 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
     }
 }
 
+// Wide matrices (slices wider than U entries per row: the P2 mass, diffusion and divergence matrices).  Each of a
+// warp's NS streams is a software pipeline over chunks of U entries per lane: the next chunk's matrix loads (the
+// rest of this slice, or the next slice's first chunk) are issued together with this chunk's gathers, so a chunk
+// costs one memory latency and a slice of width W costs ceil(W / U) of them (sell_rows spends two per chunk after
+// the first).  Same contract as sell_rows; pre(row) is evaluated when the slice's predecessor finishes.
+template <int U, typename TV>
+__device__ __forceinline__ void sell_chunk_at(const int* __restrict__ col, const TV* __restrict__ val, int off,
+                                              int rem, int (&c)[U], TV (&v)[U]) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const bool in = u < rem;
+        c[u] = in ? ld_stream(col + off + u * kSlice) : -1;
+        v[u] = in ? ld_stream(val + off + u * kSlice) : TV(0);
+    }
+}
+
+template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename Gather, typename Pre,
+          typename Epi>
+__device__ __forceinline__ void sell_rows_wide(const int* __restrict__ sliceStart, const int* __restrict__ col,
+                                               const TV* __restrict__ val, int rb, int re, Gather gather, Pre pre,
+                                               Epi epi) {
+    using PreT = decltype(pre(0));
+    if (rb >= re) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int s1 = (re + kSlice - 1) / kSlice;
+    const int sFirst = rb / kSlice + warp;
+    if (sFirst >= s1) return;
+    const int count = (s1 - sFirst + nw - 1) / nw;
+    const int per = (count + NS - 1) / NS;
+    // per stream: k = slice ordinal, kEnd = its end, off / rem = offset and entries left of the chunk in flight
+    int mb[NS], me[NS], k[NS], kEnd[NS], off[NS], rem[NS], c[NS][U];
+    TV v[NS][U];
+    TA acc[NS];
+    PreT pv[NS];
+    auto meta_load = [&](int q, int i0) {   // lane j: start / end of stream q's slice i0 + j
+        const int i = i0 + lane;
+        const bool in = i < kEnd[q];
+        const int idx = sFirst + (q * per + i) * nw;
+        mb[q] = in ? sliceStart[idx] : 0;
+        me[q] = in ? sliceStart[idx + 1] : 0;
+    };
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        k[q] = 0;
+        kEnd[q] = max(0, min(per, count - q * per));
+        acc[q] = TA(0);
+        meta_load(q, 0);
+        off[q] = __shfl_sync(0xffffffffu, mb[q], 0);
+        rem[q] = (__shfl_sync(0xffffffffu, me[q], 0) - off[q]) / kSlice;
+        off[q] += lane;
+        sell_chunk_at<U, TV>(col, val, off[q], rem[q], c[q], v[q]);
+        const int row = (sFirst + q * per * nw) * kSlice + lane;
+        pv[q] = kEnd[q] > 0 && row < re ? pre(row) : PreT{};
+    }
+    while (true) {
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) any = any || k[q] < kEnd[q];
+        if (!any) break;
+        int remC[NS];
+        TA g[NS][U];
+        TV vk[NS][U];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            remC[q] = rem[q];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                g[q][u] = c[q][u] >= 0 ? gather(c[q][u]) : TA(0);
+                vk[q][u] = v[q][u];
+            }
+        }
+        // each stream's next chunk in flight with this step's gathers
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            if (k[q] >= kEnd[q]) continue;
+            if (rem[q] > U) {
+                off[q] += U * kSlice;
+                rem[q] -= U;
+            } else {
+                const int kn = k[q] + 1;
+                int o = 0, e = 0;
+                if (kn < kEnd[q]) {
+                    if ((kn & 31) == 0) meta_load(q, kn);
+                    o = __shfl_sync(0xffffffffu, mb[q], kn & 31);
+                    e = __shfl_sync(0xffffffffu, me[q], kn & 31);
+                }
+                off[q] = o + lane;
+                rem[q] = (e - o) / kSlice;
+            }
+            sell_chunk_at<U, TV>(col, val, off[q], rem[q], c[q], v[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            if (k[q] >= kEnd[q]) continue;
+            TA self = TA(0);
+            if constexpr (Diff) self = pv[q];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (u < remC[q]) {
+                    if (Diff) acc[q] = fma(TA(vk[q][u]), g[q][u] - self, acc[q]);
+                    else acc[q] = fma(TA(vk[q][u]), g[q][u], acc[q]);
+                }
+            }
+            if (remC[q] <= U) {   // the slice's last chunk: its rows are complete
+                const int row = (sFirst + (q * per + k[q]) * nw) * kSlice + lane;
+                if (row < re) epi(row, acc[q], pv[q]);
+                acc[q] = TA(0);
+                ++k[q];
+                if (k[q] < kEnd[q]) {
+                    const int rn = row + nw * kSlice;
+                    pv[q] = rn < re ? pre(rn) : PreT{};
+                }
+            }
+        }
+    }
+}
+
 // sum_j a_ij gather(j) (or its difference form) with epi(row, sum, gather(row)).
-template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
+template <typename TV, typename TA, bool Diff, int U = kUnroll, bool Wide = false, typename Gather, typename Epi>
 __device__ __forceinline__ void sell_spmv(const int* __restrict__ sliceStart, const int* __restrict__ col,
                                           const TV* __restrict__ val, int rb, int re, Gather gather, Epi epi) {
-    sell_rows<TV, TA, Diff>(sliceStart, col, val, rb, re, gather, gather, epi);
+    if constexpr (Wide) sell_rows_wide<TV, TA, Diff, 1, U>(sliceStart, col, val, rb, re, gather, gather, epi);
+    else sell_rows<TV, TA, Diff, 1, U>(sliceStart, col, val, rb, re, gather, gather, epi);
 }
 
 // q = A p over the CTA's rows with epi(row, sum, p_row): the SELL-32 copy when the matrix has one, else the
 // warp-chunked CSR product (caller-owned CSR arrays, e.g. the allocation-free entry point).
-template <typename TV, typename TA, bool Diff, typename Gather, typename Epi>
+template <typename TV, typename TA, bool Diff, int U = kUnroll, bool Wide = false, typename Gather, typename Epi>
 __device__ __forceinline__ void matrix_product(const int* sellStart, const int* sellCol, const TV* sellVal,
                                                const int* rowptr, const int* col, const TV* val, int rb, int re,
                                                TA* stage, Gather gather, Epi epi) {
     if (sellStart) {
-        sell_spmv<TV, TA, Diff>(sellStart, sellCol, sellVal, rb, re, gather, epi);
+        sell_spmv<TV, TA, Diff, U, Wide>(sellStart, sellCol, sellVal, rb, re, gather, epi);
     } else {
         warp_spmv<TV, TA, Diff>(rowptr, col, val, rb, re, stage, gather,
                                 [&](int row, TA acc) { epi(row, acc, gather(row)); });
@@ -363,21 +481,23 @@ static __device__ void write_info(const Team& t, const CgArgs& a, int it, int st
 
 // b for this block's rows: the given vector, or the fused right-hand side mask ? g : (B x_b) - lift, stored
 // to a.bOut by the owning lane (the same lane reads it back in the residual pass).
+template <bool Wide = false>
 static __device__ void build_rhs(const CgArgs& a, int rb, int re, double* stage) {
     if (!a.bRowptr) return;
-    warp_spmv<double, double>(a.bRowptr, a.bCol, a.bVal, rb, re, stage,
-                              [&](int c) { return a.bX[c]; },
-                              [&](int row, double acc) {
-                                  double bi = a.lift ? acc - a.lift[row] : acc;
-                                  if (a.bcMask && a.bcMask[row]) bi = a.bcValue[row];
-                                  a.bOut[row] = bi;
-                              });
+    matrix_product<double, double, false, 4, Wide>(a.bSellStart, a.bSellCol, a.bSellVal, a.bRowptr, a.bCol, a.bVal, rb, re,
+                                          stage, [&](int c) { return a.bX[c]; },
+                                          [&](int row, double acc, double) {
+                                              double bi = a.lift ? acc - a.lift[row] : acc;
+                                              if (a.bcMask && a.bcMask[row]) bi = a.bcValue[row];
+                                              a.bOut[row] = bi;
+                                          });
 }
 
 // ---------------------------------------------------------------------------------------------------
 // FP64 persistent CG
 // partial regions: 0 = p.q, 1 = r.r, 2 = r0.r0, 3 = b.b
 // ---------------------------------------------------------------------------------------------------
+template <bool Wide = false>
 static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
     const int G = t.size;
     int rb, re;
@@ -385,18 +505,19 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     const double* b = a.bRowptr ? a.bOut : a.b;
 
     // prologue: (b), x = x0, r0 = b - A x0, p0 = r0
-    build_rhs(a, rb, re, stage);
+    build_rhs<Wide>(a, rb, re, stage);
     double rrp = 0, bbp = 0;
-    warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.x0[c]; },
-                              [&](int row, double acc) {
-                                  const double bi = b[row];
-                                  const double ri = bi - acc;
-                                  a.r[row] = ri;
-                                  a.pbuf0[row] = ri;
-                                  if (a.x != a.x0) a.x[row] = a.x0[row];
-                                  rrp = fma(ri, ri, rrp);
-                                  bbp = fma(bi, bi, bbp);
-                              });
+    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+                                          [&](int c) { return a.x0[c]; },
+                                          [&](int row, double acc, double x0i) {
+                                              const double bi = b[row];
+                                              const double ri = bi - acc;
+                                              a.r[row] = ri;
+                                              a.pbuf0[row] = ri;
+                                              if (a.x != a.x0) a.x[row] = x0i;
+                                              rrp = fma(ri, ri, rrp);
+                                              bbp = fma(bi, bi, bbp);
+                                          });
     rrp = block_sum(rrp, smem);
     bbp = block_sum(bbp, smem);
     if (threadIdx.x == 0) { a.partials[2 * G + t.rank] = rrp; a.partials[3 * G + t.rank] = bbp; }
@@ -413,7 +534,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     while (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
         // phase A: q = A p (streamed matrix), partial p.q
         double pq = 0;
-        matrix_product<double, double, false>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+        matrix_product<double, double, false, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
                                               [&](int c) { return p[c]; },
                                               [&](int row, double acc, double pr) {
                                                   a.q[row] = acc;
@@ -486,6 +607,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 // saves the third barrier of the FP64 kernel.
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
+template <bool Wide = false>
 static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
     float* stage32 = reinterpret_cast<float*>(stage);
     const int G = t.size;
@@ -494,7 +616,7 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
     const double* b = a.bRowptr ? a.bOut : a.b;
     const int bs = blockDim.x;
 
-    build_rhs(a, rb, re, stage);
+    build_rhs<Wide>(a, rb, re, stage);
     // x = x0 (own rows); the first true residual gathers x0, not x, so no barrier is needed here
     if (a.x != a.x0)
         for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] = a.x0[i];
@@ -511,8 +633,9 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
         double rrp = 0, bbp = 0, rip = 0;
         float* pp0 = pprev;
         const bool f0 = resetP;
-        warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xs[c]; },
-                                  [&](int row, double acc) {
+        matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
+                                              stage, [&](int c) { return xs[c]; },
+                                  [&](int row, double acc, double) {
                                       const double bi = b[row];
                                       const double ri = bi - acc;
                                       const float r32 = (float)ri;
@@ -568,7 +691,7 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
             // p.q accumulates in double-float so that the FP64 pipe does no per-row work
             float pqHi = 0.f, pqLo = 0.f;
-            matrix_product<float, float, true>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
+            matrix_product<float, float, true, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
                                                stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
                                                [&](int row, float acc, float pi) {
                                                    acc = fmaf(a.rowsum32[row], pi, acc);
@@ -627,7 +750,7 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
         f.b = b;
         f.x0 = a.x;
         f.maxIt = a.maxIt - it;
-        const int fst = team_cg_fp64(t, f, stage, smem);
+        const int fst = team_cg_fp64<Wide>(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
             a.info->iterations += it;

@@ -83,6 +83,7 @@ struct Csr {
     bool has32 = false;
     // SELL-32 copy for the CG kernels: slice s = rows [32s, 32s+32), entries column-major from sellStart[s]
     int nSlices = 0;
+    int maxWidth = 0;         // entries per row of the widest slice
     DevBuf<int> sellStart, sellCol;
     DevBuf<double> sellVal;
     DevBuf<float> sellVal32;
@@ -203,6 +204,9 @@ struct CgArgs {
     const int* bRowptr;
     const int* bCol;
     const double* bVal;
+    const int* bSellStart;   // Bm's SELL-32 copy (null: the CSR arrays above are streamed)
+    const int* bSellCol;
+    const double* bSellVal;
     const double* bX;
     const double* lift;
     const unsigned char* bcMask;
@@ -223,7 +227,9 @@ struct CgWorkspace {
 
 // launch helpers implemented in nsf_cg.cu / nsf_sparse.cu
 void cg_configure(CgWorkspace& ws, int device);
-void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, cudaStream_t s);
+// wide: the matrix has slices wider than kSellChunk entries per row (the kernels' pipelined product for them)
+constexpr int kSellChunk = 8;
+void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, bool wide, cudaStream_t s);
 void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
 void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
                      const double* bcValue, double* y, cudaStream_t s);

@@ -115,11 +115,12 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
 // the permuted vectors (F.bp, F.xp); the caller's vectors are F.natB / F.natX0 / F.natX.  In: (the fused
 // right-hand side is built in the caller's order, then) b and x0 are gathered into permuted order; out: x is
 // scattered back.  Returns false on a barrier timeout.
+template <bool Wide = false>
 static __device__ bool permute_in(Team& t, const CgArgs& a, double* stage, int& where) {
     const FactorView& F = a.f;
     int rb, re;
     team_rows(F.nNatural, t, rb, re);
-    build_rhs(a, rb, re, stage);
+    build_rhs<Wide>(a, rb, re, stage);
     if (a.bRowptr && !t.barrier(where++)) return false;
     const double* b = a.bRowptr ? a.bOut : F.natB;
     team_rows(a.n, t, rb, re);
@@ -144,6 +145,7 @@ static __device__ void permute_out(Team& t, const CgArgs& a) {
 // ---------------------------------------------------------------------------------------------------
 // FP64 PCG.  partial regions: 0 = p.q, 1 = r.r, 2 = r0.r0, 3 = b.b, 4 = r.z
 // ---------------------------------------------------------------------------------------------------
+template <bool Wide = false>
 static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, double* smem) {
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x;
@@ -155,12 +157,13 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
 
     double rrp = 0, bbp = 0;
     DotAcc<double> rz0;
-    warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.x0[c]; },
-                              [&](int row, double acc) {
+    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+                                          [&](int c) { return a.x0[c]; },
+                              [&](int row, double acc, double x0i) {
                                   const double bi = b[row];
                                   const double ri = bi - acc;
                                   a.r[row] = ri;
-                                  if (a.x != a.x0) a.x[row] = a.x0[row];
+                                  if (a.x != a.x0) a.x[row] = x0i;
                                   rrp = fma(ri, ri, rrp);
                                   bbp = fma(bi, bi, bbp);
                                   colour0_row<double>(F, w, F.dinv, row, ri, rz0);
@@ -205,7 +208,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
         if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
         // q = A p, p.q
         double pq = 0;
-        matrix_product<double, double, false>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+        matrix_product<double, double, false, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
                                               [&](int c) { return p[c]; },
                                               [&](int row, double acc, double pr) {
                                                   a.q[row] = acc;
@@ -268,7 +271,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
         f.b = b;
         f.x0 = a.x;
         f.maxIt = a.fallbackMaxIt;
-        const int fst = team_cg_fp64(t, f, stage, smem);
+        const int fst = team_cg_fp64<Wide>(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
             a.info->iterations += it;
@@ -287,6 +290,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
 // more iterations than the caller allows (the plain method's count), the solve finishes with plain FP64 CG.
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r.z
 // ---------------------------------------------------------------------------------------------------
+template <bool Wide = false>
 static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, double* smem) {
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x;
@@ -305,8 +309,9 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
         const double* xs = first ? a.x0 : a.x;
         double rrp = 0, bbp = 0;
         DotAcc<float> rzp;
-        warp_spmv<double, double>(a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xs[c]; },
-                                  [&](int row, double acc) {
+        matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
+                                              stage, [&](int c) { return xs[c]; },
+                                  [&](int row, double acc, double) {
                                       const double bi = b[row];
                                       const double ri = bi - acc;
                                       const float r32 = (float)ri;
@@ -364,7 +369,7 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
             const float* pp = pprev;
             float* pc = pcur;
             float pqHi = 0.f, pqLo = 0.f;
-            matrix_product<float, float, true>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
+            matrix_product<float, float, true, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
                                                reinterpret_cast<float*>(stage),
                                                [&](int c) { return fmaf(betaf, pp[c], w[c]); },
                                                [&](int row, float acc, float pi) {
@@ -440,7 +445,7 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
         f.b = b;
         f.x0 = a.x;
         f.maxIt = a.fallbackMaxIt > 0 ? a.fallbackMaxIt : a.maxIt - it;
-        const int fst = team_cg_fp64(t, f, stage, smem);
+        const int fst = team_cg_fp64<Wide>(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
             a.info->iterations += it;
@@ -456,24 +461,26 @@ static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, do
 // Preconditioned solves of the caller's system: permute in, solve the colour-permuted system, permute out.
 // (The solve works on the kernel's own argument block: the permuted vectors are passed in it, so no copy of the
 // arguments lands in local memory.)
+template <bool Wide = false>
 static __device__ int team_pcg_fp64(Team& t, const CgArgs& a, double* stage, double* smem) {
     int where = 190;
-    if (!permute_in(t, a, stage, where)) {
+    if (!permute_in<Wide>(t, a, stage, where)) {
         write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
         return NSF_ERR_BARRIER_TIMEOUT;
     }
-    const int st = pcg_fp64_body(t, a, stage, smem);
+    const int st = pcg_fp64_body<Wide>(t, a, stage, smem);
     if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
     return st;
 }
 
+template <bool Wide = false>
 static __device__ int team_pcg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
     int where = 190;
-    if (!permute_in(t, a, stage, where)) {
+    if (!permute_in<Wide>(t, a, stage, where)) {
         write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
         return NSF_ERR_BARRIER_TIMEOUT;
     }
-    const int st = pcg_mixed_body(t, a, stage, smem);
+    const int st = pcg_mixed_body<Wide>(t, a, stage, smem);
     if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
     return st;
 }

@@ -6,6 +6,7 @@
 // 575-595, 695-707) are fused into the product's epilogue.
 #include "nsf_internal.cuh"
 
+#include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
 namespace nsf {
@@ -138,9 +139,9 @@ __global__ void narrow_kernel(int n, const long long* __restrict__ in, int* __re
 }
 
 // One thread per (slice, lane): the row's kept entries in CSR order (kept by their FP64 value), then padding
-// (value 0, the row's own column).
+// (value 0, the row's own column, or column 0 for the rows of a tall matrix beyond its column count).
 template <typename T>
-__global__ void sell_fill_kernel(int rows, int nSlices, const int* __restrict__ rowptr, const int* __restrict__ col,
+__global__ void sell_fill_kernel(int rows, int cols, int nSlices, const int* __restrict__ rowptr, const int* __restrict__ col,
                                  const double* __restrict__ keepVal, const T* __restrict__ val,
                                  const int* __restrict__ start, int* __restrict__ scol, T* __restrict__ sval) {
     const long long total = (long long)nSlices * 32;
@@ -150,7 +151,7 @@ __global__ void sell_fill_kernel(int rows, int nSlices, const int* __restrict__ 
         const int base = start[s], W = (start[s + 1] - base) / 32;
         const int e = r < rows ? rowptr[r + 1] : 0;
         int q = r < rows ? rowptr[r] : 0;
-        const int self = r < rows ? r : 0;
+        const int self = r < rows && r < cols ? r : 0;
         for (int k = 0; k < W; ++k) {
             while (q < e && !sell_keep(keepVal, col, q, r)) ++q;
             const int idx = base + k * 32 + lane;
@@ -179,9 +180,18 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
         DevBuf<unsigned char> tmp;
         tmp.alloc(tmpBytes);
         NSF_CUDA(cub::DeviceScan::InclusiveSum(tmp.get(), tmpBytes, width.get(), start64.get() + 1, A.nSlices, s));
-        long long total = 0;
+        DevBuf<long long> widest;
+        widest.alloc(1);
+        size_t maxBytes = 0;
+        NSF_CUDA(cub::DeviceReduce::Max(nullptr, maxBytes, width.get(), widest.get(), A.nSlices, s));
+        DevBuf<unsigned char> maxTmp;
+        maxTmp.alloc(maxBytes);
+        NSF_CUDA(cub::DeviceReduce::Max(maxTmp.get(), maxBytes, width.get(), widest.get(), A.nSlices, s));
+        long long total = 0, wmax = 0;
         NSF_CUDA(cudaMemcpyAsync(&total, start64.get() + A.nSlices, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaMemcpyAsync(&wmax, widest.get(), sizeof(long long), cudaMemcpyDeviceToHost, s));
         NSF_CUDA(cudaStreamSynchronize(s));
+        A.maxWidth = (int)(wmax / 32);
         if (total > INT32_MAX) throw Error{NSF_ERR_BAD_ARG, "padded matrix exceeds 2^31-1 entries"};
         // (total may be below nnz: exact zeros are left out)
         A.sellStart.alloc((size_t)A.nSlices + 1);
@@ -191,7 +201,7 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
         A.sellCol.alloc((size_t)std::max(total, 1LL));
         A.sellVal.alloc((size_t)std::max(total, 1LL));
         sell_fill_kernel<double><<<grid_for((int64_t)A.nSlices * 32, 256), 256, 0, s>>>(
-            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val.get(), A.sellStart.get(),
+            A.rows, A.cols, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val.get(), A.sellStart.get(),
             A.sellCol.get(), A.sellVal.get());
         NSF_CUDA(cudaGetLastError());
         count_launch();
@@ -201,7 +211,7 @@ void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
     if (fp32 && !A.hasSell32) {
         A.sellVal32.alloc(A.sellVal.n);
         sell_fill_kernel<float><<<grid_for((int64_t)A.nSlices * 32, 256), 256, 0, s>>>(
-            A.rows, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.sellStart.get(), nullptr,
+            A.rows, A.cols, A.nSlices, A.rowptr.get(), A.col.get(), A.val.get(), A.val32.get(), A.sellStart.get(), nullptr,
             A.sellVal32.get());
         NSF_CUDA(cudaGetLastError());
         count_launch();

@@ -583,26 +583,33 @@ def run_batched(args):
 
 
 def run_cg_probe(args):
-    """Two pressure-matrix solves with a fixed iteration count (for kernel profiling of the CG megakernel)."""
+    """Two pressure-matrix solves with a fixed iteration count, on a handle that holds the pressure system alone
+    (the simulation that assembled it is freed first, so a profiler capture sees a few GB of device memory)."""
     import navier_stokes_fem_gb300 as nsf
 
     w = WORKLOADS[args.workload]
     mesh = make_mesh(w)
-    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], solver=args.solver, inner_tolerance=args.inner_tol)
+    sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"])
+    mat = sim.download_matrix("pressure_stiffness")
+    sim.close()
+    dev = nsf.GPUSimulationDevice(0)
+    dev.upload_matrix("pressure_stiffness", *mat)
     if args.precond == "ic0":
-        sim.precond_ic0("pressure_stiffness")
+        dev.precond_ic0("pressure_stiffness")
     elif args.precond == "learned":
         from navier_stokes_fem_gb300 import learn
 
         trainer = nsf.GPUSimulationDevice(0)
         learner, _ = learn.train(trainer, seed=args.seed, steps=args.train_steps)
-        learner.apply("pressure_stiffness", sim)
+        learner.apply("pressure_stiffness", dev)
+        learner.close()
+        trainer.close()
     b = np.random.default_rng(0).standard_normal(mesh.n_pressure)
     for _ in range(2):
-        x, it, rr, st = sim.conjugate_gradient("pressure_stiffness", b, np.zeros_like(b), max_iterations=args.cg_probe,
+        x, it, rr, st = dev.conjugate_gradient("pressure_stiffness", b, np.zeros_like(b), max_iterations=args.cg_probe,
                                                solver=args.solver, raise_on_error=False)
         print(json.dumps({"probe": "pressure CG", "rows": mesh.n_pressure, "iterations": it, "status": st}))
-    sim.close()
+    dev.close()
 
 
 def main():

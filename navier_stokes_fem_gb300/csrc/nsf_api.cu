@@ -253,7 +253,11 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
         e1 = pool_event(h);
         NSF_CUDA(cudaEventRecord(e0, h->stream));
     }
-    cg_launch(ws, a, mode, S.maxWidth > kSellChunk, h->stream);
+    const bool wide = S.maxWidth > kSellChunk;
+    if (mode == NSF_SOLVER_PCG_MIXED && !wide)
+        pcg_mixed_split_launch(ws, a, h->stream);
+    else
+        cg_launch(ws, a, mode, wide, h->stream);
     if (h->profile) {
         NSF_CUDA(cudaEventRecord(e1, h->stream));
         h->records.push_back({slot, mode, A.rows, A.nnz, e0, e1, infoIndex});

@@ -39,11 +39,18 @@ __global__ void __launch_bounds__(kCgThreads, 2) cg_fp64_kernel(CgArgs a) {
     team_cg_fp64<Wide>(t, a, stage, smem);
 }
 
+// The narrow mixed kernel streams its FP32 matrix through per-warp TMA rings (kRingBytes of dynamic shared memory).
 template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_kernel(CgArgs a) {
-    NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_cg_mixed<Wide>(t, a, stage, smem);
+    if constexpr (Wide) {
+        NSF_KERNEL_SHARED();
+        team_cg_mixed<Wide>(t, a, stage, smem);
+    } else {
+        NSF_RING_SHARED();
+        SellRing ring = ring_init(dsm, a.sync, a.timeoutNs);
+        team_cg_mixed<Wide>(t, a, stage, smem, &ring);
+    }
 }
 
 template <bool Wide>
@@ -53,28 +60,73 @@ __global__ void __launch_bounds__(kCgThreads, 2) pcg_fp64_kernel(CgArgs a) {
     team_pcg_fp64<Wide>(t, a, stage, smem);
 }
 
+// The mixed PCG kernels stream the FP32 factor (and the narrow matrix) through per-warp TMA rings.
 template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_kernel(CgArgs a) {
+    NSF_RING_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    SellRing ring = ring_init(dsm, a.sync, a.timeoutNs);
+    team_pcg_mixed<Wide>(t, a, stage, smem, &ring);
+}
+
+// The split mixed PCG for narrow matrices: the refresh launch (FP64 true residual, tests, sweeps; rare) keeps the
+// 2-CTA register budget and the TMA rings, the inner-iteration launch runs the FP32 loop alone at 4 CTAs per SM,
+// twice the warps to hide the latency of the gathers.
+__global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_refresh_kernel(CgArgs a) {
+    NSF_RING_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    SellRing ring = ring_init(dsm, a.sync, a.timeoutNs);
+    team_pcg_mixed_refresh(t, a, stage, smem, &ring);
+}
+
+__global__ void __launch_bounds__(kCgThreads, 4) pcg_mixed_inner_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed<Wide>(t, a, stage, smem);
+    team_pcg_mixed_inner(t, a, stage, smem, nullptr);
 }
 
 // ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
-// Co-resident CTAs per SM of every persistent solver kernel (the grid must fit all of them).
+// The persistent solver kernels with the dynamic shared memory each is launched with (the TMA rings).
+struct CgKernel {
+    const void* fn;
+    size_t dsm;
+};
+static const CgKernel kCgKernels[8] = {
+    {(const void*)cg_fp64_kernel<false>, 0},          {(const void*)cg_mixed_kernel<false>, kRingBytes},
+    {(const void*)pcg_fp64_kernel<false>, 0},         {(const void*)pcg_mixed_kernel<false>, kRingBytes},
+    {(const void*)cg_fp64_kernel<true>, 0},           {(const void*)cg_mixed_kernel<true>, 0},
+    {(const void*)pcg_fp64_kernel<true>, 0},          {(const void*)pcg_mixed_kernel<true>, kRingBytes}};
+
+static const CgKernel& cg_kernel(int mode, bool wide) {
+    const int m = mode == NSF_SOLVER_MIXED ? 1 : mode == NSF_SOLVER_PCG_FP64 ? 2 : mode == NSF_SOLVER_PCG_MIXED ? 3 : 0;
+    return kCgKernels[(wide ? 4 : 0) + m];
+}
+
+// Co-resident CTAs per SM of every persistent solver kernel (the grid must fit all of them); also raises the
+// dynamic shared-memory limit of the ring kernels.
 static int cg_occupancy() {
     int occ = 1 << 30;
-    for (const void* fn : {(const void*)cg_fp64_kernel<false>, (const void*)cg_mixed_kernel<false>,
-                           (const void*)pcg_fp64_kernel<false>, (const void*)pcg_mixed_kernel<false>,
-                           (const void*)cg_fp64_kernel<true>, (const void*)cg_mixed_kernel<true>,
-                           (const void*)pcg_fp64_kernel<true>, (const void*)pcg_mixed_kernel<true>}) {
+    for (const CgKernel& k : kCgKernels) {
+        if (k.dsm) NSF_CUDA(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.dsm));
         int o = 0;
-        NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kCgThreads, 0));
+        NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k.fn, kCgThreads, k.dsm));
         occ = std::min(occ, o);
     }
-    return occ;
+    NSF_CUDA(cudaFuncSetAttribute((const void*)pcg_mixed_refresh_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kRingBytes));
+    int o = 0;
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, (const void*)pcg_mixed_refresh_kernel, kCgThreads,
+                                                           kRingBytes));
+    return std::min(occ, o);
+}
+
+// CTAs per SM of the split PCG's inner-iteration kernel (at most 4)
+static int inner_occupancy() {
+    int o = 0;
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, (const void*)pcg_mixed_inner_kernel, kCgThreads, 0));
+    return std::min(4, o);
 }
 
 void cg_configure(CgWorkspace& ws, int device) {
@@ -86,28 +138,43 @@ void cg_configure(CgWorkspace& ws, int device) {
     if (perSm < 1) throw Error{NSF_ERR_CUDA, "CG kernel cannot be resident"};
     ws.grid = sms * perSm;
     ws.block = kCgThreads;
-    ws.partials.alloc((size_t)6 * ws.grid);
+    ws.gridInner = sms * std::max(perSm, inner_occupancy());
+    ws.partials.alloc((size_t)6 * std::max(ws.grid, ws.gridInner));
     ws.sync.alloc(1);
     ws.info.alloc(4096);
+    ws.loop.alloc(1);
 }
 
 void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStream_t s) {
     NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
     CgArgs a = args;
     void* params[] = {&a};
-    const void* fn;
-    if (wide)
-        fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel<true>
-             : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel<true>
-             : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel<true>
-                                            : (const void*)cg_fp64_kernel<true>;
-    else
-        fn = mode == NSF_SOLVER_MIXED       ? (const void*)cg_mixed_kernel<false>
-             : mode == NSF_SOLVER_PCG_MIXED ? (const void*)pcg_mixed_kernel<false>
-             : mode == NSF_SOLVER_PCG_FP64  ? (const void*)pcg_fp64_kernel<false>
-                                            : (const void*)cg_fp64_kernel<false>;
-    NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
+    const CgKernel& k = cg_kernel(mode, wide);
+    NSF_CUDA(cudaLaunchCooperativeKernel(k.fn, dim3(ws.grid), dim3(ws.block), params, k.dsm, s));
     count_launch();
+}
+
+void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
+    a.loop = ws.loop.get();
+    auto launch = [&](const void* fn, int grid, size_t dsm) {
+        NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
+        void* params[] = {&a};
+        NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(ws.block), params, dsm, s));
+        count_launch();
+    };
+    a.loopInit = 1;
+    launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
+    a.loopInit = 0;
+    // every refresh counts one outer cycle and the solve ends at maxOuter of them, so this loop is bounded
+    for (int cycle = 0; cycle <= a.maxOuter + 1; ++cycle) {
+        int state = 0;
+        NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        if (state != kLoopInner) return;
+        launch((const void*)pcg_mixed_inner_kernel, ws.gridInner, 0);
+        launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
+    }
+    throw Error{NSF_ERR_CUDA, "preconditioned solve did not finish within its refresh budget"};
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.

@@ -2,6 +2,7 @@
 // the persistent operator-split step kernel (nsf_step.cu).  See nsf_cg.cu for the design notes.
 #pragma once
 #include "nsf_internal.cuh"
+#include "nsf_tc.cuh"
 
 namespace nsf {
 
@@ -11,10 +12,15 @@ constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 constexpr int kRows = 4;      // rows per thread with their loads in flight in the vector phases
 
-// Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area.
+// Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area (the ring
+// kernels stage in their ring memory instead, NSF_RING_SHARED).
 #define NSF_KERNEL_SHARED()          \
     __shared__ double smem[33];      \
     __shared__ double stage[kWarps * 2 * kStage]
+#define NSF_RING_SHARED()                                     \
+    __shared__ double smem[33];                               \
+    extern __shared__ __align__(128) unsigned char dsm[];     \
+    double* stage = reinterpret_cast<double*>(dsm)
 
 
 // ---------------------------------------------------------------------------------------------------
@@ -216,6 +222,15 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
 constexpr int kSlice = 32;
 constexpr int kUnroll = kSellChunk;
 
+// pre() value of the difference-form products that also carries the row's FP32 row sum (loaded with the row's own
+// vector entry when the slice starts, not after its sum); row_self() is the entry Diff subtracts.
+template <typename TA> struct DiffPre {
+    TA self;
+    TA rs;
+};
+template <typename TA> __device__ __forceinline__ TA row_self(TA v) { return v; }
+template <typename TA> __device__ __forceinline__ TA row_self(const DiffPre<TA>& v) { return v.self; }
+
 // Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W).
 template <int U, typename TV>
 __device__ __forceinline__ void sell_chunk(const int* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
@@ -299,7 +314,7 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
         for (int q = 0; q < NS; ++q) {
             if (!live[q]) continue;
             TA self = TA(0);
-            if constexpr (Diff) self = pv[q];
+            if constexpr (Diff) self = row_self<TA>(pv[q]);
             TA acc = TA(0);
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -363,6 +378,8 @@ __device__ __forceinline__ void sell_rows_wide(const int* __restrict__ sliceStar
     TV v[NS][U];
     TA acc[NS];
     PreT pv[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) kEnd[q] = max(0, min(per, count - q * per));
     auto meta_load = [&](int q, int i0) {   // lane j: start / end of stream q's slice i0 + j
         const int i = i0 + lane;
         const bool in = i < kEnd[q];
@@ -373,7 +390,6 @@ __device__ __forceinline__ void sell_rows_wide(const int* __restrict__ sliceStar
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
         k[q] = 0;
-        kEnd[q] = max(0, min(per, count - q * per));
         acc[q] = TA(0);
         meta_load(q, 0);
         off[q] = __shfl_sync(0xffffffffu, mb[q], 0);
@@ -424,7 +440,7 @@ __device__ __forceinline__ void sell_rows_wide(const int* __restrict__ sliceStar
         for (int q = 0; q < NS; ++q) {
             if (k[q] >= kEnd[q]) continue;
             TA self = TA(0);
-            if constexpr (Diff) self = pv[q];
+            if constexpr (Diff) self = row_self<TA>(pv[q]);
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (u < remC[q]) {
@@ -446,6 +462,177 @@ __device__ __forceinline__ void sell_rows_wide(const int* __restrict__ sliceStar
     }
 }
 
+// ---------------------------------------------------------------------------------------------------
+// TMA-fed SELL-32 product for narrow FP32 matrices (every slice at most kRingWidth entries per row: the pressure
+// system and the preconditioner's factor).  Each warp owns a ring of kRingDepth shared-memory stages; lane 0 issues
+// one bulk asynchronous copy (cp.async.bulk with an evict-first L2 policy, completion counted on the stage's
+// mbarrier) per array and slice, kRingDepth slices ahead of the warp, so the matrix stream stays in flight without
+// holding registers and the gathered vectors keep L2.  A step takes kRingStep slices, whose gathers are in flight
+// together.  All copies a call issues are consumed in the same call.
+// ---------------------------------------------------------------------------------------------------
+constexpr int kRingDepth = 6;
+constexpr int kRingStep = 2;
+constexpr int kRingWidth = kSellChunk;
+constexpr int kRingStage = kRingWidth * kSlice;   // entries per array and stage
+constexpr size_t kRingDataPerWarp = (size_t)kRingDepth * kRingStage * 8;
+constexpr size_t kRingBytes = kRingDataPerWarp * kWarps + (size_t)kRingDepth * kWarps * sizeof(uint64_t);
+static_assert(kRingDataPerWarp * kWarps >= sizeof(double) * kWarps * 2 * kStage,
+              "the ring kernels use the ring memory as the CSR product's staging area");
+
+struct SellRing {
+    int* col;           // [kRingDepth][kRingStage] of this warp
+    float* val;
+    uint64_t* bar;      // [kRingDepth]
+    unsigned seq;       // slices this warp has taken through the ring: stage seq % D, phase parity (seq / D) & 1
+    uint64_t policy;    // L2 evict-first
+    GridSync* sync;     // its abort word is raised when a stage's wait times out
+    long long timeoutNs;
+};
+
+// Every thread calls this at kernel start; dsm is the launch's dynamic shared memory (kRingBytes, 128-byte aligned).
+__device__ __forceinline__ SellRing ring_init(unsigned char* dsm, GridSync* sync, long long timeoutNs) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* base = dsm + (size_t)warp * kRingDataPerWarp;
+    SellRing r;
+    r.col = reinterpret_cast<int*>(base);
+    r.val = reinterpret_cast<float*>(base + (size_t)kRingDepth * kRingStage * 4);
+    r.bar = reinterpret_cast<uint64_t*>(dsm + kRingDataPerWarp * kWarps) + warp * kRingDepth;
+    r.seq = 0;
+    r.policy = tc::policy_evict_first();
+    r.sync = sync;
+    r.timeoutNs = timeoutNs;
+    if (lane == 0)
+        for (int d = 0; d < kRingDepth; ++d) tc::mbar_init(&r.bar[d], 1);
+    __syncwarp();
+    return r;
+}
+
+// Rows [rb, re) of a narrow FP32 SELL-32 matrix through the warp's ring; the contract of sell_rows (padding
+// entries may carry column -1).  On a wait time-out the team's abort word is raised (its next barrier fails), the
+// copies still in flight are waited for (bounded) and the call returns.
+template <typename TA, bool Diff, typename Gather, typename Pre, typename Epi>
+__device__ __forceinline__ void sell_rows_ring(SellRing& ring, const int* __restrict__ sliceStart,
+                                               const int* __restrict__ col, const float* __restrict__ val, int rb,
+                                               int re, Gather gather, Pre pre, Epi epi) {
+    using PreT = decltype(pre(0));
+    constexpr int S = kRingStep;
+    static_assert(32 % S == 0 && kRingDepth >= 2 * S, "ring step");
+    if (rb >= re) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int s1 = (re + kSlice - 1) / kSlice;
+    const int sFirst = rb / kSlice + warp;
+    if (sFirst >= s1) return;
+    const int count = (s1 - sFirst + nw - 1) / nw;   // this warp's slices (slice i: sFirst + i nw)
+    // lane j holds the start / end of slice 32 b + j for the block b of the slices being consumed (mb0, me0) and
+    // for the next block (mb1, me1)
+    int mb0, me0, mb1, me1;
+    auto meta = [&](int blk, int& mb, int& me) {
+        const int i = blk * 32 + lane;
+        const bool in = i < count;
+        const int idx = sFirst + i * nw;
+        mb = in ? sliceStart[idx] : 0;
+        me = in ? sliceStart[idx + 1] : 0;
+    };
+    meta(0, mb0, me0);
+    meta(1, mb1, me1);
+    int cur = 0;
+    auto issue = [&](int i) {   // every lane calls (shuffles); lane 0 starts the copies of slice i
+        const bool same = (i >> 5) == cur;
+        const int o = __shfl_sync(0xffffffffu, same ? mb0 : mb1, i & 31);
+        const int e = __shfl_sync(0xffffffffu, same ? me0 : me1, i & 31);
+        if (lane == 0) {
+            const unsigned st = (ring.seq + (unsigned)i) % kRingDepth;
+            const uint32_t bytes = (uint32_t)(e - o) * 4u;   // W * 32 entries of 4 bytes per array
+            tc::fence_proxy_async();                        // the stage's earlier reads before the async writes
+            tc::mbar_expect_tx(&ring.bar[st], 2u * bytes);
+            if (bytes) {
+                tc::bulk_g2s_hint(ring.col + st * kRingStage, col + o, bytes, &ring.bar[st], ring.policy);
+                tc::bulk_g2s_hint(ring.val + st * kRingStage, val + o, bytes, &ring.bar[st], ring.policy);
+            }
+        }
+    };
+    int issued = min(kRingDepth, count);
+    for (int i = 0; i < issued; ++i) issue(i);
+    PreT pv[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+        const int row = (sFirst + q * nw) * kSlice + lane;
+        pv[q] = q < count && row < re ? pre(row) : PreT{};
+    }
+    int i = 0;
+    bool ok = true;
+    for (; i < count; i += S) {
+        int W[S], c[S][kRingWidth];
+        float v[S][kRingWidth];
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+            const int k = (i + q) & 31;
+            W[q] = i + q < count ? (__shfl_sync(0xffffffffu, me0, k) - __shfl_sync(0xffffffffu, mb0, k)) / kSlice : 0;
+            bool got = true;
+            const unsigned seq = ring.seq + (unsigned)(i + q);
+            if (i + q < count) got = tc::mbar_wait(&ring.bar[seq % kRingDepth], (seq / kRingDepth) & 1u, ring.timeoutNs);
+            ok = ok && __all_sync(0xffffffffu, got);
+            const int* sc = ring.col + (seq % kRingDepth) * kRingStage + lane;
+            const float* sv = ring.val + (seq % kRingDepth) * kRingStage + lane;
+#pragma unroll
+            for (int u = 0; u < kRingWidth; ++u) {
+                c[q][u] = ok && u < W[q] ? sc[u * kSlice] : -1;
+                v[q][u] = ok && u < W[q] ? sv[u * kSlice] : 0.0f;
+            }
+        }
+        if (!ok) {
+            if (lane == 0 && atomicCAS(&ring.sync->abort, 0, 1) == 0) ring.sync->where = 900;
+            break;
+        }
+        __syncwarp();   // every lane has read the step's stages: refill them kRingDepth slices ahead
+#pragma unroll
+        for (int q = 0; q < S; ++q)
+            if (issued < count) {
+                issue(issued);
+                ++issued;
+            }
+        TA g[S][kRingWidth];
+#pragma unroll
+        for (int q = 0; q < S; ++q)
+#pragma unroll
+            for (int u = 0; u < kRingWidth; ++u) g[q][u] = c[q][u] >= 0 ? gather(c[q][u]) : TA(0);
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+            if (i + q >= count) continue;
+            TA self = TA(0);
+            if constexpr (Diff) self = row_self<TA>(pv[q]);
+            TA acc = TA(0);
+#pragma unroll
+            for (int u = 0; u < kRingWidth; ++u) {
+                if (u < W[q]) {
+                    if (Diff) acc = fma(TA(v[q][u]), g[q][u] - self, acc);
+                    else acc = fma(TA(v[q][u]), g[q][u], acc);
+                }
+            }
+            const int row = (sFirst + (i + q) * nw) * kSlice + lane;
+            if (row < re) epi(row, acc, pv[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+            const int row = (sFirst + (i + S + q) * nw) * kSlice + lane;
+            if (i + S + q < count) pv[q] = row < re ? pre(row) : PreT{};
+        }
+        if (((i + S) & 31) == 0) {
+            ++cur;
+            mb0 = mb1;
+            me0 = me1;
+            meta(cur + 1, mb1, me1);
+        }
+    }
+    // after a time-out: the copies still in flight land before the ring is left (bounded waits)
+    for (int j = i; j < issued; ++j) {
+        const unsigned seq = ring.seq + (unsigned)j;
+        tc::mbar_wait(&ring.bar[seq % kRingDepth], (seq / kRingDepth) & 1u, ring.timeoutNs);
+    }
+    __syncwarp();
+    ring.seq += (unsigned)issued;
+}
+
 // sum_j a_ij gather(j) (or its difference form) with epi(row, sum, gather(row)).
 template <typename TV, typename TA, bool Diff, int U = kUnroll, bool Wide = false, typename Gather, typename Epi>
 __device__ __forceinline__ void sell_spmv(const int* __restrict__ sliceStart, const int* __restrict__ col,
@@ -465,6 +652,30 @@ __device__ __forceinline__ void matrix_product(const int* sellStart, const int* 
     } else {
         warp_spmv<TV, TA, Diff>(rowptr, col, val, rb, re, stage, gather,
                                 [&](int row, TA acc) { epi(row, acc, gather(row)); });
+    }
+}
+
+// The FP32 difference-form product of the mixed solvers, q_i = sum_j a_ij (p_j - p_i) + rowsum_i p_i: through
+// the warp's ring for narrow matrices when the kernel has one, else the register-pipelined SELL-32 product (or the
+// CSR product without a SELL copy).  epi(row, sum with the row-sum term, p_row).
+template <bool Wide, int U = kUnroll, typename Gather, typename Epi>
+__device__ __forceinline__ void product32(SellRing* ring, const CgArgs& a, int rb, int re, float* stage,
+                                          Gather gather, Epi epi) {
+    auto pre = [&](int row) { return DiffPre<float>{gather(row), a.rowsum32[row]}; };
+    auto fin = [&](int row, float acc, const DiffPre<float>& q) { epi(row, fmaf(q.rs, q.self, acc), q.self); };
+    if constexpr (!Wide) {
+        if (ring && a.sellStart) {
+            sell_rows_ring<float, true>(*ring, a.sellStart, a.sellCol, a.sellVal32, rb, re, gather, pre, fin);
+            return;
+        }
+    }
+    if (a.sellStart) {
+        if constexpr (Wide) sell_rows_wide<float, float, true, 1, U>(a.sellStart, a.sellCol, a.sellVal32, rb, re,
+                                                                   gather, pre, fin);
+        else sell_rows<float, float, true, 1, U>(a.sellStart, a.sellCol, a.sellVal32, rb, re, gather, pre, fin);
+    } else {
+        warp_spmv<float, float, true>(a.rowptr, a.col, a.val32, rb, re, stage, gather,
+                                      [&](int row, float acc) { fin(row, acc, pre(row)); });
     }
 }
 
@@ -608,7 +819,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
 template <bool Wide = false>
-static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
+static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring = nullptr) {
     float* stage32 = reinterpret_cast<float*>(stage);
     const int G = t.size;
     int rb, re;
@@ -691,10 +902,8 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
             // p.q accumulates in double-float so that the FP64 pipe does no per-row work
             float pqHi = 0.f, pqLo = 0.f;
-            matrix_product<float, float, true, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
-                                               stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
                                                [&](int row, float acc, float pi) {
-                                                   acc = fmaf(a.rowsum32[row], pi, acc);
                                                    pc[row] = pi;
                                                    a.q32[row] = acc;
                                                    df_acc(pqHi, pqLo, pi, acc);

@@ -106,6 +106,7 @@ struct FactorView {
     int colourRow[kMaxColours + 1] = {};      // colour c = permuted rows [colourRow[c], colourRow[c+1]) (x 32)
     int nNatural = 0;                         // rows of the caller's system
     const int* perm = nullptr;                // permuted row -> caller's row (-1: padding row)
+    int loMaxW = 0, upMaxW = 0;               // entries per row of the widest lower / upper slice
     const int* loStart = nullptr;             // lower part (L_ij, colour j < colour i), SELL-32, permuted rows
     const int* loCol = nullptr;
     const double* loVal = nullptr;
@@ -141,6 +142,7 @@ struct Factor {
     Csr Ap;                                    // P A P^T (padded), with its SELL copies
     DevBuf<int> apFrom;                        // Ap value k = A.val[apFrom[k]] (-1: padding diagonal, 1.0)
     DevBuf<int> loStart, loCol, loFrom, upStart, upCol, upFrom;
+    int loMaxW = 0, upMaxW = 0;
     DevBuf<double> loVal, upVal, dinv;
     DevBuf<float> loVal32, upVal32, dinv32;
     int kind = 0;                              // NSF_PRECOND_NONE / IC0 / LEARNED
@@ -164,6 +166,16 @@ struct GridSync {
     int abort;
     int where;
 };
+
+// Control state of a mixed-precision PCG solve: the recurrence scalars and counters, identical in every thread of
+// the solve.  The split form keeps it in device memory between its refresh and inner-iteration kernels.
+struct PcgLoop {
+    double rr64, bb, target, rz, beta, rrBest, rrCycle, rrRef;
+    int it, refresh, stalls, itRef;
+    int first, resetP, flip, innerBreakdown;
+    int state, status;
+};
+enum { kLoopInner = 1, kLoopRefresh = 2, kLoopDone = 3 };
 
 // Kernel-level arguments of the persistent CG solvers.
 struct CgArgs {
@@ -195,6 +207,8 @@ struct CgArgs {
     CgInfo* info;
     int maxIt;
     int fallbackMaxIt;       // preconditioned solvers: iteration budget of the plain-CG fallback (0: what is left)
+    PcgLoop* loop;           // split mixed PCG: the control state between kernels
+    int loopInit;            // split mixed PCG: this refresh kernel starts the solve
     double tol2;
     double innerTol2;
     int maxOuter;
@@ -221,8 +235,10 @@ struct CgWorkspace {
     DevBuf<double> partials;
     DevBuf<GridSync> sync;
     DevBuf<CgInfo> info;     // ring of infos (one per solve in a step)
+    DevBuf<PcgLoop> loop;    // split mixed PCG control state
     int grid = 0;            // persistent grid size (blocks)
     int block = 0;
+    int gridInner = 0;       // grid of the split mixed PCG's inner-iteration kernel
 };
 
 // launch helpers implemented in nsf_cg.cu / nsf_sparse.cu
@@ -230,6 +246,9 @@ void cg_configure(CgWorkspace& ws, int device);
 // wide: the matrix has slices wider than kSellChunk entries per row (the kernels' pipelined product for them)
 constexpr int kSellChunk = 8;
 void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, bool wide, cudaStream_t s);
+// The split mixed PCG (narrow matrices): refresh kernel, then inner-iteration and refresh kernels until the solve
+// is done; one small device-to-host read per refresh cycle.
+void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
 void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
 void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
                      const double* bcValue, double* y, cudaStream_t s);

@@ -71,37 +71,53 @@ __device__ __forceinline__ void colour0_store(const FactorView& F, TA* w, int ro
 // Forward colours 1..C-1 and backward colours C-2..0 of M^-1 r (colour 0 already done), then the grid-wide r.z.
 // Each colour phase is the pipelined SELL-32 product over the colour's rows of L (or L^T).  `rz` holds this
 // thread's r.z terms so far.  Returns false on a barrier timeout.
-template <typename TV, typename TA>
+// One colour phase of a sweep: through the warp's ring when the kernel has one and the factor is narrow enough
+// (FP32 factors), else the register-pipelined SELL-32 product.
+// (Lean: one slice stream per warp, for the kernels that run at more CTAs per SM.)
+template <typename TV, typename TA, bool Lean = false, typename Gather, typename Pre, typename Epi>
+__device__ __forceinline__ void sweep_rows(SellRing* ring, int maxW, const int* start, const int* col, const TV* val,
+                                           int r0, int r1, Gather gather, Pre pre, Epi epi) {
+    if constexpr (sizeof(TV) == 4) {
+        if (ring && maxW <= kRingWidth) {
+            sell_rows_ring<TA, false>(*ring, start, col, val, r0, r1, gather, pre, epi);
+            return;
+        }
+    }
+    sell_rows<TV, TA, false, (sizeof(TA) == 4 && !Lean) ? 2 : 1, 4>(start, col, val, r0, r1, gather, pre, epi);
+}
+
+template <typename TV, typename TA, bool Lean = false>
 __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, const TV* loVal, const TV* upVal,
-                               const TA* dinv, DotAcc<TA>& rz, double* smem, int& where, double& rzOut) {
+                               const TA* dinv, DotAcc<TA>& rz, double* smem, int& where, double& rzOut,
+                               SellRing* ring = nullptr) {
     const FactorView& F = a.f;
     const int C = F.colours;
     for (int c = 1; c < C; ++c) {
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
         const bool last = c == C - 1;
-        sell_rows<TV, TA, false, sizeof(TA) == 4 ? 2 : 1, 4>(F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
-                                 [&](int i) { return SweepRow<TA>{r[i], dinv[i], TA(0)}; },
-                                 [&](int i, TA acc, const SweepRow<TA>& q) {
-                                     TA y = (q.src - acc) * q.d;
-                                     if (last) {   // backward step of the last colour: z_i = y_i / L_ii
-                                         y *= q.d;
-                                         rz.add(q.src, y);
-                                     }
-                                     w[i] = y;
-                                 });
+        sweep_rows<TV, TA, Lean>(ring, F.loMaxW, F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
+                           [&](int i) { return SweepRow<TA>{r[i], dinv[i], TA(0)}; },
+                           [&](int i, TA acc, const SweepRow<TA>& q) {
+                               TA y = (q.src - acc) * q.d;
+                               if (last) {   // backward step of the last colour: z_i = y_i / L_ii
+                                   y *= q.d;
+                                   rz.add(q.src, y);
+                               }
+                               w[i] = y;
+                           });
         if (!t.barrier(where++)) return false;
     }
     for (int c = C - 2; c >= 0; --c) {
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
-        sell_rows<TV, TA, false, sizeof(TA) == 4 ? 2 : 1, 4>(F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
-                                 [&](int i) { return SweepRow<TA>{w[i], dinv[i], r[i]}; },
-                                 [&](int i, TA acc, const SweepRow<TA>& q) {
-                                     const TA z = (q.src - acc) * q.d;
-                                     rz.add(q.r, z);
-                                     w[i] = z;
-                                 });
+        sweep_rows<TV, TA, Lean>(ring, F.upMaxW, F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
+                           [&](int i) { return SweepRow<TA>{w[i], dinv[i], r[i]}; },
+                           [&](int i, TA acc, const SweepRow<TA>& q) {
+                               const TA z = (q.src - acc) * q.d;
+                               rz.add(q.r, z);
+                               w[i] = z;
+                           });
         if (c > 0 && !t.barrier(where++)) return false;
     }
     const double part = block_sum(rz.value(), smem);
@@ -290,172 +306,213 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
 // more iterations than the caller allows (the plain method's count), the solve finishes with plain FP64 CG.
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r.z
 // ---------------------------------------------------------------------------------------------------
+// Mixed-precision PCG on the permuted system, as two steps over a PcgLoop state:
+//   refresh: (fold the FP32 correction into x,) true residual b - A64 x in FP64, the stopping and stagnation tests,
+//            the sweeps of M^-1 r, and the restart decision for the recurrence;
+//   inner:   FP32 iterations (product, x/r update, sweeps) until the FP32 residual has fallen by innerTol since the
+//            last true residual, the stopping test is met or the iteration budget is spent.
+// Both return false on a barrier time-out.  partial regions: 0 = p.q, 1 = r.r, 2 = r64.r64, 3 = b.b, 4 = r.z
+__device__ __forceinline__ void pcg_loop_init(PcgLoop& L) {
+    L.rr64 = L.bb = L.target = L.rz = L.beta = 0.0;
+    L.rrBest = L.rrCycle = INFINITY;
+    L.rrRef = 0.0;
+    L.it = L.refresh = L.stalls = L.itRef = 0;
+    L.first = 1;
+    L.resetP = 1;
+    L.flip = 0;
+    L.innerBreakdown = 0;
+    L.state = kLoopRefresh;
+    L.status = NSF_ERR_NOT_CONVERGED;
+}
+
 template <bool Wide = false>
-static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, double* smem) {
+static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
+                                         PcgLoop& L, int& where) {
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x;
     int rb, re;
     team_rows(a.n, t, rb, re);
     const double* b = a.b;   // permuted right-hand side (permute_in); x0 == x
     float* w = F.w32;
-
-    int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 300, stalls = 0;
-    double rr64 = 0, bb = 0, target = 0, rz = 0, beta = 0.0, rrBest = INFINITY, rrCycle = INFINITY;
-    float* pprev = a.p32a;
-    float* pcur = a.p32b;
-    bool first = true, resetP = true, timedOut = false;
-    while (true) {
-        // true residual r = b - A64 x, r32 = (float) r, d32 = 0, colour 0 of the forward sweep
-        const double* xs = first ? a.x0 : a.x;
-        double rrp = 0, bbp = 0;
-        DotAcc<float> rzp;
-        matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
-                                              stage, [&](int c) { return xs[c]; },
-                                  [&](int row, double acc, double) {
-                                      const double bi = b[row];
-                                      const double ri = bi - acc;
-                                      const float r32 = (float)ri;
-                                      a.r32[row] = r32;
-                                      a.d32[row] = 0.0f;
-                                      if (resetP) pprev[row] = 0.0f;   // restart: p = z (beta = 0)
-                                      rrp = fma(ri, ri, rrp);
-                                      bbp = fma(bi, bi, bbp);
-                                      colour0_row<float>(F, w, F.dinv32, row, r32, rzp);
-                                  });
-        rrp = block_sum(rrp, smem);
-        bbp = block_sum(bbp, smem);
-        if (threadIdx.x == 0) {
-            a.partials[2 * G + t.rank] = rrp;
-            a.partials[3 * G + t.rank] = bbp;
-        }
-        if (!t.barrier(where++)) { timedOut = true; break; }
-        rr64 = grid_sum(a.partials + 2 * G, G, smem);
-        if (first) {
-            bb = grid_sum(a.partials + 3 * G, G, smem);
-            target = bb > 0 ? a.tol2 * bb : a.tol2 * rr64;
-        }
-        if (!(rr64 == rr64) || isinf(rr64)) { status = NSF_ERR_BREAKDOWN; break; }
-        if (rr64 <= target) { status = NSF_OK; break; }
-        if (it >= a.maxIt || refresh >= a.maxOuter) break;
-        if (refresh > 0 && rr64 > 0.81 * rrBest) {   // stagnation guard (see team_cg_mixed)
-            if (++stalls >= 3) break;
-        } else {
-            stalls = 0;
-        }
-        rrBest = fmin(rrBest, rr64);
-        double rzT = 0;
-        if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT)) {
-            timedOut = true;
-            break;
-        }
-        if (!(rzT > 0.0) || isinf(rzT)) { status = NSF_ERR_BREAKDOWN; break; }
-        // Continue the recurrence from the refreshed residual (beta' = r.z / r_prev.z_prev), unless the cycle just
-        // ended has drifted: its FP32 recursive residual fell by innerTol^2 but the true one by less than a quarter.
-        // Then restart it (p = z).  Carried recurrences converged fastest on the large pressure systems once the flow
-        // had settled, but in the first steps of a cavity they drifted and took up to 5x the iterations.
-        const bool drifted = refresh > 0 && rr64 > 0.25 * rrCycle;
-        beta = (resetP || drifted) ? 0.0 : rzT / rz;
-        resetP = false;
-        rz = rzT;
-        rrCycle = rr64;
-        const double rrRef = rr64;
-        const int itRef = it;
-        ++refresh;
-        first = false;
-
-        bool innerBreakdown = false;
-        while (it < a.maxIt) {
-            const float betaf = (float)beta;
-            const float* pp = pprev;
-            float* pc = pcur;
-            float pqHi = 0.f, pqLo = 0.f;
-            matrix_product<float, float, true, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal32, a.rowptr, a.col, a.val32, rb, re,
-                                               reinterpret_cast<float*>(stage),
-                                               [&](int c) { return fmaf(betaf, pp[c], w[c]); },
-                                               [&](int row, float acc, float pi) {
-                                                   acc = fmaf(a.rowsum32[row], pi, acc);
-                                                   pc[row] = pi;
-                                                   a.q32[row] = acc;
-                                                   df_acc(pqHi, pqLo, pi, acc);
-                                               });
-            const double pq = block_sum((double)pqHi + (double)pqLo, smem);
-            if (threadIdx.x == 0) a.partials[t.rank] = pq;
-            if (!t.barrier(where++)) { timedOut = true; break; }
-            const double pqs = grid_sum(a.partials, G, smem);
-            if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
-            const float alphaf = (float)(rz / pqs);
-            float rrHi = 0.f, rrLo = 0.f;
-            DotAcc<float> rzn;
-            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
-                float pi[kRows], qi[kRows], di[kRows], ri[kRows], vi[kRows];
-#pragma unroll
-                for (int u = 0; u < kRows; ++u) {
-                    const int i = i0 + u * bs;
-                    if (i < re) {
-                        pi[u] = pc[i];
-                        qi[u] = a.q32[i];
-                        di[u] = a.d32[i];
-                        ri[u] = a.r32[i];
-                        vi[u] = i < F.colourRow[1] ? F.dinv32[i] : 0.0f;
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kRows; ++u) {
-                    const int i = i0 + u * bs;
-                    if (i < re) {
-                        a.d32[i] = fmaf(alphaf, pi[u], di[u]);
-                        const float rn = fmaf(-alphaf, qi[u], ri[u]);
-                        a.r32[i] = rn;
-                        df_acc(rrHi, rrLo, rn, rn);
-                        colour0_store<float>(F, w, i, rn, vi[u], rzn);
-                    }
-                }
-            }
-            const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
-            if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
-            if (!t.barrier(where++)) { timedOut = true; break; }
-            const double rrs = grid_sum(a.partials + G, G, smem);
-            ++it;
-            { float* tmp = pprev; pprev = pcur; pcur = tmp; }
-            if (!(rrs == rrs) || isinf(rrs)) { innerBreakdown = true; break; }
-            if (rrs <= a.innerTol2 * rrRef || rrs <= target) break;   // time for a true residual
-            if (it - itRef >= kMaxInnerBetweenRefresh) break;
-            double rzs = 0;
-            if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzn, smem, where, rzs)) {
-                timedOut = true;
-                break;
-            }
-            if (!(rzs > 0.0) || isinf(rzs)) { innerBreakdown = true; break; }
-            beta = rzs / rz;
-            rz = rzs;
-        }
-        if (timedOut) break;
+    float* pprev = L.flip ? a.p32b : a.p32a;
+    if (!L.first) {   // fold the FP32 correction into x; the true residual gathers x across blocks
         for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
-        if (!t.barrier(where++)) { timedOut = true; break; }
-        if (innerBreakdown) resetP = true;
+        if (!t.barrier(where++)) return false;
+        if (L.innerBreakdown) L.resetP = 1;
     }
-    if (timedOut) {
-        write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb);
-        return NSF_ERR_BARRIER_TIMEOUT;
+    // true residual r = b - A64 x, r32 = (float) r, d32 = 0, colour 0 of the forward sweep
+    const double* xs = L.first ? a.x0 : a.x;
+    const bool resetP = L.resetP != 0;
+    double rrp = 0, bbp = 0;
+    DotAcc<float> rzp;
+    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
+                                                   stage, [&](int c) { return xs[c]; },
+                                                   [&](int row, double acc, double) {
+                                                       const double bi = b[row];
+                                                       const double ri = bi - acc;
+                                                       const float r32 = (float)ri;
+                                                       a.r32[row] = r32;
+                                                       a.d32[row] = 0.0f;
+                                                       if (resetP) pprev[row] = 0.0f;   // restart: p = z
+                                                       rrp = fma(ri, ri, rrp);
+                                                       bbp = fma(bi, bi, bbp);
+                                                       colour0_row<float>(F, w, F.dinv32, row, r32, rzp);
+                                                   });
+    rrp = block_sum(rrp, smem);
+    bbp = block_sum(bbp, smem);
+    if (threadIdx.x == 0) {
+        a.partials[2 * G + t.rank] = rrp;
+        a.partials[3 * G + t.rank] = bbp;
     }
-    if (status == NSF_ERR_NOT_CONVERGED && (a.fallbackMaxIt > 0 || it < a.maxIt)) {
-        // plain FP64 CG from the current iterate, with the plain method's own iteration budget
+    if (!t.barrier(where++)) return false;
+    L.rr64 = grid_sum(a.partials + 2 * G, G, smem);
+    if (L.first) {
+        L.bb = grid_sum(a.partials + 3 * G, G, smem);
+        L.target = L.bb > 0 ? a.tol2 * L.bb : a.tol2 * L.rr64;
+    }
+    L.state = kLoopDone;
+    if (!(L.rr64 == L.rr64) || isinf(L.rr64)) { L.status = NSF_ERR_BREAKDOWN; return true; }
+    if (L.rr64 <= L.target) { L.status = NSF_OK; return true; }
+    if (L.it >= a.maxIt || L.refresh >= a.maxOuter) return true;
+    if (L.refresh > 0 && L.rr64 > 0.81 * L.rrBest) {   // stagnation guard (see team_cg_mixed)
+        if (++L.stalls >= 3) return true;
+    } else {
+        L.stalls = 0;
+    }
+    L.rrBest = fmin(L.rrBest, L.rr64);
+    double rzT = 0;
+    if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT, ring))
+        return false;
+    if (!(rzT > 0.0) || isinf(rzT)) { L.status = NSF_ERR_BREAKDOWN; return true; }
+    // Continue the recurrence from the refreshed residual (beta' = r.z / r_prev.z_prev), unless the cycle just
+    // ended has drifted: its FP32 recursive residual fell by innerTol^2 but the true one by less than a quarter.
+    // Then restart it (p = z).  Carried recurrences converged fastest on the large pressure systems once the flow
+    // had settled, but in the first steps of a cavity they drifted and took up to 5x the iterations.
+    const bool drifted = L.refresh > 0 && L.rr64 > 0.25 * L.rrCycle;
+    L.beta = (L.resetP || drifted) ? 0.0 : rzT / L.rz;
+    L.resetP = 0;
+    L.rz = rzT;
+    L.rrCycle = L.rr64;
+    L.rrRef = L.rr64;
+    L.itRef = L.it;
+    ++L.refresh;
+    L.first = 0;
+    L.state = kLoopInner;
+    return true;
+}
+
+template <bool Wide = false, bool Lean = false>
+static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
+                                       PcgLoop& L, int& where) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    float* w = F.w32;
+    L.innerBreakdown = 0;
+    while (L.it < a.maxIt) {
+        const float betaf = (float)L.beta;
+        const float* pp = L.flip ? a.p32b : a.p32a;
+        float* pc = L.flip ? a.p32a : a.p32b;
+        float pqHi = 0.f, pqLo = 0.f;
+        product32<Wide, Lean ? 6 : kUnroll>(ring, a, rb, re, reinterpret_cast<float*>(stage),
+                        [&](int c) { return fmaf(betaf, pp[c], w[c]); },
+                        [&](int row, float acc, float pi) {
+                            pc[row] = pi;
+                            a.q32[row] = acc;
+                            df_acc(pqHi, pqLo, pi, acc);
+                        });
+        const double pq = block_sum((double)pqHi + (double)pqLo, smem);
+        if (threadIdx.x == 0) a.partials[t.rank] = pq;
+        if (!t.barrier(where++)) return false;
+        const double pqs = grid_sum(a.partials, G, smem);
+        if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
+        const float alphaf = (float)(L.rz / pqs);
+        float rrHi = 0.f, rrLo = 0.f;
+        DotAcc<float> rzn;
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
+            float pi[kRows], qi[kRows], di[kRows], ri[kRows], vi[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    pi[u] = pc[i];
+                    qi[u] = a.q32[i];
+                    di[u] = a.d32[i];
+                    ri[u] = a.r32[i];
+                    vi[u] = i < F.colourRow[1] ? F.dinv32[i] : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                    const float rn = fmaf(-alphaf, qi[u], ri[u]);
+                    a.r32[i] = rn;
+                    df_acc(rrHi, rrLo, rn, rn);
+                    colour0_store<float>(F, w, i, rn, vi[u], rzn);
+                }
+            }
+        }
+        const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
+        if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
+        if (!t.barrier(where++)) return false;
+        const double rrs = grid_sum(a.partials + G, G, smem);
+        ++L.it;
+        L.flip ^= 1;
+        if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
+        if (rrs <= a.innerTol2 * L.rrRef || rrs <= L.target) break;   // time for a true residual
+        if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
+        double rzs = 0;
+        if (!precond_sweeps<float, float, Lean>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzn, smem, where, rzs, ring))
+            return false;
+        if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
+        L.beta = rzs / L.rz;
+        L.rz = rzs;
+    }
+    L.state = kLoopRefresh;
+    return true;
+}
+
+// The end of a mixed PCG solve (state kLoopDone): when it stopped short of the tolerance with budget left, plain
+// FP64 CG from the current iterate with the plain method's own budget; then the solve's info.
+template <bool Wide = false>
+static __device__ int pcg_mixed_finish(Team& t, const CgArgs& a, double* stage, double* smem, const PcgLoop& L) {
+    if (L.status == NSF_ERR_NOT_CONVERGED && (a.fallbackMaxIt > 0 || L.it < a.maxIt)) {
         CgArgs f = a;
         f.bRowptr = nullptr;
-        f.b = b;
+        f.b = a.b;
         f.x0 = a.x;
-        f.maxIt = a.fallbackMaxIt > 0 ? a.fallbackMaxIt : a.maxIt - it;
+        f.maxIt = a.fallbackMaxIt > 0 ? a.fallbackMaxIt : a.maxIt - L.it;
         const int fst = team_cg_fp64<Wide>(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
-            a.info->iterations += it;
-            a.info->outer = refresh;
+            a.info->iterations += L.it;
+            a.info->outer = L.refresh;
             a.info->fallback = 1;
         }
         return fst;
     }
-    write_info(t, a, it, status, refresh, rr64, bb);
-    return status;
+    write_info(t, a, L.it, L.status, L.refresh, L.rr64, L.bb);
+    return L.status;
+}
+
+// The whole mixed PCG solve in one persistent launch.
+template <bool Wide = false>
+static __device__ int pcg_mixed_body(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
+    PcgLoop L;
+    pcg_loop_init(L);
+    int where = 300;
+    while (true) {
+        if (!pcg_mixed_refresh<Wide>(t, a, stage, smem, ring, L, where) ||
+            (L.state == kLoopInner && !pcg_mixed_inner<Wide>(t, a, stage, smem, ring, L, where))) {
+            write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, L.refresh, L.rr64, L.bb);
+            return NSF_ERR_BARRIER_TIMEOUT;
+        }
+        if (L.state == kLoopDone) break;
+    }
+    return pcg_mixed_finish<Wide>(t, a, stage, smem, L);
 }
 
 // Preconditioned solves of the caller's system: permute in, solve the colour-permuted system, permute out.
@@ -474,15 +531,74 @@ static __device__ int team_pcg_fp64(Team& t, const CgArgs& a, double* stage, dou
 }
 
 template <bool Wide = false>
-static __device__ int team_pcg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
+static __device__ int team_pcg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring = nullptr) {
     int where = 190;
     if (!permute_in<Wide>(t, a, stage, where)) {
         write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
         return NSF_ERR_BARRIER_TIMEOUT;
     }
-    const int st = pcg_mixed_body<Wide>(t, a, stage, smem);
+    const int st = pcg_mixed_body<Wide>(t, a, stage, smem, ring);
     if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
     return st;
+}
+
+// The split form (narrow matrices; a.loop holds the state between launches).  Refresh launch: on the first, the
+// permutation in and a fresh state; a true-residual refresh; when the solve is done, its end and the permutation
+// out.  Inner launch: FP32 iterations up to the next refresh.  State and info are written by thread 0 of block 0
+// (every thread holds the same state).
+static __device__ void pcg_loop_store(const Team& t, const CgArgs& a, const PcgLoop& L) {
+    if (t.rank == 0 && threadIdx.x == 0) *a.loop = L;
+}
+
+static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
+    int where = 190;
+    PcgLoop L;
+    if (a.loopInit) {
+        pcg_loop_init(L);
+        if (!permute_in<false>(t, a, stage, where)) {
+            write_info(t, a, 0, NSF_ERR_BARRIER_TIMEOUT, 0, 0, 0);
+            L.state = kLoopDone;
+            pcg_loop_store(t, a, L);
+            return;
+        }
+    } else {
+        L = *a.loop;
+    }
+    if (!pcg_mixed_refresh<false>(t, a, stage, smem, ring, L, where)) {
+        write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, L.refresh, L.rr64, L.bb);
+        L.state = kLoopDone;
+        pcg_loop_store(t, a, L);
+        return;
+    }
+    if (L.state == kLoopDone) {
+        const int st = pcg_mixed_finish<false>(t, a, stage, smem, L);
+        if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
+    }
+    pcg_loop_store(t, a, L);
+}
+
+static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
+    int where = 400;
+    // the fields the inner iterations read or write (the rest of the state stays in memory)
+    const PcgLoop& G = *a.loop;
+    PcgLoop L;
+    L.rz = G.rz;
+    L.beta = G.beta;
+    L.rrRef = G.rrRef;
+    L.target = G.target;
+    L.it = G.it;
+    L.itRef = G.itRef;
+    L.flip = G.flip;
+    const bool ok = pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
+    if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
+    if (t.rank == 0 && threadIdx.x == 0) {
+        a.loop->rz = L.rz;
+        a.loop->beta = L.beta;
+        a.loop->it = L.it;
+        a.loop->flip = L.flip;
+        a.loop->innerBreakdown = L.innerBreakdown;
+        a.loop->state = ok ? L.state : kLoopDone;
+    }
 }
 
 }  // namespace nsf

@@ -30,6 +30,7 @@ int grid_for(int64_t work, int threads) {
 // row 32 s + lane at start[s] + 32 k + lane, padded with column -1.  `from` is carried along per entry.
 struct HostSell {
     std::vector<int> start, col, from;
+    int maxWidth = 0;
 };
 
 HostSell build_sell(int rows, const std::vector<int>& rowptr, const std::vector<int>& col,
@@ -41,6 +42,7 @@ HostSell build_sell(int rows, const std::vector<int>& rowptr, const std::vector<
     for (int s = 0; s < nSlices; ++s) {
         int w = 0;
         for (int l = 0; l < 32; ++l) w = std::max(w, rowptr[s * 32 + l + 1] - rowptr[s * 32 + l]);
+        S.maxWidth = std::max(S.maxWidth, w);
         S.start[s] = (int)total;
         total += (int64_t)w * 32;
         if (total > INT32_MAX) throw Error{NSF_ERR_BAD_ARG, "factor too large for 32-bit offsets"};
@@ -219,6 +221,8 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
     F.aIndexL.upload(aIdx.data(), aIdx.size(), s);
     F.aIndexDiag.upload(aDiag.data(), aDiag.size(), s);
     F.perm.upload(perm.data(), perm.size(), s);
+    F.loMaxW = lo.maxWidth;
+    F.upMaxW = up.maxWidth;
     F.loStart.upload(lo.start.data(), lo.start.size(), s);
     F.loCol.upload(lo.col.data(), lo.col.size(), s);
     F.loFrom.upload(lo.from.data(), lo.from.size(), s);
@@ -365,6 +369,8 @@ FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     for (int c = 0; c <= F.colours; ++c) v.colourRow[c] = F.colourRow[c];
     v.nNatural = F.rows;
     v.perm = F.perm.get();
+    v.loMaxW = F.loMaxW;
+    v.upMaxW = F.upMaxW;
     v.loStart = F.loStart.get();
     v.loCol = F.loCol.get();
     v.loVal = F.loVal.get();

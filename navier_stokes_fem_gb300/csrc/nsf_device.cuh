@@ -11,14 +11,16 @@ constexpr int kWarps = kCgThreads / 32;
 constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 constexpr int kRows = 4;      // rows per thread with their loads in flight in the vector phases
+// reduction slots of a CG kernel's shared memory: [0, 16) block_sum, [16, 32) spare, 32 grid_sum, 33 block_scalar
+constexpr int kSmemSlots = 34;
 
 // Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area (the ring
 // kernels stage in their ring memory instead, NSF_RING_SHARED).
 #define NSF_KERNEL_SHARED()          \
-    __shared__ double smem[33];      \
+    __shared__ double smem[kSmemSlots]; \
     __shared__ double stage[kWarps * 2 * kStage]
 #define NSF_RING_SHARED()                                     \
-    __shared__ double smem[33];                               \
+    __shared__ double smem[kSmemSlots];                       \
     extern __shared__ __align__(128) unsigned char dsm[];     \
     double* stage = reinterpret_cast<double*>(dsm)
 
@@ -119,23 +121,60 @@ __device__ __forceinline__ void df_acc(float& hi, float& lo, float a, float b) {
     lo = __fadd_rn(lo, __fadd_rn(se, pe));
 }
 
-// Sum of the per-block partials of one region, identical in every block and thread.  Every thread loads its
-// partials at once (one memory latency), then a fixed-order warp and block reduction.
-static __device__ double grid_sum(const double* part, int G, double* smem) {
-    const int tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
-    double p[4];
+// block_sum of a double-float pair (hi + lo, the FP32 dot accumulators): the warp stage adds pairs in FP32
+// (Knuth's two-sum), so only one lane per warp and thread 0 touch the FP64 pipe, which on GB300 is too narrow for
+// per-thread scalar work.  Result valid in thread 0; fixed order -> deterministic.
+static __device__ double block_sum_df(float hi, float lo, double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) p[k] = tid + k * bs < G ? ld_cg(part + tid + k * bs) : 0.0;
-    double v = (p[0] + p[1]) + (p[2] + p[3]);
-    for (int i = tid + 4 * bs; i < G; i += bs) v += ld_cg(part + i);   // (teams wider than 4 blocks per thread)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) smem[16 + warp] = v;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float bh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float bl = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float sh = __fadd_rn(hi, bh);
+        const float bp = __fsub_rn(sh, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(sh, bp)), __fsub_rn(bh, bp));
+        hi = sh;
+        lo = __fadd_rn(__fadd_rn(lo, bl), e);
+    }
+    if (lane == 0) smem[warp] = (double)hi + (double)lo;
     __syncthreads();
     double t = 0;
-    for (int w = 0; w < nw; ++w) t += smem[16 + w];
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += smem[w];
     __syncthreads();
     return t;
+}
+
+// Sum of the per-block partials of one region, identical in every block and thread.  Warp 0 loads them (each
+// lane a strided share, all loads in flight at once) and reduces in a fixed order; the sum reaches the other
+// threads through shared memory, so the FP64 work is one warp's, not every thread's.
+static __device__ double grid_sum(const double* part, int G, double* smem) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double p[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[k] = lane + 32 * k < G ? ld_cg(part + lane + 32 * k) : 0.0;
+        double v = (p[0] + p[1]) + (p[2] + p[3]);
+        for (int i = lane + 128; i < G; i += 32) v += ld_cg(part + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) smem[32] = v;
+    }
+    __syncthreads();
+    const double t = smem[32];
+    __syncthreads();
+    return t;
+}
+
+// f() evaluated once by thread 0 and handed to every thread of the block (scalar FP64 work such as the CG
+// coefficients' divisions, kept off the narrow FP64 pipe's per-thread budget).
+template <typename F>
+__device__ __forceinline__ double block_scalar(double* smem, F f) {
+    if (threadIdx.x == 0) smem[33] = f();
+    __syncthreads();
+    const double v = smem[33];
+    __syncthreads();
+    return v;
 }
 
 // Row-range of this CTA within its team: contiguous chunks keep each CTA's gathers local; chunks are whole
@@ -756,7 +795,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
         if (!t.barrier(2)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
         const double pqs = grid_sum(a.partials, G, smem);
         if (!(pqs > 0.0) || isinf(pqs)) { status = NSF_ERR_BREAKDOWN; break; }
-        const double alpha = rr / pqs;
+        const double alpha = block_scalar(smem, [&] { return rr / pqs; });
         // phase B: x += alpha p, r -= alpha q, partial r.r (four rows per thread in flight)
         double rrn = 0;
         for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
@@ -783,7 +822,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
         const double rrs = grid_sum(a.partials + G, G, smem);
         ++it;
         if (!(rrs == rrs) || isinf(rrs)) { status = NSF_ERR_BREAKDOWN; break; }
-        const double beta = rrs / rr;
+        const double beta = block_scalar(smem, [&] { return rrs / rr; });
         rr = rrs;
         if (rr <= target) { status = NSF_OK; break; }
         // phase C: p = r + beta p; the next product gathers p across blocks, hence the third barrier
@@ -908,12 +947,12 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
                                                    a.q32[row] = acc;
                                                    df_acc(pqHi, pqLo, pi, acc);
                                                });
-            const double pq = block_sum((double)pqHi + (double)pqLo, smem);
+            const double pq = block_sum_df(pqHi, pqLo, smem);
             if (threadIdx.x == 0) a.partials[t.rank] = pq;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
             const double pqs = grid_sum(a.partials, G, smem);
             if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
-            const float alphaf = (float)(rr / pqs);
+            const float alphaf = (float)block_scalar(smem, [&] { return rr / pqs; });
             float rrHi = 0.f, rrLo = 0.f;
             for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
                 float pi[kRows], qi[kRows], di[kRows], ri[kRows];
@@ -933,14 +972,14 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
                     }
                 }
             }
-            const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
+            const double rrn = block_sum_df(rrHi, rrLo, smem);
             if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
             const double rrs = grid_sum(a.partials + G, G, smem);
             ++it;
             { float* t = pprev; pprev = pcur; pcur = t; }
             if (!(rrs == rrs) || isinf(rrs)) { innerBreakdown = true; break; }
-            beta = rrs / rr;
+            beta = block_scalar(smem, [&] { return rrs / rr; });
             rrPrev = rr;
             rr = rrs;
             if (rr <= a.innerTol2 * rrRef || rr <= target) break;   // time for a true residual

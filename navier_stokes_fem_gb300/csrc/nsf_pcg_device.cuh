@@ -33,12 +33,12 @@ template <typename TA> struct DotAcc;
 template <> struct DotAcc<double> {
     double v = 0.0;
     __device__ void add(double a, double b) { v = fma(a, b, v); }
-    __device__ double value() const { return v; }
+    __device__ double block(double* smem) const { return block_sum(v, smem); }
 };
 template <> struct DotAcc<float> {
     float hi = 0.f, lo = 0.f;
     __device__ void add(float a, float b) { df_acc(hi, lo, a, b); }
-    __device__ double value() const { return (double)hi + (double)lo; }
+    __device__ double block(double* smem) const { return block_sum_df(hi, lo, smem); }
 };
 
 // Colour-0 rows of the forward sweep (permuted rows [0, colourRow[1])), fused into the phase that writes r_i:
@@ -120,7 +120,7 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
                            });
         if (c > 0 && !t.barrier(where++)) return false;
     }
-    const double part = block_sum(rz.value(), smem);
+    const double part = rz.block(smem);
     if (threadIdx.x == 0) a.partials[4 * t.size + t.rank] = part;
     if (!t.barrier(where++)) return false;
     rzOut = grid_sum(a.partials + 4 * t.size, t.size, smem);
@@ -235,7 +235,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
         if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
         const double pqs = grid_sum(a.partials, G, smem);
         if (!(pqs > 0.0) || isinf(pqs)) { status = NSF_ERR_BREAKDOWN; break; }
-        const double alpha = rz / pqs;
+        const double alpha = block_scalar(smem, [&] { return rz / pqs; });
         // x += alpha p, r -= alpha q, r.r, colour-0 rows of the forward sweep
         double rrn = 0;
         DotAcc<double> rzp;
@@ -277,7 +277,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
             return NSF_ERR_BARRIER_TIMEOUT;
         }
         if (!(rzn > 0.0) || isinf(rzn)) { status = NSF_ERR_BREAKDOWN; break; }
-        beta = rzn / rz;
+        beta = block_scalar(smem, [&] { return rzn / rz; });
         rz = rzn;
     }
     if (status == NSF_ERR_NOT_CONVERGED && a.fallbackMaxIt > 0) {
@@ -410,6 +410,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
     team_rows(a.n, t, rb, re);
     float* w = F.w32;
     L.innerBreakdown = 0;
+    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
     while (L.it < a.maxIt) {
         const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -422,12 +423,12 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
                             a.q32[row] = acc;
                             df_acc(pqHi, pqLo, pi, acc);
                         });
-        const double pq = block_sum((double)pqHi + (double)pqLo, smem);
+        const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;
         const double pqs = grid_sum(a.partials, G, smem);
         if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
-        const float alphaf = (float)(L.rz / pqs);
+        const float alphaf = (float)block_scalar(smem, [&] { return L.rz / pqs; });
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
         for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
@@ -455,20 +456,20 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
                 }
             }
         }
-        const double rrn = block_sum((double)rrHi + (double)rrLo, smem);
+        const double rrn = block_sum_df(rrHi, rrLo, smem);
         if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
         if (!t.barrier(where++)) return false;
         const double rrs = grid_sum(a.partials + G, G, smem);
         ++L.it;
         L.flip ^= 1;
         if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
-        if (rrs <= a.innerTol2 * L.rrRef || rrs <= L.target) break;   // time for a true residual
+        if (rrs <= rrStop) break;   // time for a true residual
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
         double rzs = 0;
         if (!precond_sweeps<float, float, Lean>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzn, smem, where, rzs, ring))
             return false;
         if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
-        L.beta = rzs / L.rz;
+        L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
         L.rz = rzs;
     }
     L.state = kLoopRefresh;

@@ -11,6 +11,7 @@ constexpr int kWarps = kCgThreads / 32;
 constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 constexpr int kRows = 4;      // rows per thread with their loads in flight in the vector phases
+constexpr int kRowsLean = 2;  // (the kernels that run at 4 CTAs per SM)
 // reduction slots of a CG kernel's shared memory: [0, 16) block_sum, [16, 32) spare, 32 grid_sum, 33 block_scalar
 constexpr int kSmemSlots = 34;
 

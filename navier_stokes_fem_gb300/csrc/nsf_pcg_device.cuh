@@ -431,10 +431,11 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
         const float alphaf = (float)block_scalar(smem, [&] { return L.rz / pqs; });
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
-        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {   // kRows rows' loads in flight
-            float pi[kRows], qi[kRows], di[kRows], ri[kRows], vi[kRows];
+        constexpr int R = Lean ? kRowsLean : kRows;
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += R * bs) {   // R rows' loads in flight
+            float pi[R], qi[R], di[R], ri[R], vi[R];
 #pragma unroll
-            for (int u = 0; u < kRows; ++u) {
+            for (int u = 0; u < R; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) {
                     pi[u] = pc[i];
@@ -445,7 +446,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kRows; ++u) {
+            for (int u = 0; u < R; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) {
                     a.d32[i] = fmaf(alphaf, pi[u], di[u]);

@@ -874,6 +874,8 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
 
     int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 10, stalls = 0;
     double rr64 = 0, bb = 0, target = 0, rr = 0, rrPrev = 1.0, beta = 0.0, rrBest = INFINITY;
+    double cycleTol2 = a.innerTol2;   // FP32 residual reduction between true residuals (adapted per cycle)
+    int lastCycle = 0;                // FP32 iterations of the cycle that just ended
     float* pprev = a.p32a;
     float* pcur = a.p32b;
     bool first = true;       // the first true residual gathers x0 and sets the target
@@ -924,6 +926,16 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             stalls = 0;
         }
         rrBest = fmin(rrBest, rr64);
+        // Short cycles (a well-conditioned system: the velocity systems refresh every ~3 iterations at innerTol
+        // 0.1) lengthen while the FP32 recurrence stays accurate: when the true residual matches the recursive
+        // one within 2x in norm, the next cycle may reduce 10x further (to 1e-4 at most); when they differ by more
+        // than 4x the interval returns towards innerTol.  Long cycles (the ill-conditioned pressure system, whose
+        // refreshes cost nothing next to ~1000 FP32 iterations) keep innerTol.
+        if (refresh > 0 && rr > 0.0) {
+            const double drift = rr64 / rr;
+            if (drift < 4.0 && lastCycle < 32) cycleTol2 = fmax(cycleTol2 * 1e-2, 1e-8);
+            else if (drift > 16.0) cycleTol2 = fmin(cycleTol2 * 1e2, a.innerTol2);
+        }
         // continue the recurrence from the refreshed residual: beta' = |r_new|^2 / |r_prev|^2
         beta = resetP ? 0.0 : rrTrue / rrPrev;
         resetP = false;
@@ -983,9 +995,10 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             beta = block_scalar(smem, [&] { return rrs / rr; });
             rrPrev = rr;
             rr = rrs;
-            if (rr <= a.innerTol2 * rrRef || rr <= target) break;   // time for a true residual
+            if (rr <= cycleTol2 * rrRef || rr <= target) break;   // time for a true residual
             if (it - itRef >= kMaxInnerBetweenRefresh) break;        // bound the work between true residuals
         }
+        lastCycle = it - itRef;
         // fold the correction into x (FP64); the next true residual gathers x across blocks
         for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
         if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }

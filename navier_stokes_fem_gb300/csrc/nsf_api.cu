@@ -163,6 +163,7 @@ void ensure_workspace(nsf_device* h, int rows) {
     ws.p0.ensure(rows);
     ws.p1.ensure(rows);
     ws.r32.ensure(rows);
+    ws.r32b.ensure(rows);
     ws.d32.ensure(rows);
     ws.q32.ensure(rows);
     ws.p32a.ensure(rows);
@@ -219,6 +220,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.pbuf0 = ws.p0.get();
     a.pbuf1 = ws.p1.get();
     a.r32 = ws.r32.get();
+    a.r32b = ws.r32b.get();
     a.d32 = ws.d32.get();
     a.q32 = ws.q32.get();
     a.p32a = ws.p32a.get();

@@ -173,6 +173,7 @@ struct PcgLoop {
     double rr64, bb, target, rz, beta, rrBest, rrCycle, rrRef;
     int it, refresh, stalls, itRef;
     int first, resetP, flip, innerBreakdown;
+    int rflip;               // which residual buffer is current (r32 or r32b; the fused inner iterations alternate)
     int state, status;
 };
 enum { kLoopInner = 1, kLoopRefresh = 2, kLoopDone = 3 };
@@ -198,6 +199,7 @@ struct CgArgs {
     double* pbuf0;
     double* pbuf1;
     float* r32;      // mixed precision inner vectors
+    float* r32b;     // (the split PCG's second residual buffer)
     float* d32;
     float* q32;
     float* p32a;
@@ -231,7 +233,7 @@ struct CgArgs {
 // the workspace shared by every solve on a handle (sized for the largest system)
 struct CgWorkspace {
     DevBuf<double> r, q, p0, p1, w, xp, bp;
-    DevBuf<float> r32, d32, q32, p32a, p32b, w32;
+    DevBuf<float> r32, r32b, d32, q32, p32a, p32b, w32;
     DevBuf<double> partials;
     DevBuf<GridSync> sync;
     DevBuf<CgInfo> info;     // ring of infos (one per solve in a step)

@@ -86,13 +86,14 @@ __device__ __forceinline__ void sweep_rows(SellRing* ring, int maxW, const int* 
     sell_rows<TV, TA, false, (sizeof(TA) == 4 && !Lean) ? 2 : 1, 4>(start, col, val, r0, r1, gather, pre, epi);
 }
 
+// (cFirst = 2: colour 1 of the forward sweep, and with two colours its backward step, are already done.)
 template <typename TV, typename TA, bool Lean = false>
 __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, const TV* loVal, const TV* upVal,
                                const TA* dinv, DotAcc<TA>& rz, double* smem, int& where, double& rzOut,
-                               SellRing* ring = nullptr) {
+                               SellRing* ring = nullptr, int cFirst = 1) {
     const FactorView& F = a.f;
     const int C = F.colours;
-    for (int c = 1; c < C; ++c) {
+    for (int c = cFirst; c < C; ++c) {
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
         const bool last = c == C - 1;
@@ -321,6 +322,7 @@ __device__ __forceinline__ void pcg_loop_init(PcgLoop& L) {
     L.resetP = 1;
     L.flip = 0;
     L.innerBreakdown = 0;
+    L.rflip = 0;
     L.state = kLoopRefresh;
     L.status = NSF_ERR_NOT_CONVERGED;
 }
@@ -335,6 +337,7 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
     const double* b = a.b;   // permuted right-hand side (permute_in); x0 == x
     float* w = F.w32;
     float* pprev = L.flip ? a.p32b : a.p32a;
+    float* r32 = L.rflip ? a.r32b : a.r32;   // the current residual buffer
     if (!L.first) {   // fold the FP32 correction into x; the true residual gathers x across blocks
         for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
         if (!t.barrier(where++)) return false;
@@ -350,13 +353,13 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
                                                    [&](int row, double acc, double) {
                                                        const double bi = b[row];
                                                        const double ri = bi - acc;
-                                                       const float r32 = (float)ri;
-                                                       a.r32[row] = r32;
+                                                       const float rf = (float)ri;
+                                                       r32[row] = rf;
                                                        a.d32[row] = 0.0f;
                                                        if (resetP) pprev[row] = 0.0f;   // restart: p = z
                                                        rrp = fma(ri, ri, rrp);
                                                        bbp = fma(bi, bi, bbp);
-                                                       colour0_row<float>(F, w, F.dinv32, row, r32, rzp);
+                                                       colour0_row<float>(F, w, F.dinv32, row, rf, rzp);
                                                    });
     rrp = block_sum(rrp, smem);
     bbp = block_sum(bbp, smem);
@@ -381,7 +384,7 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
     }
     L.rrBest = fmin(L.rrBest, L.rr64);
     double rzT = 0;
-    if (!precond_sweeps<float, float>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT, ring))
+    if (!precond_sweeps<float, float>(t, a, r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT, ring))
         return false;
     if (!(rzT > 0.0) || isinf(rzT)) { L.status = NSF_ERR_BREAKDOWN; return true; }
     // Continue the recurrence from the refreshed residual (beta' = r.z / r_prev.z_prev), unless the cycle just
@@ -468,6 +471,121 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
         double rzs = 0;
         if (!precond_sweeps<float, float, Lean>(t, a, a.r32, w, F.loVal32, F.upVal32, F.dinv32, rzn, smem, where, rzs, ring))
+            return false;
+        if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
+        L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
+        L.rz = rzs;
+    }
+    L.state = kLoopRefresh;
+    return true;
+}
+
+// The split form's inner iterations with the x/r update fused into colour 1 of the forward sweep (two or more
+// colours): colour-0 rows update d, r and y0 = r0 / L_00 as before; colour-1 rows update their d and r in the
+// sweep's pre step and take their lower neighbours' y0 from the previous residual, y0_j = (r_j - alpha q_j) / L_jj
+// (the same arithmetic as the stored y0, so the sweep sees the same values); rows of colours >= 2 update d and r.  The residual alternates between two buffers, since the neighbours' previous r is read while the
+// own rows' new r is written.  On two colours an iteration has 3 grid barriers instead of 4.
+static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
+                                             PcgLoop& L, int& where) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x, C = F.colours;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    float* w = F.w32;
+    const float* dinv = F.dinv32;
+    L.innerBreakdown = 0;
+    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
+    while (L.it < a.maxIt) {
+        const float betaf = (float)L.beta;
+        const float* pp = L.flip ? a.p32b : a.p32a;
+        float* pc = L.flip ? a.p32a : a.p32b;
+        const float* rOld = L.rflip ? a.r32b : a.r32;
+        float* rNew = L.rflip ? a.r32 : a.r32b;
+        float pqHi = 0.f, pqLo = 0.f;
+        product32<false, 6>(ring, a, rb, re, reinterpret_cast<float*>(stage),
+                            [&](int c) { return fmaf(betaf, pp[c], w[c]); },
+                            [&](int row, float acc, float pi) {
+                                pc[row] = pi;
+                                a.q32[row] = acc;
+                                df_acc(pqHi, pqLo, pi, acc);
+                            });
+        const double pq = block_sum_df(pqHi, pqLo, smem);
+        if (threadIdx.x == 0) a.partials[t.rank] = pq;
+        if (!t.barrier(where++)) return false;
+        const double pqs = grid_sum(a.partials, G, smem);
+        if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
+        const float alphaf = (float)block_scalar(smem, [&] { return L.rz / pqs; });
+        float rrHi = 0.f, rrLo = 0.f;
+        DotAcc<float> rzn;
+        // colours other than 1: d += alpha p, r -= alpha q; colour 0 also y0 = r / L_00
+        for (int c = 0; c < C; ++c) {
+            if (c == 1) continue;
+            int r0, r1;
+            team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
+            for (int i0 = r0 + (int)threadIdx.x; i0 < r1; i0 += kRowsLean * bs) {
+                float pi[kRowsLean], qi[kRowsLean], di[kRowsLean], ri[kRowsLean], vi[kRowsLean];
+#pragma unroll
+                for (int u = 0; u < kRowsLean; ++u) {
+                    const int i = i0 + u * bs;
+                    if (i < r1) {
+                        pi[u] = pc[i];
+                        qi[u] = a.q32[i];
+                        di[u] = a.d32[i];
+                        ri[u] = rOld[i];
+                        vi[u] = c == 0 ? dinv[i] : 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kRowsLean; ++u) {
+                    const int i = i0 + u * bs;
+                    if (i < r1) {
+                        a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                        const float rn = fmaf(-alphaf, qi[u], ri[u]);
+                        rNew[i] = rn;
+                        df_acc(rrHi, rrLo, rn, rn);
+                        if (c == 0) w[i] = rn * vi[u];
+                    }
+                }
+            }
+        }
+        // colour 1: its d and r in the pre step, y1 = (r1 - sum L_1j y0_j) / L_11 (and z1 = y1 / L_11 when it is the
+        // last colour)
+        {
+            int r0, r1;
+            team_block(F.colourRow[1], F.colourRow[2], t, r0, r1);
+            const bool last = C == 2;
+            sell_rows<float, float, false, 1, 4>(
+                F.loStart, F.loCol, F.loVal32, r0, r1,
+                [&](int j) { return fmaf(-alphaf, a.q32[j], rOld[j]) * dinv[j]; },
+                [&](int i) {
+                    const float rn = fmaf(-alphaf, a.q32[i], rOld[i]);
+                    a.d32[i] = fmaf(alphaf, pc[i], a.d32[i]);
+                    rNew[i] = rn;
+                    df_acc(rrHi, rrLo, rn, rn);
+                    return SweepRow<float>{rn, dinv[i], 0.0f};
+                },
+                [&](int i, float acc, const SweepRow<float>& q) {
+                    float y = (q.src - acc) * q.d;
+                    if (last) {   // backward step of the last colour: z_i = y_i / L_ii
+                        y *= q.d;
+                        rzn.add(q.src, y);
+                    }
+                    w[i] = y;
+                });
+        }
+        const double rrn = block_sum_df(rrHi, rrLo, smem);
+        if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
+        if (!t.barrier(where++)) return false;
+        const double rrs = grid_sum(a.partials + G, G, smem);
+        ++L.it;
+        L.flip ^= 1;
+        L.rflip ^= 1;
+        if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
+        if (rrs <= rrStop) break;   // time for a true residual
+        if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
+        double rzs = 0;
+        if (!precond_sweeps<float, float, true>(t, a, rNew, w, F.loVal32, F.upVal32, dinv, rzn, smem, where, rzs,
+                                                ring, 2))
             return false;
         if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
         L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
@@ -591,13 +709,16 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.it = G.it;
     L.itRef = G.itRef;
     L.flip = G.flip;
-    const bool ok = pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
+    L.rflip = G.rflip;
+    const bool ok = a.f.colours >= 2 ? pcg_mixed_inner_fused(t, a, stage, smem, ring, L, where)
+                                     : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
     if (t.rank == 0 && threadIdx.x == 0) {
         a.loop->rz = L.rz;
         a.loop->beta = L.beta;
         a.loop->it = L.it;
         a.loop->flip = L.flip;
+        a.loop->rflip = L.rflip;
         a.loop->innerBreakdown = L.innerBreakdown;
         a.loop->state = ok ? L.state : kLoopDone;
     }

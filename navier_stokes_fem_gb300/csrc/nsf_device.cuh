@@ -719,6 +719,10 @@ __device__ __forceinline__ void product32(SellRing* ring, const CgArgs& a, int r
     }
 }
 
+// entries per lane and chunk of the FP64 residual and right-hand-side passes: 4 in the narrow kernels (register
+// budget), 8 in the wide ones (P2 rows of 9 and 19 entries take 2 and 3 chunks instead of 3 and 5)
+template <bool Wide> constexpr int kResidU = Wide ? 8 : 4;
+
 static __device__ void write_info(const Team& t, const CgArgs& a, int it, int status, int outer, double rr, double bb) {
     if (t.rank == 0 && threadIdx.x == 0) {
         a.info->iterations = it;
@@ -735,7 +739,7 @@ static __device__ void write_info(const Team& t, const CgArgs& a, int it, int st
 template <bool Wide = false>
 static __device__ void build_rhs(const CgArgs& a, int rb, int re, double* stage) {
     if (!a.bRowptr) return;
-    matrix_product<double, double, false, 4, Wide>(a.bSellStart, a.bSellCol, a.bSellVal, a.bRowptr, a.bCol, a.bVal, rb, re,
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(a.bSellStart, a.bSellCol, a.bSellVal, a.bRowptr, a.bCol, a.bVal, rb, re,
                                           stage, [&](int c) { return a.bX[c]; },
                                           [&](int row, double acc, double) {
                                               double bi = a.lift ? acc - a.lift[row] : acc;
@@ -758,7 +762,7 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     // prologue: (b), x = x0, r0 = b - A x0, p0 = r0
     build_rhs<Wide>(a, rb, re, stage);
     double rrp = 0, bbp = 0;
-    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
                                           [&](int c) { return a.x0[c]; },
                                           [&](int row, double acc, double x0i) {
                                               const double bi = b[row];
@@ -886,7 +890,7 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
         double rrp = 0, bbp = 0, rip = 0;
         float* pp0 = pprev;
         const bool f0 = resetP;
-        matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
+        matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
                                               stage, [&](int c) { return xs[c]; },
                                   [&](int row, double acc, double) {
                                       const double bi = b[row];

@@ -174,7 +174,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
 
     double rrp = 0, bbp = 0;
     DotAcc<double> rz0;
-    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
                                           [&](int c) { return a.x0[c]; },
                               [&](int row, double acc, double x0i) {
                                   const double bi = b[row];
@@ -348,7 +348,7 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
     const bool resetP = L.resetP != 0;
     double rrp = 0, bbp = 0;
     DotAcc<float> rzp;
-    matrix_product<double, double, false, 4, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
                                                    stage, [&](int c) { return xs[c]; },
                                                    [&](int row, double acc, double) {
                                                        const double bi = b[row];

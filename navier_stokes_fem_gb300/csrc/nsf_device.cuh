@@ -958,12 +958,30 @@ static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, dou
             // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
             // p.q accumulates in double-float so that the FP64 pipe does no per-row work
             float pqHi = 0.f, pqLo = 0.f;
-            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                                               [&](int row, float acc, float pi) {
-                                                   pc[row] = pi;
-                                                   a.q32[row] = acc;
-                                                   df_acc(pqHi, pqLo, pi, acc);
-                                               });
+            if constexpr (Wide) {
+                // P2 rows (9 and 19 entries): p = r32 + beta p_prev is written first, so that the product gathers one
+                // vector instead of forming p per gathered entry from two (one more barrier, half the gathers)
+                for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
+#pragma unroll
+                    for (int u = 0; u < kRows; ++u) {
+                        const int i = i0 + u * bs;
+                        if (i < re) pc[i] = fmaf(betaf, pp[i], r32[i]);
+                    }
+                }
+                if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+                product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return pc[c]; },
+                                [&](int row, float acc, float pi) {
+                                    a.q32[row] = acc;
+                                    df_acc(pqHi, pqLo, pi, acc);
+                                });
+            } else {
+                product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+                                [&](int row, float acc, float pi) {
+                                    pc[row] = pi;
+                                    a.q32[row] = acc;
+                                    df_acc(pqHi, pqLo, pi, acc);
+                                });
+            }
             const double pq = block_sum_df(pqHi, pqLo, smem);
             if (threadIdx.x == 0) a.partials[t.rank] = pq;
             if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }

@@ -36,6 +36,7 @@ struct TcArgs {
     const float* resid;           // rows x N or null
     int* error;                   // raised on a barrier time-out
     long long timeoutNs;
+    int vec8;                     // set by tc_dense: stage the A tile 8 values (16 bytes) at a time
 };
 
 void tc_dense(const TcArgs& a, cudaStream_t s, int sms);

@@ -59,10 +59,56 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_dense_kernel(TcArgs g) {
     bool ok = true;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int r0 = tile * kTcM;
-        for (int e = tid; e < kTcM * K; e += kTcThreads) {
-            const int r = e / K, k = e - r * K;
-            const float v = r0 + r < g.rows ? seg_value(g, r0 + r, k) : 0.0f;
-            sA[tc::core_offset(r, k, K)] = __float2bfloat16_rn(v);
+        if (g.vec8) {
+            // 8 consecutive k of one row per item: two 16-byte loads from the row's source, one 16-byte store of
+            // 8 BF16 values (contiguous in the core-matrix layout); four items' loads in flight per thread
+            const int kg = K >> 3, items = kTcM * kg;
+            for (int e0 = tid; e0 < items; e0 += 4 * kTcThreads) {
+                float4 lo[4], hi[4];
+                int off[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * kTcThreads;
+                    lo[u] = hi[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    off[u] = -1;
+                    if (e < items) {
+                        const int r = e / kg, g8 = e - r * kg;
+                        int k = g8 << 3, sgi = 0;
+                        while (sgi + 1 < g.nseg && k >= g.seg[sgi].width) {
+                            k -= g.seg[sgi].width;
+                            ++sgi;
+                        }
+                        const TcSeg& sg = g.seg[sgi];
+                        const int row = r0 + r;
+                        const int src = row < g.rows ? (sg.index ? sg.index[row] : row) : -1;
+                        if (src >= 0) {
+                            const float4* q = reinterpret_cast<const float4*>(sg.base + (size_t)src * sg.width + k);
+                            lo[u] = q[0];
+                            hi[u] = q[1];
+                        }
+                        off[u] = tc::core_offset(r, g8 << 3, K);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (off[u] < 0) continue;
+                    union {
+                        __nv_bfloat162 h[4];
+                        uint4 v;
+                    } pk;
+                    pk.h[0] = __floats2bfloat162_rn(lo[u].x, lo[u].y);
+                    pk.h[1] = __floats2bfloat162_rn(lo[u].z, lo[u].w);
+                    pk.h[2] = __floats2bfloat162_rn(hi[u].x, hi[u].y);
+                    pk.h[3] = __floats2bfloat162_rn(hi[u].z, hi[u].w);
+                    *reinterpret_cast<uint4*>(sA + off[u]) = pk.v;
+                }
+            }
+        } else {
+            for (int e = tid; e < kTcM * K; e += kTcThreads) {
+                const int r = e / K, k = e - r * K;
+                const float v = r0 + r < g.rows ? seg_value(g, r0 + r, k) : 0.0f;
+                sA[tc::core_offset(r, k, K)] = __float2bfloat16_rn(v);
+            }
         }
         tc::fence_proxy_async();   // generic-proxy stores -> visible to the tensor core (async proxy)
         tc::fence_before();
@@ -127,13 +173,18 @@ void tc_dense(const TcArgs& a, cudaStream_t s, int sms) {
     for (int i = 0; i < a.nseg; ++i) w += a.seg[i].width;
     if (w != a.K) throw bad_arg("segment widths must add up to K");
     const size_t smem = (size_t)kTcM * a.K * 2 + (size_t)a.N * a.K * 2;
+    // 16-byte staging when every segment's rows are 16-byte aligned groups of 8 values
+    TcArgs b = a;
+    b.vec8 = 1;
+    for (int i = 0; i < a.nseg; ++i)
+        if (a.seg[i].width % 8 || reinterpret_cast<uintptr_t>(a.seg[i].base) % 16) b.vec8 = 0;
     static bool attr = false;
     if (!attr) {
         NSF_CUDA(cudaFuncSetAttribute(tc_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
         attr = true;
     }
     const int tiles = (a.rows + kTcM - 1) / kTcM;
-    tc_dense_kernel<<<std::min(tiles, std::max(sms, 1)), kTcThreads, smem, s>>>(a);
+    tc_dense_kernel<<<std::min(tiles, std::max(sms, 1)), kTcThreads, smem, s>>>(b);
     NSF_CUDA(cudaGetLastError());
     count_launch();
 }

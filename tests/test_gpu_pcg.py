@@ -147,3 +147,62 @@ def test_steps_with_preconditioned_pressure_match_oracle(solver):
     # the pressure solves need fewer iterations; the mixed form restarts its FP32 recurrence at every FP64 refresh
     # (robust on the ill-conditioned large systems), which costs it some of the gain on small ones
     assert it[:, 2].sum() < (0.7 if solver == "pcg_fp64" else 0.9) * it_plain[:, 2].sum()
+
+
+def _perturbed_cavity(n, seed=11, amp=0.3):
+    """A cavity whose interior vertices are moved randomly (no edge axis-aligned): its pressure matrix has no
+    exact zeros off the diagonal, three colours and at most 7 entries per row (the narrow, split solver)."""
+    m = M.cavity(n)
+    rng = np.random.default_rng(seed)
+    h = 1.0 / n
+    xy = m.nodes.astype(np.float64)
+    P = m.n_pressure
+    interior = (xy[:P, 0] > 0) & (xy[:P, 0] < 1) & (xy[:P, 1] > 0) & (xy[:P, 1] < 1)
+    xy[:P][interior] += rng.uniform(-amp * h, amp * h, size=(int(interior.sum()), 2))
+    for e in m.elements:
+        for k, (a, b) in zip((3, 4, 5), ((1, 2), (0, 2), (0, 1))):
+            xy[e[k]] = 0.5 * (xy[e[a]] + xy[e[b]])
+    m.nodes = xy.astype(np.float32)
+    return m
+
+
+def _golden_small():
+    import os
+    from tests._meshes import golden_mesh
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_kdtree_lookup.npz"))
+    return golden_mesh(g, "mesh_small")
+
+
+@pytest.mark.parametrize("which", ["perturbed64", "mesh_small"])
+def test_multicolour_pcg_on_unstructured_pressure(which):
+    """Three colours on a narrow system (the split mixed solver, colours >= 2 after the fused first colour) and
+    five on the reference's own unstructured mesh (the one-launch solver): FP64 PCG against the oracle's PCG with
+    the same factor, and mixed PCG to the FP64 residual."""
+    m = _perturbed_cavity(64) if which == "perturbed64" else _golden_small()
+    o = oracle.Oracle(m, 0.01, 0.01)
+    name = "pressure_stiffness"
+    rp, col, val, shape = o.matrix(name)
+    d = nsf.GPUSimulationDevice(0)
+    d.upload_matrix(name, rp.astype(np.int32), col, val, shape)
+    colours = int(d.precond_pattern(name)[2].max()) + 1
+    assert colours == (3 if which == "perturbed64" else 5)
+    d.precond_ic0(name)
+    n = shape[0]
+    rng = np.random.default_rng(12)
+    b = rng.standard_normal(n)
+    x0 = 0.1 * rng.standard_normal(n)
+    x, it, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_fp64")
+    F = oracle.McFactor(o.scipy_matrix(name))
+    F.ic0()
+    xr, itr, _, st = F.pcg(b, x0, tol=TOL)
+    assert st == 0
+    assert abs(it - itr) <= max(2, itr // 50)
+    assert _relres(o, name, x, b) < 1.5 * TOL
+    xm, itm, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_mixed")
+    assert _relres(o, name, xm, b) < 1.5 * TOL           # the contract: the FP64 residual
+    xt, st, _, _ = o.cg(name, b, x0, max_iter=20 * n, tol=1e-13)
+    assert st == 0 and rel(xm, xt) < 1e-5 and rel(x, xt) < 1e-5
+    _, it_plain, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="fp64")
+    assert itm < it_plain
+    d.close()
+    o.close()

@@ -97,8 +97,18 @@ __device__ __noinline__ int step_cg_fp64(Team& t, const CgArgs& a, double* stage
 __device__ __noinline__ int step_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem) {
     return team_cg_mixed(t, a, stage, smem);
 }
+// the velocity systems (P2 rows of 9 and 19 entries): the pipelined wide product
+__device__ __noinline__ int step_cg_fp64_wide(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_cg_fp64<true>(t, a, stage, smem);
+}
+__device__ __noinline__ int step_cg_mixed_wide(Team& t, const CgArgs& a, double* stage, double* smem) {
+    return team_cg_mixed<true>(t, a, stage, smem);
+}
 __device__ __forceinline__ int run_cg(Team& t, const CgArgs& a, int mode, double* stage, double* smem) {
     return mode == NSF_SOLVER_MIXED ? step_cg_mixed(t, a, stage, smem) : step_cg_fp64(t, a, stage, smem);
+}
+__device__ __forceinline__ int run_cg_wide(Team& t, const CgArgs& a, int mode, double* stage, double* smem) {
+    return mode == NSF_SOLVER_MIXED ? step_cg_mixed_wide(t, a, stage, smem) : step_cg_fp64_wide(t, a, stage, smem);
 }
 
 __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance* __restrict__ insts,
@@ -149,6 +159,9 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.bRowptr = I.M.rowptr;
         a.bCol = I.M.col;
         a.bVal = I.M.val;
+        a.bSellStart = I.M.sellStart;
+        a.bSellCol = I.M.sellCol;
+        a.bSellVal = I.M.sellVal;
         a.bX = I.tmp + (size_t)ch * Nv;
         a.lift = ch ? I.liftV1 : I.liftV0;
         a.bcMask = I.bcV;
@@ -158,7 +171,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.tmp + (size_t)ch * Nv;
         a.x = I.uv + (size_t)ch * Nv;
         a.info = info + ch;
-        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg_wide(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // pressure: Kp p = -(1/dt) Div u - lift, pinned nodes -> g; x0 = p
     {
@@ -190,7 +203,7 @@ __global__ void __launch_bounds__(kCgThreads, 2) step_kernel(const StepInstance*
         a.x0 = I.uv + (size_t)ch * Nv;
         a.x = I.tmp + (size_t)ch * Nv;
         a.info = info + 3 + ch;
-        if (run_cg(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
+        if (run_cg_wide(t, a, sp.mode, stage, smem) == NSF_ERR_BARRIER_TIMEOUT) return;
     }
     // u <- du + u with the Dirichlet values re-imposed (include/assembly.h:686-707), in place
     team_rows(Nv, t, rb, re);

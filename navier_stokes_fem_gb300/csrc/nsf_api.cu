@@ -258,6 +258,8 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     const bool wide = S.maxWidth > kSellChunk;
     if (mode == NSF_SOLVER_PCG_MIXED && !wide)
         pcg_mixed_split_launch(ws, a, h->stream);
+    else if (mode == NSF_SOLVER_MIXED && wide)
+        cg_mixed_split_launch(ws, a, h->stream);
     else
         cg_launch(ws, a, mode, wide, h->stream);
     if (h->profile) {

@@ -85,6 +85,66 @@ __global__ void __launch_bounds__(kCgThreads, 4) pcg_mixed_inner_kernel(CgArgs a
     team_pcg_mixed_inner(t, a, stage, smem, nullptr);
 }
 
+// The split plain mixed CG for wide (P2) systems: refresh launches (fold, FP64 true residual, tests) at 2 CTAs per
+// SM and FP32 iteration launches at 4.
+static __device__ void team_cg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem) {
+    int where = 10;
+    PcgLoop L;
+    if (a.loopInit) {
+        cg_mixed_start<true>(t, a, stage);
+        cg_loop_init(L, a);
+    } else {
+        L = *a.loop;
+    }
+    if (!cg_mixed_refresh<true>(t, a, stage, smem, L, where)) {
+        write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, L.refresh, L.rr64, L.bb);
+        L.state = kLoopDone;
+    } else if (L.state == kLoopDone) {
+        cg_mixed_finish<true>(t, a, stage, smem, L);
+    }
+    pcg_loop_store(t, a, L);
+}
+
+static __device__ void team_cg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem) {
+    int where = 400;
+    // the fields the FP32 iterations read or write (the rest of the state stays in memory)
+    const PcgLoop& G = *a.loop;
+    PcgLoop L;
+    L.beta = G.beta;
+    L.flip = G.flip;
+    L.rr = G.rr;
+    L.rrPrev = G.rrPrev;
+    L.rrRef = G.rrRef;
+    L.target = G.target;
+    L.cycleTol2 = G.cycleTol2;
+    L.it = G.it;
+    L.itRef = G.itRef;
+    const bool ok = cg_mixed_inner<true, true>(t, a, stage, smem, nullptr, L, where);
+    if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
+    if (t.rank == 0 && threadIdx.x == 0) {
+        a.loop->beta = L.beta;
+        a.loop->flip = L.flip;
+        a.loop->rr = L.rr;
+        a.loop->rrPrev = L.rrPrev;
+        a.loop->it = L.it;
+        a.loop->lastCycle = L.lastCycle;
+        a.loop->innerBreakdown = L.innerBreakdown;
+        a.loop->state = ok ? L.state : kLoopDone;
+    }
+}
+
+__global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_refresh_kernel(CgArgs a) {
+    NSF_KERNEL_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_cg_mixed_refresh(t, a, stage, smem);
+}
+
+__global__ void __launch_bounds__(kCgThreads, 4) cg_mixed_inner_kernel(CgArgs a) {
+    NSF_KERNEL_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_cg_mixed_inner(t, a, stage, smem);
+}
+
 // ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
@@ -122,11 +182,14 @@ static int cg_occupancy() {
     return std::min(occ, o);
 }
 
-// CTAs per SM of the split PCG's inner-iteration kernel (at most 4)
+// CTAs per SM of the split solvers' inner-iteration kernels (at most 4)
 static int inner_occupancy() {
-    int o = 0;
+    int o = 0, c = 0, r = 0;
     NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, (const void*)pcg_mixed_inner_kernel, kCgThreads, 0));
-    return std::min(4, o);
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, (const void*)cg_mixed_inner_kernel, kCgThreads, 0));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, (const void*)cg_mixed_refresh_kernel, kCgThreads, 0));
+    if (r < 2) throw Error{NSF_ERR_CUDA, "mixed refresh kernel cannot be resident at 2 CTAs per SM"};
+    return std::min(4, std::min(o, c));
 }
 
 void cg_configure(CgWorkspace& ws, int device) {
@@ -152,6 +215,35 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStr
     const CgKernel& k = cg_kernel(mode, wide);
     NSF_CUDA(cudaLaunchCooperativeKernel(k.fn, dim3(ws.grid), dim3(ws.block), params, k.dsm, s));
     count_launch();
+}
+
+// A split solve: the refresh launch, then inner-iteration and refresh launches while the state says so.
+static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t refreshDsm, const void* inner,
+                         cudaStream_t s) {
+    a.loop = ws.loop.get();
+    auto launch = [&](const void* fn, int grid, size_t dsm) {
+        NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
+        void* params[] = {&a};
+        NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(ws.block), params, dsm, s));
+        count_launch();
+    };
+    a.loopInit = 1;
+    launch(refresh, ws.grid, refreshDsm);
+    a.loopInit = 0;
+    // every refresh counts one outer cycle and the solve ends at maxOuter of them, so this loop is bounded
+    for (int cycle = 0; cycle <= a.maxOuter + 1; ++cycle) {
+        int state = 0;
+        NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        if (state != kLoopInner) return;
+        launch(inner, ws.gridInner, 0);
+        launch(refresh, ws.grid, refreshDsm);
+    }
+    throw Error{NSF_ERR_CUDA, "mixed-precision solve did not finish within its refresh budget"};
+}
+
+void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
+    split_launch(ws, a, (const void*)cg_mixed_refresh_kernel, 0, (const void*)cg_mixed_inner_kernel, s);
 }
 
 void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {

@@ -854,197 +854,248 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 // Mixed precision: FP32 CG with FP64 reliable updates.
 // The search direction p, the product q = A32 p, the residual r32 and the accumulated correction d32 are FP32;
 // the dot products and alpha/beta are FP64.  x, b and the true residual stay FP64: whenever the FP32 residual
-// has fallen by the factor delta (innerTol) since the last true residual, d32 is folded into x, the residual
-// b - A64 x is recomputed with the FP64 matrix and replaces r32, and the recurrence continues with the same
-// search direction.  This is iterative refinement that keeps the Krylov recurrence instead of restarting it, so
-// the FP32 matrix error costs little in iteration count even on the ill-conditioned pressure system.
-// The FP32 product gathers p_j = r32_j + beta p_prev_j on the fly (FP32 arithmetic is cheap on GB300), which
-// saves the third barrier of the FP64 kernel.
+// has fallen by the cycle's tolerance since the last true residual, d32 is folded into x, the residual b - A64 x
+// is recomputed with the FP64 matrix and replaces r32, and the recurrence continues with the same search
+// direction.  This is iterative refinement that keeps the Krylov recurrence instead of restarting it, so the FP32
+// matrix error costs little in iteration count even on the ill-conditioned pressure system.
+// Narrow systems form p_j = r32_j + beta p_prev_j per gathered entry (saving a barrier); wide (P2) systems write p
+// first and gather it once.  The solve is two steps over a PcgLoop state - a refresh (fold, true residual, tests)
+// and the FP32 iterations up to the next refresh - run in one launch (team_cg_mixed) or, for wide systems, as
+// separate launches (the inner one at 4 CTAs per SM).
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void cg_loop_init(PcgLoop& L, const CgArgs& a) {
+    L.rr64 = L.bb = L.target = L.rz = L.beta = 0.0;
+    L.rrBest = L.rrCycle = INFINITY;
+    L.rrRef = 0.0;
+    L.rr = 0.0;
+    L.rrPrev = 1.0;
+    L.cycleTol2 = a.innerTol2;
+    L.lastCycle = 0;
+    L.it = L.refresh = L.stalls = L.itRef = 0;
+    L.first = 1;
+    L.resetP = 1;
+    L.flip = 0;
+    L.innerBreakdown = 0;
+    L.rflip = 0;
+    L.state = kLoopRefresh;
+    L.status = NSF_ERR_NOT_CONVERGED;
+}
+
+// The start of the solve (first step only): the fused right-hand side and x = x0 (own rows; the first true
+// residual gathers x0, not x, so no barrier is needed).
 template <bool Wide = false>
-static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring = nullptr) {
-    float* stage32 = reinterpret_cast<float*>(stage);
-    const int G = t.size;
+static __device__ void cg_mixed_start(Team& t, const CgArgs& a, double* stage) {
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    build_rhs<Wide>(a, rb, re, stage);
+    if (a.x != a.x0)
+        for (int i = rb + (int)threadIdx.x; i < re; i += blockDim.x) a.x[i] = a.x0[i];
+}
+
+template <bool Wide = false>
+static __device__ bool cg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem, PcgLoop& L,
+                                        int& where) {
+    const int G = t.size, bs = blockDim.x;
     int rb, re;
     team_rows(a.n, t, rb, re);
     const double* b = a.bRowptr ? a.bOut : a.b;
-    const int bs = blockDim.x;
-
-    build_rhs<Wide>(a, rb, re, stage);
-    // x = x0 (own rows); the first true residual gathers x0, not x, so no barrier is needed here
-    if (a.x != a.x0)
-        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] = a.x0[i];
-
-    int it = 0, refresh = 0, status = NSF_ERR_NOT_CONVERGED, where = 10, stalls = 0;
-    double rr64 = 0, bb = 0, target = 0, rr = 0, rrPrev = 1.0, beta = 0.0, rrBest = INFINITY;
-    double cycleTol2 = a.innerTol2;   // FP32 residual reduction between true residuals (adapted per cycle)
-    int lastCycle = 0;                // FP32 iterations of the cycle that just ended
-    float* pprev = a.p32a;
-    float* pcur = a.p32b;
-    bool first = true;       // the first true residual gathers x0 and sets the target
-    bool resetP = true;      // (re)start the recurrence: p_prev := r32, beta := 0
-    while (true) {
-        // true residual: r = b - A64 x; r32 = (float) r; d32 = 0
-        const double* xs = first ? a.x0 : a.x;
-        double rrp = 0, bbp = 0, rip = 0;
-        float* pp0 = pprev;
-        const bool f0 = resetP;
-        matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re,
-                                              stage, [&](int c) { return xs[c]; },
-                                  [&](int row, double acc, double) {
-                                      const double bi = b[row];
-                                      const double ri = bi - acc;
-                                      const float r32 = (float)ri;
-                                      a.r32[row] = r32;
-                                      if (f0) pp0[row] = r32;
-                                      a.d32[row] = 0.0f;
-                                      rrp = fma(ri, ri, rrp);
-                                      bbp = fma(bi, bi, bbp);
-                                      rip = fma((double)r32, (double)r32, rip);
-                                  });
-        rrp = block_sum(rrp, smem);
-        bbp = block_sum(bbp, smem);
-        rip = block_sum(rip, smem);
-        if (threadIdx.x == 0) {
-            a.partials[2 * G + t.rank] = rrp;
-            a.partials[3 * G + t.rank] = bbp;
-            a.partials[4 * G + t.rank] = rip;
-        }
-        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-        rr64 = grid_sum(a.partials + 2 * G, G, smem);
-        if (first) {
-            bb = grid_sum(a.partials + 3 * G, G, smem);
-            target = bb > 0 ? a.tol2 * bb : a.tol2 * rr64;
-        }
-        const double rrTrue = grid_sum(a.partials + 4 * G, G, smem);
-        if (!(rr64 == rr64) || isinf(rr64)) { status = NSF_ERR_BREAKDOWN; break; }
-        if (rr64 <= target) { status = NSF_OK; break; }
-        if (it >= a.maxIt || refresh >= a.maxOuter) break;
-        // stagnation guard: a refresh cycle normally cuts the true residual norm by ~1/delta.  Three consecutive
-        // cycles that gain less than 10% mean the FP32 recurrence cannot resolve this system, and the solve
-        // finishes in FP64 below.  (CG residuals are not monotone, so single weak cycles are tolerated.)
-        if (refresh > 0 && rr64 > 0.81 * rrBest) {
-            if (++stalls >= 3) break;
-        } else {
-            stalls = 0;
-        }
-        rrBest = fmin(rrBest, rr64);
-        // Short cycles (a well-conditioned system: the velocity systems refresh every ~3 iterations at innerTol
-        // 0.1) lengthen while the FP32 recurrence stays accurate: when the true residual matches the recursive
-        // one within 2x in norm, the next cycle may reduce 10x further (to 1e-4 at most); when they differ by more
-        // than 4x the interval returns towards innerTol.  Long cycles (the ill-conditioned pressure system, whose
-        // refreshes cost nothing next to ~1000 FP32 iterations) keep innerTol.
-        if (refresh > 0 && rr > 0.0) {
-            const double drift = rr64 / rr;
-            if (drift < 4.0 && lastCycle < 32) cycleTol2 = fmax(cycleTol2 * 1e-2, 1e-8);
-            else if (drift > 16.0) cycleTol2 = fmin(cycleTol2 * 1e2, a.innerTol2);
-        }
-        // continue the recurrence from the refreshed residual: beta' = |r_new|^2 / |r_prev|^2
-        beta = resetP ? 0.0 : rrTrue / rrPrev;
-        resetP = false;
-        rr = rrTrue;
-        const double rrRef = rrTrue;
-        const int itRef = it;
-        ++refresh;
-        first = false;
-
-        bool innerBreakdown = false;
-        while (it < a.maxIt) {
-            const float betaf = (float)beta;
-            const float* pp = pprev;
-            float* pc = pcur;
-            const float* r32 = a.r32;
-            // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
-            // p.q accumulates in double-float so that the FP64 pipe does no per-row work
-            float pqHi = 0.f, pqLo = 0.f;
-            if constexpr (Wide) {
-                // P2 rows (9 and 19 entries): p = r32 + beta p_prev is written first, so that the product gathers one
-                // vector instead of forming p per gathered entry from two (one more barrier, half the gathers)
-                for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
-#pragma unroll
-                    for (int u = 0; u < kRows; ++u) {
-                        const int i = i0 + u * bs;
-                        if (i < re) pc[i] = fmaf(betaf, pp[i], r32[i]);
-                    }
-                }
-                if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-                product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return pc[c]; },
-                                [&](int row, float acc, float pi) {
-                                    a.q32[row] = acc;
-                                    df_acc(pqHi, pqLo, pi, acc);
-                                });
-            } else {
-                product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                                [&](int row, float acc, float pi) {
-                                    pc[row] = pi;
-                                    a.q32[row] = acc;
-                                    df_acc(pqHi, pqLo, pi, acc);
-                                });
-            }
-            const double pq = block_sum_df(pqHi, pqLo, smem);
-            if (threadIdx.x == 0) a.partials[t.rank] = pq;
-            if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-            const double pqs = grid_sum(a.partials, G, smem);
-            if (!(pqs > 0.0) || isinf(pqs)) { innerBreakdown = true; break; }
-            const float alphaf = (float)block_scalar(smem, [&] { return rr / pqs; });
-            float rrHi = 0.f, rrLo = 0.f;
-            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += kRows * bs) {
-                float pi[kRows], qi[kRows], di[kRows], ri[kRows];
-#pragma unroll
-                for (int u = 0; u < kRows; ++u) {
-                    const int i = i0 + u * bs;
-                    if (i < re) { pi[u] = pc[i]; qi[u] = a.q32[i]; di[u] = a.d32[i]; ri[u] = a.r32[i]; }
-                }
-#pragma unroll
-                for (int u = 0; u < kRows; ++u) {
-                    const int i = i0 + u * bs;
-                    if (i < re) {
-                        a.d32[i] = fmaf(alphaf, pi[u], di[u]);
-                        const float rn = fmaf(-alphaf, qi[u], ri[u]);
-                        a.r32[i] = rn;
-                        df_acc(rrHi, rrLo, rn, rn);
-                    }
-                }
-            }
-            const double rrn = block_sum_df(rrHi, rrLo, smem);
-            if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
-            if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-            const double rrs = grid_sum(a.partials + G, G, smem);
-            ++it;
-            { float* t = pprev; pprev = pcur; pcur = t; }
-            if (!(rrs == rrs) || isinf(rrs)) { innerBreakdown = true; break; }
-            beta = block_scalar(smem, [&] { return rrs / rr; });
-            rrPrev = rr;
-            rr = rrs;
-            if (rr <= cycleTol2 * rrRef || rr <= target) break;   // time for a true residual
-            if (it - itRef >= kMaxInnerBetweenRefresh) break;        // bound the work between true residuals
-        }
-        lastCycle = it - itRef;
-        // fold the correction into x (FP64); the next true residual gathers x across blocks
+    if (!L.first) {   // fold the correction into x (FP64); the true residual gathers x across blocks
         for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
-        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, refresh, rr64, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-        if (innerBreakdown) resetP = true;   // restart the recurrence from the true residual
+        if (!t.barrier(where++)) return false;
+        if (L.innerBreakdown) L.resetP = 1;   // restart the recurrence from the true residual
     }
-    if (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
-        // fall back to the plain FP64 method from the current iterate (x is complete after the last barrier);
-        // the right-hand side is final too, so the fused build is not repeated
+    // true residual: r = b - A64 x; r32 = (float) r; d32 = 0
+    const double* xs = L.first ? a.x0 : a.x;
+    double rrp = 0, bbp = 0, rip = 0;
+    float* pp0 = L.flip ? a.p32b : a.p32a;
+    const bool f0 = L.resetP != 0;
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(
+        a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xs[c]; },
+        [&](int row, double acc, double) {
+            const double bi = b[row];
+            const double ri = bi - acc;
+            const float r32 = (float)ri;
+            a.r32[row] = r32;
+            if (f0) pp0[row] = r32;
+            a.d32[row] = 0.0f;
+            rrp = fma(ri, ri, rrp);
+            bbp = fma(bi, bi, bbp);
+            rip = fma((double)r32, (double)r32, rip);
+        });
+    rrp = block_sum(rrp, smem);
+    bbp = block_sum(bbp, smem);
+    rip = block_sum(rip, smem);
+    if (threadIdx.x == 0) {
+        a.partials[2 * G + t.rank] = rrp;
+        a.partials[3 * G + t.rank] = bbp;
+        a.partials[4 * G + t.rank] = rip;
+    }
+    if (!t.barrier(where++)) return false;
+    L.rr64 = grid_sum(a.partials + 2 * G, G, smem);
+    if (L.first) {
+        L.bb = grid_sum(a.partials + 3 * G, G, smem);
+        L.target = L.bb > 0 ? a.tol2 * L.bb : a.tol2 * L.rr64;
+    }
+    const double rrTrue = grid_sum(a.partials + 4 * G, G, smem);
+    L.state = kLoopDone;
+    if (!(L.rr64 == L.rr64) || isinf(L.rr64)) { L.status = NSF_ERR_BREAKDOWN; return true; }
+    if (L.rr64 <= L.target) { L.status = NSF_OK; return true; }
+    if (L.it >= a.maxIt || L.refresh >= a.maxOuter) return true;
+    // stagnation guard: a refresh cycle normally cuts the true residual norm by ~1/delta.  Three consecutive
+    // cycles that gain less than 10% mean the FP32 recurrence cannot resolve this system, and the solve
+    // finishes in FP64.  (CG residuals are not monotone, so single weak cycles are tolerated.)
+    if (L.refresh > 0 && L.rr64 > 0.81 * L.rrBest) {
+        if (++L.stalls >= 3) return true;
+    } else {
+        L.stalls = 0;
+    }
+    L.rrBest = fmin(L.rrBest, L.rr64);
+    // Short refresh cycles (a well-conditioned system: the velocity systems refresh every ~3 iterations at
+    // innerTol 0.1) lengthen while the FP32 recurrence stays accurate: when the true residual matches the
+    // recursive one within 2x in norm, the next cycle may reduce 10x further (to 1e-4 at most); when they differ by
+    // more than 4x the interval returns towards innerTol.  Long cycles (the ill-conditioned pressure system, whose
+    // refreshes cost nothing next to ~1000 FP32 iterations) keep innerTol.
+    if (L.refresh > 0 && L.rr > 0.0) {
+        const double drift = L.rr64 / L.rr;
+        if (drift < 4.0 && L.lastCycle < 32) L.cycleTol2 = fmax(L.cycleTol2 * 1e-2, 1e-8);
+        else if (drift > 16.0) L.cycleTol2 = fmin(L.cycleTol2 * 1e2, a.innerTol2);
+    }
+    // continue the recurrence from the refreshed residual: beta' = |r_new|^2 / |r_prev|^2
+    L.beta = L.resetP ? 0.0 : block_scalar(smem, [&] { return rrTrue / L.rrPrev; });
+    L.resetP = 0;
+    L.rr = rrTrue;
+    L.rrRef = rrTrue;
+    L.itRef = L.it;
+    ++L.refresh;
+    L.first = 0;
+    L.state = kLoopInner;
+    return true;
+}
+
+template <bool Wide = false, bool Lean = false>
+static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
+                                      PcgLoop& L, int& where) {
+    float* stage32 = reinterpret_cast<float*>(stage);
+    const int G = t.size, bs = blockDim.x;
+    constexpr int R = Lean ? kRowsLean : kRows;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    L.innerBreakdown = 0;
+    while (L.it < a.maxIt) {
+        const float betaf = (float)L.beta;
+        const float* pp = L.flip ? a.p32b : a.p32a;
+        float* pc = L.flip ? a.p32a : a.p32b;
+        const float* r32 = a.r32;
+        // q = A32 p in difference form: sum_j a_ij (p_j - p_i) + rowsum_i p_i (exact row sums, see warp_spmv);
+        // p.q accumulates in double-float so that the FP64 pipe does no per-row work
+        float pqHi = 0.f, pqLo = 0.f;
+        if constexpr (Wide) {
+            // P2 rows (9 and 19 entries): p = r32 + beta p_prev is written first, so that the product gathers one
+            // vector instead of forming p per gathered entry from two (one more barrier, half the gathers)
+            for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += R * bs) {
+#pragma unroll
+                for (int u = 0; u < R; ++u) {
+                    const int i = i0 + u * bs;
+                    if (i < re) pc[i] = fmaf(betaf, pp[i], r32[i]);
+                }
+            }
+            if (!t.barrier(where++)) return false;
+            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return pc[c]; },
+                            [&](int row, float acc, float pi) {
+                                a.q32[row] = acc;
+                                df_acc(pqHi, pqLo, pi, acc);
+                            });
+        } else {
+            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
+                            [&](int row, float acc, float pi) {
+                                pc[row] = pi;
+                                a.q32[row] = acc;
+                                df_acc(pqHi, pqLo, pi, acc);
+                            });
+        }
+        const double pq = block_sum_df(pqHi, pqLo, smem);
+        if (threadIdx.x == 0) a.partials[t.rank] = pq;
+        if (!t.barrier(where++)) return false;
+        const double pqs = grid_sum(a.partials, G, smem);
+        if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
+        const float alphaf = (float)block_scalar(smem, [&] { return L.rr / pqs; });
+        float rrHi = 0.f, rrLo = 0.f;
+        for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += R * bs) {
+            float pi[R], qi[R], di[R], ri[R];
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) { pi[u] = pc[i]; qi[u] = a.q32[i]; di[u] = a.d32[i]; ri[u] = a.r32[i]; }
+            }
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+                const int i = i0 + u * bs;
+                if (i < re) {
+                    a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                    const float rn = fmaf(-alphaf, qi[u], ri[u]);
+                    a.r32[i] = rn;
+                    df_acc(rrHi, rrLo, rn, rn);
+                }
+            }
+        }
+        const double rrn = block_sum_df(rrHi, rrLo, smem);
+        if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
+        if (!t.barrier(where++)) return false;
+        const double rrs = grid_sum(a.partials + G, G, smem);
+        ++L.it;
+        L.flip ^= 1;
+        if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
+        L.beta = block_scalar(smem, [&] { return rrs / L.rr; });
+        L.rrPrev = L.rr;
+        L.rr = rrs;
+        if (L.rr <= L.cycleTol2 * L.rrRef || L.rr <= L.target) break;   // time for a true residual
+        if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;           // bound the work between true residuals
+    }
+    L.lastCycle = L.it - L.itRef;
+    L.state = kLoopRefresh;
+    return true;
+}
+
+// The end of a plain mixed solve (state kLoopDone): when it stalled short of the tolerance with budget left, the
+// plain FP64 method from the current iterate (x is complete; the right-hand side is final, so the fused build is
+// not repeated); then the solve's info.
+template <bool Wide = false>
+static __device__ int cg_mixed_finish(Team& t, const CgArgs& a, double* stage, double* smem, const PcgLoop& L) {
+    if (L.status == NSF_ERR_NOT_CONVERGED && L.it < a.maxIt) {
         CgArgs f = a;
         f.bRowptr = nullptr;
-        f.b = b;
+        f.b = a.bRowptr ? a.bOut : a.b;
         f.x0 = a.x;
-        f.maxIt = a.maxIt - it;
+        f.maxIt = a.maxIt - L.it;
         const int fst = team_cg_fp64<Wide>(t, f, stage, smem);
         if (fst == NSF_ERR_BARRIER_TIMEOUT) return fst;
         if (t.rank == 0 && threadIdx.x == 0) {
-            a.info->iterations += it;
-            a.info->outer = refresh;
+            a.info->iterations += L.it;
+            a.info->outer = L.refresh;
             a.info->fallback = 1;   // finished in FP64
         }
         return fst;
     }
-    write_info(t, a, it, status, refresh, rr64, bb);
-    return status;
+    write_info(t, a, L.it, L.status, L.refresh, L.rr64, L.bb);
+    return L.status;
+}
+
+template <bool Wide = false>
+static __device__ int team_cg_mixed(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring = nullptr) {
+    cg_mixed_start<Wide>(t, a, stage);
+    PcgLoop L;
+    cg_loop_init(L, a);
+    int where = 10;
+    while (true) {
+        if (!cg_mixed_refresh<Wide>(t, a, stage, smem, L, where) ||
+            (L.state == kLoopInner && !cg_mixed_inner<Wide>(t, a, stage, smem, ring, L, where))) {
+            write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, L.refresh, L.rr64, L.bb);
+            return NSF_ERR_BARRIER_TIMEOUT;
+        }
+        if (L.state == kLoopDone) break;
+    }
+    return cg_mixed_finish<Wide>(t, a, stage, smem, L);
 }
 
 }  // namespace nsf

@@ -171,6 +171,8 @@ struct GridSync {
 // the solve.  The split form keeps it in device memory between its refresh and inner-iteration kernels.
 struct PcgLoop {
     double rr64, bb, target, rz, beta, rrBest, rrCycle, rrRef;
+    double rr, rrPrev, cycleTol2;   // plain mixed CG: recursive r.r, its previous value, the cycle's tolerance
+    int lastCycle;
     int it, refresh, stalls, itRef;
     int first, resetP, flip, innerBreakdown;
     int rflip;               // which residual buffer is current (r32 or r32b; the fused inner iterations alternate)
@@ -251,6 +253,8 @@ void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, bool wide, cudaStream
 // The split mixed PCG (narrow matrices): refresh kernel, then inner-iteration and refresh kernels until the solve
 // is done; one small device-to-host read per refresh cycle.
 void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
+// The split plain mixed CG (wide systems): the same launch pattern.
+void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s);
 void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
 void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
                      const double* bcValue, double* y, cudaStream_t s);

@@ -350,9 +350,9 @@ def nonzeros(sim, slot):
 
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
-# 4,198,401 rows, whose vectors exceed L2): pcg_mixed_inner_kernel 18.85 GB over 40 iterations, cg_fp64_kernel
+# 4,198,401 rows, whose vectors exceed L2): pcg_mixed_inner_kernel 19.90 GB over 40 iterations, cg_fp64_kernel
 # 30.67 GB over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 112.2, "cg_fp64_kernel": 121.7}
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 118.5, "cg_fp64_kernel": 121.7}
 
 
 def roofline(sim, arm, args):

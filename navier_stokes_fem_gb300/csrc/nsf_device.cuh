@@ -519,6 +519,10 @@ constexpr size_t kRingBytes = kRingDataPerWarp * kWarps + (size_t)kRingDepth * k
 static_assert(kRingDataPerWarp * kWarps >= sizeof(double) * kWarps * 2 * kStage,
               "the ring kernels use the ring memory as the CSR product's staging area");
 
+// Waits on asynchronous copies never give up sooner than this, whatever the grid-barrier limit (even a zero
+// one, used to test the time-out path): a warp must not leave a stage while its copy may still land.
+constexpr long long kAsyncWaitFloorNs = 200000000LL;
+
 struct SellRing {
     int* col;           // [kRingDepth][kRingStage] of this warp
     float* val;
@@ -540,7 +544,7 @@ __device__ __forceinline__ SellRing ring_init(unsigned char* dsm, GridSync* sync
     r.seq = 0;
     r.policy = tc::policy_evict_first();
     r.sync = sync;
-    r.timeoutNs = timeoutNs;
+    r.timeoutNs = timeoutNs > kAsyncWaitFloorNs ? timeoutNs : kAsyncWaitFloorNs;
     if (lane == 0)
         for (int d = 0; d < kRingDepth; ++d) tc::mbar_init(&r.bar[d], 1);
     __syncwarp();

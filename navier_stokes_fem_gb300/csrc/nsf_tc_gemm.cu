@@ -175,6 +175,8 @@ void tc_dense(const TcArgs& a, cudaStream_t s, int sms) {
     const size_t smem = (size_t)kTcM * a.K * 2 + (size_t)a.N * a.K * 2;
     // 16-byte staging when every segment's rows are 16-byte aligned groups of 8 values
     TcArgs b = a;
+    // the MMA waits never give up sooner than 200 ms (TMEM is freed only after the MMAs in flight completed)
+    b.timeoutNs = std::max(a.timeoutNs, 200000000LL);
     b.vec8 = 1;
     for (int i = 0; i < a.nseg; ++i)
         if (a.seg[i].width % 8 || reinterpret_cast<uintptr_t>(a.seg[i].base) % 16) b.vec8 = 0;

@@ -136,3 +136,24 @@ def test_bad_arguments_are_statuses():
     with pytest.raises(nsf.NSFemError):
         d.locate(np.zeros((3, 2), np.float32))                               # no mesh yet
     d.close()
+
+
+@pytest.mark.parametrize("name,solver", [("pressure_stiffness", "mixed"), ("diffusion", "mixed"),
+                                         ("pressure_stiffness", "pcg_mixed"), ("diffusion", "pcg_mixed")])
+def test_barrier_time_limit_in_every_mixed_form(system, name, solver):
+    """The one-launch and the split (refresh + inner-iteration launches) mixed solvers, narrow and wide systems:
+    with a zero wait limit every grid-wide wait expires, the solve returns the time-out status without hanging
+    the host loop, and the next solve on the same handle converges."""
+    d, o = system
+    n = d.matrix_shape(name)[0]
+    b = np.random.default_rng(9).standard_normal(n)
+    if solver == "pcg_mixed":
+        d.precond_ic0(name)
+    d.set_barrier_timeout(0.0)
+    with pytest.raises(nsf.NSFemError) as e:
+        d.conjugate_gradient(name, b, np.zeros(n), solver=solver)
+    assert e.value.status == 4
+    d.set_barrier_timeout(2.0)
+    x, it, _ = d.conjugate_gradient(name, b, np.zeros(n), solver=solver)
+    assert _relres(o, name, x, b) < 1.5 * TOL
+    d.precond_clear(name)

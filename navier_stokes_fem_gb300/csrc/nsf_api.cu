@@ -212,6 +212,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.sellCol = S.sellCol.get();
     a.sellVal = S.sellVal.get();
     a.sellVal32 = S.sellVal32.get();
+    a.sellMaxW = S.maxWidth;
     a.b = b;
     a.x0 = x0;
     a.x = x;

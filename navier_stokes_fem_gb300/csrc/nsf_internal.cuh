@@ -211,6 +211,7 @@ struct CgArgs {
     CgInfo* info;
     int maxIt;
     int fallbackMaxIt;       // preconditioned solvers: iteration budget of the plain-CG fallback (0: what is left)
+    int sellMaxW;            // entries per row of the SELL copy's widest slice
     PcgLoop* loop;           // split mixed PCG: the control state between kernels
     int loopInit;            // split mixed PCG: this refresh kernel starts the solve
     double tol2;

@@ -502,13 +502,15 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         const float* rOld = L.rflip ? a.r32b : a.r32;
         float* rNew = L.rflip ? a.r32 : a.r32b;
         float pqHi = 0.f, pqLo = 0.f;
-        product32<false, 6>(ring, a, rb, re, reinterpret_cast<float*>(stage),
-                            [&](int c) { return fmaf(betaf, pp[c], w[c]); },
-                            [&](int row, float acc, float pi) {
-                                pc[row] = pi;
-                                a.q32[row] = acc;
-                                df_acc(pqHi, pqLo, pi, acc);
-                            });
+        auto gp = [&](int c) { return fmaf(betaf, pp[c], w[c]); };
+        auto ep = [&](int row, float acc, float pi) {
+            pc[row] = pi;
+            a.q32[row] = acc;
+            df_acc(pqHi, pqLo, pi, acc);
+        };
+        // chunks as wide as the widest slice when that is 5 (a structured P1 system without its exact zeros)
+        if (a.sellMaxW <= 5) product32<false, 5>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        else product32<false, 6>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;

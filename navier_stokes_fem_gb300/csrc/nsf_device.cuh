@@ -793,12 +793,18 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
     while (status == NSF_ERR_NOT_CONVERGED && it < a.maxIt) {
         // phase A: q = A p (streamed matrix), partial p.q
         double pq = 0;
-        matrix_product<double, double, false, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
-                                              [&](int c) { return p[c]; },
-                                              [&](int row, double acc, double pr) {
-                                                  a.q[row] = acc;
-                                                  pq = fma(pr, acc, pq);
-                                              });
+        auto gq = [&](int c) { return p[c]; };
+        auto eq = [&](int row, double acc, double pr) {
+            a.q[row] = acc;
+            pq = fma(pr, acc, pq);
+        };
+        // chunks as wide as the widest slice when that is 5 (a structured P1 system without its exact zeros)
+        if (!Wide && a.sellMaxW <= 5)
+            matrix_product<double, double, false, 5, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val,
+                                                           rb, re, stage, gq, eq);
+        else
+            matrix_product<double, double, false, kUnroll, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col,
+                                                                 a.val, rb, re, stage, gq, eq);
         pq = block_sum(pq, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(2)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
@@ -1011,12 +1017,14 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
                                 df_acc(pqHi, pqLo, pi, acc);
                             });
         } else {
-            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return fmaf(betaf, pp[c], r32[c]); },
-                            [&](int row, float acc, float pi) {
-                                pc[row] = pi;
-                                a.q32[row] = acc;
-                                df_acc(pqHi, pqLo, pi, acc);
-                            });
+            auto gp = [&](int c) { return fmaf(betaf, pp[c], r32[c]); };
+            auto ep = [&](int row, float acc, float pi) {
+                pc[row] = pi;
+                a.q32[row] = acc;
+                df_acc(pqHi, pqLo, pi, acc);
+            };
+            if (a.sellMaxW <= 5) product32<Wide, 5>(ring, a, rb, re, stage32, gp, ep);
+            else product32<Wide>(ring, a, rb, re, stage32, gp, ep);
         }
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;

@@ -196,6 +196,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     // a preconditioned solve runs on the factor's colour-permuted copy of the matrix
     Csr& S = precond ? h->factors[slot].Ap : A;
     prepare_matrix(S, mode == NSF_SOLVER_MIXED || mode == NSF_SOLVER_PCG_MIXED, h->stream);
+    if (mode == NSF_SOLVER_PCG_MIXED) prepare_col16(S, h->stream);   // the inner iterations' narrow product
     ensure_workspace(h, S.rows);
     CgWorkspace& ws = h->ws;
     const int infoIndex = h->infoCursor;
@@ -210,6 +211,8 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     a.rowsum32 = S.rowsum32.get();
     a.sellStart = S.sellStart.get();
     a.sellCol = S.sellCol.get();
+    a.sellCol16 = S.hasCol16 ? S.sellCol16.get() : nullptr;
+    a.sellColBase = S.hasCol16 ? S.sellColBase.get() : nullptr;
     a.sellVal = S.sellVal.get();
     a.sellVal32 = S.sellVal32.get();
     a.sellMaxW = S.maxWidth;

@@ -79,10 +79,12 @@ __global__ void __launch_bounds__(kCgThreads, 2) pcg_mixed_refresh_kernel(CgArgs
     team_pcg_mixed_refresh(t, a, stage, smem, &ring);
 }
 
+// (C16: the matrix and both factor parts have 16-bit column copies.)
+template <bool C16>
 __global__ void __launch_bounds__(kCgThreads, 4) pcg_mixed_inner_kernel(CgArgs a) {
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed_inner(t, a, stage, smem, nullptr);
+    team_pcg_mixed_inner<C16>(t, a, stage, smem, nullptr);
 }
 
 // The split plain mixed CG for wide (P2) systems: refresh launches (fold, FP64 true residual, tests) at 2 CTAs per
@@ -184,8 +186,12 @@ static int cg_occupancy() {
 
 // CTAs per SM of the split solvers' inner-iteration kernels (at most 4)
 static int inner_occupancy() {
-    int o = 0, c = 0, r = 0;
-    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, (const void*)pcg_mixed_inner_kernel, kCgThreads, 0));
+    int o = 0, o16 = 0, c = 0, r = 0;
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, (const void*)pcg_mixed_inner_kernel<false>, kCgThreads,
+                                                           0));
+    NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o16, (const void*)pcg_mixed_inner_kernel<true>,
+                                                           kCgThreads, 0));
+    o = std::min(o, o16);
     NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, (const void*)cg_mixed_inner_kernel, kCgThreads, 0));
     NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, (const void*)cg_mixed_refresh_kernel, kCgThreads, 0));
     if (r < 2) throw Error{NSF_ERR_CUDA, "mixed refresh kernel cannot be resident at 2 CTAs per SM"};
@@ -257,13 +263,15 @@ void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     a.loopInit = 1;
     launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
     a.loopInit = 0;
+    const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;
+    const void* inner = c16 ? (const void*)pcg_mixed_inner_kernel<true> : (const void*)pcg_mixed_inner_kernel<false>;
     // every refresh counts one outer cycle and the solve ends at maxOuter of them, so this loop is bounded
     for (int cycle = 0; cycle <= a.maxOuter + 1; ++cycle) {
         int state = 0;
         NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
         NSF_CUDA(cudaStreamSynchronize(s));
         if (state != kLoopInner) return;
-        launch((const void*)pcg_mixed_inner_kernel, ws.gridInner, 0);
+        launch(inner, ws.gridInner, 0);
         launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
     }
     throw Error{NSF_ERR_CUDA, "preconditioned solve did not finish within its refresh budget"};

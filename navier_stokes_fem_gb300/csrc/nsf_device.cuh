@@ -50,6 +50,7 @@ __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ unsigned short ld_stream(const unsigned short* p) { return __ldcs(p); }
 
 // A team: `size` consecutive CTAs of a persistent launch that cooperate on one system (the whole grid for a
 // single solve; a share of the grid per instance in the batched step).  Its barrier is a monotone arrival
@@ -271,15 +272,27 @@ template <typename TA> struct DiffPre {
 template <typename TA> __device__ __forceinline__ TA row_self(TA v) { return v; }
 template <typename TA> __device__ __forceinline__ TA row_self(const DiffPre<TA>& v) { return v.self; }
 
-// Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W).
-template <int U, typename TV>
-__device__ __forceinline__ void sell_chunk(const int* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
-                                           int (&c)[U], TV (&v)[U]) {
+// Column indices of a SELL-32 matrix are 32-bit (TC = int) or, when every slice's columns span fewer than 65535,
+// 16-bit offsets from a per-slice base (TC = unsigned short; kCol16Pad marks a padding entry of column -1).
+
+// Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W); cb is the slice's
+// column base of a 16-bit column array.
+template <int U, typename TV, typename TC = int>
+__device__ __forceinline__ void sell_chunk(const TC* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
+                                           int (&c)[U], TV (&v)[U], int cb = 0) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const bool in = k0 + u < W;
-        c[u] = in ? ld_stream(cp + (k0 + u) * kSlice) : -1;
-        v[u] = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
+        if constexpr (sizeof(TC) == 2) {
+            // a padding entry's value is zeroed too: the 16-bit copy of a matrix stores its diagonal as padding
+            const int d = in ? (int)ld_stream(cp + (k0 + u) * kSlice) : kCol16Pad;
+            const TV x = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
+            c[u] = d == kCol16Pad ? -1 : cb + d;
+            v[u] = d == kCol16Pad ? TV(0) : x;
+        } else {
+            c[u] = in ? ld_stream(cp + (k0 + u) * kSlice) : -1;
+            v[u] = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
+        }
     }
 }
 
@@ -289,11 +302,13 @@ __device__ __forceinline__ void sell_chunk(const int* __restrict__ cp, const TV*
 // at a time, one per lane, and handed out by shuffles.
 // pre(row) is evaluated when a slice starts (its loads overlap the slice's), and its value goes to epi(row, sum,
 // pre); with Diff it must be the row's own vector entry.  Rows [rb, re): rb a multiple of 32 unless rb == re.
-template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename Gather, typename Pre,
-          typename Epi>
-__device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, const int* __restrict__ col,
+// With 16-bit columns (TC = unsigned short) colBase holds each slice's column base.
+template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename TC = int, typename Gather,
+          typename Pre, typename Epi>
+__device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, const TC* __restrict__ col,
                                           const TV* __restrict__ val, int rb, int re, Gather gather, Pre pre,
-                                          Epi epi) {
+                                          Epi epi, const int* __restrict__ colBase = nullptr) {
+    constexpr bool C16 = sizeof(TC) == 2;
     using PreT = decltype(pre(0));
     if (rb >= re) return;   // (an empty range may start inside the last, partial slice)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -303,22 +318,25 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
     const int count = (s1 - sFirst + nw - 1) / nw;   // this warp's slices
     const int per = (count + NS - 1) / NS;           // per stream: stream q takes i in [q per, (q + 1) per)
     int mb[NS], me[NS], base[NS], W[NS], c[NS][U];
+    int mcb[NS], cb[NS];   // 16-bit columns: the slices' column bases (lane j: slice i0 + j) and the current one's
     TV v[NS][U];
     auto meta_load = [&](int q, int i0) {   // lane j: start / end of stream q's slice i0 + j
         const int idx = sFirst + (q * per + i0 + lane) * nw;
         const bool in = idx < s1 && i0 + lane < per;
         mb[q] = in ? sliceStart[idx] : 0;
         me[q] = in ? sliceStart[idx + 1] : 0;
+        if constexpr (C16) mcb[q] = in ? colBase[idx] : 0;
     };
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
         meta_load(q, 0);
         base[q] = __shfl_sync(0xffffffffu, mb[q], 0);
         W[q] = (__shfl_sync(0xffffffffu, me[q], 0) - base[q]) / kSlice;
-        sell_chunk<U, TV>(col + base[q] + lane, val + base[q] + lane, W[q], 0, c[q], v[q]);
+        cb[q] = C16 ? __shfl_sync(0xffffffffu, mcb[q], 0) : 0;
+        sell_chunk<U, TV, TC>(col + base[q] + lane, val + base[q] + lane, W[q], 0, c[q], v[q], cb[q]);
     }
     for (int k = 0; k < per; ++k) {
-        int row[NS], Wc[NS], bc[NS];
+        int row[NS], Wc[NS], bc[NS], cbc[NS];
         bool live[NS];
         PreT pv[NS];
         TA g[NS][U];
@@ -340,15 +358,18 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
         for (int q = 0; q < NS; ++q) {
             Wc[q] = W[q];
             bc[q] = base[q];
-            int baseN = 0, WN = 0;
+            cbc[q] = cb[q];
+            int baseN = 0, WN = 0, cbN = 0;
             if (k + 1 < per && q * per + k + 1 < count) {
                 if (((k + 1) & 31) == 0) meta_load(q, k + 1);
                 baseN = __shfl_sync(0xffffffffu, mb[q], (k + 1) & 31);
                 WN = (__shfl_sync(0xffffffffu, me[q], (k + 1) & 31) - baseN) / kSlice;
+                if constexpr (C16) cbN = __shfl_sync(0xffffffffu, mcb[q], (k + 1) & 31);
             }
-            sell_chunk<U, TV>(col + baseN + lane, val + baseN + lane, WN, 0, c[q], v[q]);
+            sell_chunk<U, TV, TC>(col + baseN + lane, val + baseN + lane, WN, 0, c[q], v[q], cbN);
             base[q] = baseN;
             W[q] = WN;
+            cb[q] = cbN;
         }
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
@@ -368,7 +389,7 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
                 int c2[U];
                 TV v2[U];
                 TA g2[U];
-                sell_chunk<U, TV>(col + bc[q] + lane, val + bc[q] + lane, Wc[q], k0, c2, v2);
+                sell_chunk<U, TV, TC>(col + bc[q] + lane, val + bc[q] + lane, Wc[q], k0, c2, v2, cbc[q]);
 #pragma unroll
                 for (int u = 0; u < U; ++u) g2[u] = c2[u] >= 0 ? gather(c2[u]) : TA(0);
 #pragma unroll
@@ -702,11 +723,18 @@ __device__ __forceinline__ void matrix_product(const int* sellStart, const int* 
 // The FP32 difference-form product of the mixed solvers, q_i = sum_j a_ij (p_j - p_i) + rowsum_i p_i: through
 // the warp's ring for narrow matrices when the kernel has one, else the register-pipelined SELL-32 product (or the
 // CSR product without a SELL copy).  epi(row, sum with the row-sum term, p_row).
-template <bool Wide, int U = kUnroll, typename Gather, typename Epi>
+// (C16: the narrow register-pipelined product over the 16-bit column copy, which the caller has checked exists;
+// that copy stores the diagonal entries as padding, whose difference-form terms are exactly zero.)
+template <bool Wide, int U = kUnroll, bool C16 = false, typename Gather, typename Epi>
 __device__ __forceinline__ void product32(SellRing* ring, const CgArgs& a, int rb, int re, float* stage,
                                           Gather gather, Epi epi) {
     auto pre = [&](int row) { return DiffPre<float>{gather(row), a.rowsum32[row]}; };
     auto fin = [&](int row, float acc, const DiffPre<float>& q) { epi(row, fmaf(q.rs, q.self, acc), q.self); };
+    if constexpr (C16 && !Wide) {
+        sell_rows<float, float, true, 1, U, unsigned short>(a.sellStart, a.sellCol16, a.sellVal32, rb, re, gather,
+                                                            pre, fin, a.sellColBase);
+        return;
+    }
     if constexpr (!Wide) {
         if (ring && a.sellStart) {
             sell_rows_ring<float, true>(*ring, a.sellStart, a.sellCol, a.sellVal32, rb, re, gather, pre, fin);

@@ -8,6 +8,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/nsfem_gb300.h"
@@ -88,6 +89,11 @@ struct Csr {
     DevBuf<double> sellVal;
     DevBuf<float> sellVal32;
     bool hasSell = false, hasSell32 = false;
+    // 16-bit copy of sellCol (offsets from a per-slice base; diagonal entries as padding), built on request when
+    // every slice fits; for the difference-form FP32 product only
+    DevBuf<int> sellColBase;
+    DevBuf<unsigned short> sellCol16;
+    bool col16Tried = false, hasCol16 = false;
     void values_changed() {
         has32 = hasSell = hasSell32 = false;
         val32.release();
@@ -100,6 +106,7 @@ struct Csr {
 // coloured so that no two neighbours share a colour, and "lower" means a neighbour of a smaller colour.  The
 // triangular solves then run colour by colour, every row of a colour in parallel.
 constexpr int kMaxColours = 16;
+constexpr int kCol16Pad = 0xFFFF;   // padding entry (column -1) of a 16-bit SELL column array
 
 struct FactorView {
     int colours = 0;
@@ -115,6 +122,10 @@ struct FactorView {
     const int* upCol = nullptr;
     const double* upVal = nullptr;
     const float* upVal32 = nullptr;
+    const unsigned short* loCol16 = nullptr;  // 16-bit column copies of both parts (null: not built, or a slice's
+    const int* loColBase = nullptr;           // columns span 65535 or more)
+    const unsigned short* upCol16 = nullptr;
+    const int* upColBase = nullptr;
     const double* dinv = nullptr;             // 1 / L_ii per permuted row (1 on padding rows)
     const float* dinv32 = nullptr;
     double* w = nullptr;                      // work vector: forward-sweep result, then M^-1 r (in place)
@@ -142,6 +153,9 @@ struct Factor {
     Csr Ap;                                    // P A P^T (padded), with its SELL copies
     DevBuf<int> apFrom;                        // Ap value k = A.val[apFrom[k]] (-1: padding diagonal, 1.0)
     DevBuf<int> loStart, loCol, loFrom, upStart, upCol, upFrom;
+    DevBuf<int> loColBase, upColBase;           // 16-bit column copies of the two parts (when both fit)
+    DevBuf<unsigned short> loCol16, upCol16;
+    bool col16 = false;
     int loMaxW = 0, upMaxW = 0;
     DevBuf<double> loVal, upVal, dinv;
     DevBuf<float> loVal32, upVal32, dinv32;
@@ -190,6 +204,8 @@ struct CgArgs {
     const float* rowsum32;   // row sums of the FP64 matrix, rounded once (mixed precision difference form)
     const int* sellStart;    // SELL-32 copy (null: the CSR arrays are used)
     const int* sellCol;
+    const unsigned short* sellCol16;   // its 16-bit column copy (null: none)
+    const int* sellColBase;
     const double* sellVal;
     const float* sellVal32;
     FactorView f;            // preconditioned solvers only
@@ -264,6 +280,16 @@ void axpy_bc_launch(int n, const double* a, double* y, const unsigned char* mask
 void make_fp32_values(Csr& A, cudaStream_t s);
 // SELL-32 copy (FP64 values; with fp32 also the FP32 values and row sums) for the CG kernels; no-op when current
 void prepare_matrix(Csr& A, bool fp32, cudaStream_t s);
+// 16-bit column copy of a SELL-32 column array (16-bit offsets from each slice's smallest column; kCol16Pad for
+// padding entries of column -1 and, with noDiag, for the diagonal entries) when every slice's remaining columns
+// span fewer than kCol16Pad; false, with nothing allocated, otherwise.  Synchronises the stream.
+bool sell_col16(int nSlices, const int* start, const int* col, bool noDiag, DevBuf<int>& base,
+                DevBuf<unsigned short>& col16, cudaStream_t s);
+// The matrix's 16-bit column copy, after prepare_matrix (tried once per SELL copy), for the difference-form FP32
+// product only: its diagonal entries are padding there, since the difference form's diagonal term
+// a_ii (p_i - p_i) is exactly zero (and a row's own entry usually lies in another colour block of the permuted
+// system than its neighbours, which would put the slice's columns far apart).
+void prepare_col16(Csr& A, cudaStream_t s);
 
 // preconditioner factors (nsf_precond.cu)
 void factor_structure(Factor& F, const Csr& A, cudaStream_t s);

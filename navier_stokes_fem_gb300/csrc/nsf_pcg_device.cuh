@@ -73,10 +73,16 @@ __device__ __forceinline__ void colour0_store(const FactorView& F, TA* w, int ro
 // thread's r.z terms so far.  Returns false on a barrier timeout.
 // One colour phase of a sweep: through the warp's ring when the kernel has one and the factor is narrow enough
 // (FP32 factors), else the register-pipelined SELL-32 product.
-// (Lean: one slice stream per warp, for the kernels that run at more CTAs per SM.)
-template <typename TV, typename TA, bool Lean = false, typename Gather, typename Pre, typename Epi>
+// (Lean: one slice stream per warp, for the kernels that run at more CTAs per SM.  C16: the register product
+// over the part's 16-bit column copy col16 / colBase, which the caller has checked exists.)
+template <typename TV, typename TA, bool Lean = false, bool C16 = false, typename Gather, typename Pre, typename Epi>
 __device__ __forceinline__ void sweep_rows(SellRing* ring, int maxW, const int* start, const int* col, const TV* val,
-                                           int r0, int r1, Gather gather, Pre pre, Epi epi) {
+                                           int r0, int r1, Gather gather, Pre pre, Epi epi,
+                                           const unsigned short* col16 = nullptr, const int* colBase = nullptr) {
+    if constexpr (C16) {
+        sell_rows<TV, TA, false, 1, 4, unsigned short>(start, col16, val, r0, r1, gather, pre, epi, colBase);
+        return;
+    }
     if constexpr (sizeof(TV) == 4) {
         if (ring && maxW <= kRingWidth) {
             sell_rows_ring<TA, false>(*ring, start, col, val, r0, r1, gather, pre, epi);
@@ -87,7 +93,7 @@ __device__ __forceinline__ void sweep_rows(SellRing* ring, int maxW, const int* 
 }
 
 // (cFirst = 2: colour 1 of the forward sweep, and with two colours its backward step, are already done.)
-template <typename TV, typename TA, bool Lean = false>
+template <typename TV, typename TA, bool Lean = false, bool C16 = false>
 __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, const TV* loVal, const TV* upVal,
                                const TA* dinv, DotAcc<TA>& rz, double* smem, int& where, double& rzOut,
                                SellRing* ring = nullptr, int cFirst = 1) {
@@ -97,7 +103,7 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
         const bool last = c == C - 1;
-        sweep_rows<TV, TA, Lean>(ring, F.loMaxW, F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
+        sweep_rows<TV, TA, Lean, C16>(ring, F.loMaxW, F.loStart, F.loCol, loVal, r0, r1, [&](int j) { return w[j]; },
                            [&](int i) { return SweepRow<TA>{r[i], dinv[i], TA(0)}; },
                            [&](int i, TA acc, const SweepRow<TA>& q) {
                                TA y = (q.src - acc) * q.d;
@@ -106,19 +112,19 @@ __device__ bool precond_sweeps(Team& t, const CgArgs& a, const TA* r, TA* w, con
                                    rz.add(q.src, y);
                                }
                                w[i] = y;
-                           });
+                           }, F.loCol16, F.loColBase);
         if (!t.barrier(where++)) return false;
     }
     for (int c = C - 2; c >= 0; --c) {
         int r0, r1;
         team_block(F.colourRow[c], F.colourRow[c + 1], t, r0, r1);
-        sweep_rows<TV, TA, Lean>(ring, F.upMaxW, F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
+        sweep_rows<TV, TA, Lean, C16>(ring, F.upMaxW, F.upStart, F.upCol, upVal, r0, r1, [&](int j) { return w[j]; },
                            [&](int i) { return SweepRow<TA>{w[i], dinv[i], r[i]}; },
                            [&](int i, TA acc, const SweepRow<TA>& q) {
                                const TA z = (q.src - acc) * q.d;
                                rz.add(q.r, z);
                                w[i] = z;
-                           });
+                           }, F.upCol16, F.upColBase);
         if (c > 0 && !t.barrier(where++)) return false;
     }
     const double part = rz.block(smem);
@@ -485,6 +491,8 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
 // sweep's pre step and take their lower neighbours' y0 from the previous residual, y0_j = (r_j - alpha q_j) / L_jj
 // (the same arithmetic as the stored y0, so the sweep sees the same values); rows of colours >= 2 update d and r.  The residual alternates between two buffers, since the neighbours' previous r is read while the
 // own rows' new r is written.  On two colours an iteration has 3 grid barriers instead of 4.
+// (C16: the product and the sweeps read the 16-bit column copies of the matrix and of both factor parts.)
+template <bool C16 = false>
 static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
                                              PcgLoop& L, int& where) {
     const FactorView& F = a.f;
@@ -509,8 +517,8 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
             df_acc(pqHi, pqLo, pi, acc);
         };
         // chunks as wide as the widest slice when that is 5 (a structured P1 system without its exact zeros)
-        if (a.sellMaxW <= 5) product32<false, 5>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
-        else product32<false, 6>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        if (a.sellMaxW <= 5) product32<false, 5, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        else product32<false, 6, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;
@@ -556,8 +564,12 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
             int r0, r1;
             team_block(F.colourRow[1], F.colourRow[2], t, r0, r1);
             const bool last = C == 2;
-            sell_rows<float, float, false, 1, 4>(
-                F.loStart, F.loCol, F.loVal32, r0, r1,
+            using TC = std::conditional_t<C16, unsigned short, int>;
+            const TC* loCol;
+            if constexpr (C16) loCol = F.loCol16;
+            else loCol = F.loCol;
+            sell_rows<float, float, false, 1, 4, TC>(
+                F.loStart, loCol, F.loVal32, r0, r1,
                 [&](int j) { return fmaf(-alphaf, a.q32[j], rOld[j]) * dinv[j]; },
                 [&](int i) {
                     const float rn = fmaf(-alphaf, a.q32[i], rOld[i]);
@@ -573,7 +585,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                         rzn.add(q.src, y);
                     }
                     w[i] = y;
-                });
+                }, F.loColBase);
         }
         const double rrn = block_sum_df(rrHi, rrLo, smem);
         if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
@@ -586,8 +598,8 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         if (rrs <= rrStop) break;   // time for a true residual
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
         double rzs = 0;
-        if (!precond_sweeps<float, float, true>(t, a, rNew, w, F.loVal32, F.upVal32, dinv, rzn, smem, where, rzs,
-                                                ring, 2))
+        if (!precond_sweeps<float, float, true, C16>(t, a, rNew, w, F.loVal32, F.upVal32, dinv, rzn, smem, where,
+                                                     rzs, ring, 2))
             return false;
         if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
         L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
@@ -699,6 +711,7 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
     pcg_loop_store(t, a, L);
 }
 
+template <bool C16 = false>
 static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
     int where = 400;
     // the fields the inner iterations read or write (the rest of the state stays in memory)
@@ -712,7 +725,7 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.itRef = G.itRef;
     L.flip = G.flip;
     L.rflip = G.rflip;
-    const bool ok = a.f.colours >= 2 ? pcg_mixed_inner_fused(t, a, stage, smem, ring, L, where)
+    const bool ok = a.f.colours >= 2 ? pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where)
                                      : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
     if (t.rank == 0 && threadIdx.x == 0) {

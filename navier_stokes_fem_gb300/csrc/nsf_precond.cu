@@ -229,6 +229,15 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
     F.upStart.upload(up.start.data(), up.start.size(), s);
     F.upCol.upload(up.col.data(), up.col.size(), s);
     F.upFrom.upload(up.from.data(), up.from.size(), s);
+    // 16-bit column copies for the inner iterations (both parts or neither)
+    F.col16 = sell_col16(np / 32, F.loStart.get(), F.loCol.get(), false, F.loColBase, F.loCol16, s) &&
+              sell_col16(np / 32, F.upStart.get(), F.upCol.get(), false, F.upColBase, F.upCol16, s);
+    if (!F.col16) {
+        F.loColBase.release();
+        F.loCol16.release();
+        F.upColBase.release();
+        F.upCol16.release();
+    }
     F.lVal.alloc(std::max<int64_t>(nnzL, 1));
     F.diag.alloc((size_t)n);
     F.loVal.alloc(std::max<size_t>(lo.col.size(), 1));
@@ -379,6 +388,12 @@ FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     v.upCol = F.upCol.get();
     v.upVal = F.upVal.get();
     v.upVal32 = F.upVal32.get();
+    if (F.col16) {
+        v.loCol16 = F.loCol16.get();
+        v.loColBase = F.loColBase.get();
+        v.upCol16 = F.upCol16.get();
+        v.upColBase = F.upColBase.get();
+    }
     v.dinv = F.dinv.get();
     v.dinv32 = F.dinv32.get();
     v.w = ws.w.get();

@@ -6,6 +6,8 @@
 // 575-595, 695-707) are fused into the product's epilogue.
 #include "nsf_internal.cuh"
 
+#include <climits>
+
 #include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -163,9 +165,91 @@ __global__ void sell_fill_kernel(int rows, int cols, int nSlices, const int* __r
     }
 }
 
+// Entry i of slice sl (lane = i mod 32) is a padding entry of the 16-bit copy: column -1, or (noDiag) the row's
+// own column.
+__device__ __forceinline__ bool col16_pad(int c, int sl, int lane, bool noDiag) {
+    return c < 0 || (noDiag && c == sl * 32 + lane);
+}
+
+// One warp per slice: the slice's smallest and largest column (padding entries left out).
+__global__ void col16_base_kernel(int nSlices, const int* __restrict__ start, const int* __restrict__ col,
+                                  bool noDiag, int* __restrict__ base, int* __restrict__ overflow) {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < nSlices; sl += gridDim.x * wpb) {
+        const int b = start[sl], e = start[sl + 1];   // e - b is a multiple of 32: every lane runs the same trips
+        int lo = INT_MAX, hi = -1;
+        for (int i = b + lane; i < e; i += 32) {
+            const int c = col[i];
+            if (!col16_pad(c, sl, lane, noDiag)) {
+                lo = min(lo, c);
+                hi = max(hi, c);
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            base[sl] = hi < 0 ? 0 : lo;
+            if (hi >= 0 && hi - lo >= kCol16Pad) atomicOr(overflow, 1);
+        }
+    }
+}
+
+__global__ void col16_fill_kernel(int nSlices, const int* __restrict__ start, const int* __restrict__ col,
+                                  bool noDiag, const int* __restrict__ base, unsigned short* __restrict__ col16) {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (int sl = blockIdx.x * wpb + (threadIdx.x >> 5); sl < nSlices; sl += gridDim.x * wpb) {
+        const int b = start[sl], e = start[sl + 1], cb = base[sl];
+        for (int i = b + lane; i < e; i += 32) {
+            const int c = col[i];
+            col16[i] = (unsigned short)(col16_pad(c, sl, lane, noDiag) ? kCol16Pad : c - cb);
+        }
+    }
+}
+
+bool sell_col16(int nSlices, const int* start, const int* col, bool noDiag, DevBuf<int>& base,
+                DevBuf<unsigned short>& col16, cudaStream_t s) {
+    base.release();
+    col16.release();
+    if (nSlices <= 0) return false;
+    int entries = 0;
+    NSF_CUDA(cudaMemcpyAsync(&entries, start + nSlices, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DevBuf<int> flag;
+    flag.alloc(1);
+    flag.zero(s);
+    base.alloc((size_t)nSlices);
+    const int blocks = grid_for((int64_t)nSlices * 32, 256);
+    col16_base_kernel<<<blocks, 256, 0, s>>>(nSlices, start, col, noDiag, base.get(), flag.get());
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+    int over = 0;
+    NSF_CUDA(cudaMemcpyAsync(&over, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSF_CUDA(cudaStreamSynchronize(s));
+    if (over || entries <= 0) {
+        base.release();
+        return false;
+    }
+    col16.alloc((size_t)entries);
+    col16_fill_kernel<<<blocks, 256, 0, s>>>(nSlices, start, col, noDiag, base.get(), col16.get());
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+    NSF_CUDA(cudaStreamSynchronize(s));
+    return true;
+}
+
+void prepare_col16(Csr& A, cudaStream_t s) {
+    if (!A.hasSell || A.col16Tried) return;
+    A.col16Tried = true;
+    A.hasCol16 = sell_col16(A.nSlices, A.sellStart.get(), A.sellCol.get(), true, A.sellColBase, A.sellCol16, s);
+}
+
 void prepare_matrix(Csr& A, bool fp32, cudaStream_t s) {
     if (fp32) make_fp32_values(A, s);
     if (!A.hasSell) {
+        A.col16Tried = A.hasCol16 = false;
+        A.sellColBase.release();
+        A.sellCol16.release();
         A.nSlices = (A.rows + 31) / 32;
         DevBuf<long long> width, start64;
         width.alloc((size_t)A.nSlices);

@@ -206,3 +206,26 @@ def test_multicolour_pcg_on_unstructured_pressure(which):
     assert itm < it_plain
     d.close()
     o.close()
+
+
+def test_mixed_pcg_when_slice_columns_span_beyond_16_bits():
+    """A periodic chain of 140000 rows: after the two-colour permutation the wrap-around couples permuted rows
+    70000 apart, so neither the matrix nor the factor gets a 16-bit column copy and the inner iterations read the
+    32-bit columns; the solve still reaches the FP64 residual and matches FP64 PCG."""
+    import scipy.sparse as sp
+    n = 140000
+    A = sp.diags([np.full(n - 1, -1.0), np.full(n, 2.001), np.full(n - 1, -1.0)], [-1, 0, 1], format="lil")
+    A[0, n - 1] = A[n - 1, 0] = -1.0
+    A = A.tocsr()
+    A.sort_indices()
+    name = "pressure_stiffness"
+    d = nsf.GPUSimulationDevice(0)
+    d.upload_matrix(name, A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data, A.shape)
+    assert int(d.precond_pattern(name)[2].max()) + 1 == 2
+    d.precond_ic0(name)
+    b = np.random.default_rng(13).standard_normal(n)
+    xm, itm, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_mixed")
+    assert np.linalg.norm(b - A @ xm) / np.linalg.norm(b) < 1.5 * TOL
+    x, it, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
+    assert rel(xm, x) < 1e-6 and itm <= 2 * it + 10
+    d.close()

@@ -301,14 +301,14 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def pcg_bytes(mixed, n, nz, nzl, its, outer):
-    """Minimal DRAM bytes of one preconditioned solve (int32 indices): per iteration the product with the
-    non-zeros of A and both triangular sweeps over the factor's nzl strictly lower entries (values + indices),
-    plus about 15 vector passes (product gathers and outputs, the x/r update, the sweeps' right-hand sides,
-    inverse diagonals and in-place results).  The mixed form moves FP32 values and vectors and adds an FP64
-    residual per refresh."""
+def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4):
+    """Minimal DRAM bytes of one preconditioned solve: per iteration the product with the non-zeros of A and both
+    triangular sweeps over the factor's nzl strictly lower entries (values + idx-byte column indices: 2 where the
+    mixed iterations read 16-bit column copies), plus about 15 vector passes (product gathers and outputs, the x/r
+    update, the sweeps' right-hand sides, inverse diagonals and in-place results).  The mixed form moves FP32
+    values and vectors and adds an FP64 residual (int32 indices) per refresh."""
     v = 4 if mixed else 8
-    it_bytes = (v + 4) * (nz + 2 * nzl) + 4 * (n + 1) + 15 * v * n
+    it_bytes = (v + idx) * (nz + 2 * nzl) + 4 * (n + 1) + 15 * v * n
     refresh = 12 * nz + 4 * (n + 1) + 28 * n
     return (outer + 1) * refresh + its * it_bytes
 
@@ -350,9 +350,9 @@ def nonzeros(sim, slot):
 
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
-# 4,198,401 rows, whose vectors exceed L2): pcg_mixed_inner_kernel 19.90 GB over 40 iterations, cg_fp64_kernel
-# 30.67 GB over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 118.5, "cg_fp64_kernel": 121.7}
+# 4,198,401 rows, whose vectors exceed L2): pcg_mixed_inner_kernel 16.94 GB over 40 iterations (16-bit column
+# copies), cg_fp64_kernel 30.67 GB over 60 iterations (its prologue included).
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 100.9, "cg_fp64_kernel": 121.7}
 
 
 def roofline(sim, arm, args):
@@ -361,17 +361,18 @@ def roofline(sim, arm, args):
     of its time, and the solve is reported under that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
-    nzl = {}
+    nzl, idx = {}, {}
     for slot in (0, 1, 2):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
+            idx[slot] = sim.precond_index_bytes(slot)
     names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel", 2: "pcg_mixed_inner_kernel", 3: "pcg_fp64_kernel"}
     bytes_by, ms_by, rowit_by = {}, {}, {}
     for sl, m_, n_, i_, o_, t_ in zip(prof["slot"], prof["mode"], prof["rows"], prof["iterations"], prof["outer"],
                                       prof["ms"]):
         m_, sl = int(m_), int(sl)
         if m_ in (2, 3):
-            b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_))
+            b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4)
         else:
             b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_))
         bytes_by[names[m_]] = bytes_by.get(names[m_], 0.0) + b

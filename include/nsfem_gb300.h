@@ -128,6 +128,10 @@ int nsf_precond_ic0(nsf_device* h, int slot, double* shiftUsed);
 int nsf_precond_set(nsf_device* h, int slot, const double* lower, const double* diag);
 int nsf_precond_get(nsf_device* h, int slot, double* lower, double* diag);
 int nsf_precond_kind(nsf_device* h, int slot);
+/* Bytes per column index that the FP32 iterations of the slot's mixed PCG read: 2 when its colour-permuted matrix
+ * and both factor parts have 16-bit column copies (every 32-row slice's columns within 65535 of each other; decided
+ * by the slot's first mixed PCG solve), else 4. */
+int nsf_precond_index_bytes(nsf_device* h, int slot);
 int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
 int nsf_precond_cap(nsf_device* h, int slot, int maxIterations);

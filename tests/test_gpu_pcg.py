@@ -200,6 +200,7 @@ def test_multicolour_pcg_on_unstructured_pressure(which):
     assert _relres(o, name, x, b) < 1.5 * TOL
     xm, itm, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_mixed")
     assert _relres(o, name, xm, b) < 1.5 * TOL           # the contract: the FP64 residual
+    assert d.precond_index_bytes(name) == 2              # small systems: the 16-bit column copies
     xt, st, _, _ = o.cg(name, b, x0, max_iter=20 * n, tol=1e-13)
     assert st == 0 and rel(xm, xt) < 1e-5 and rel(x, xt) < 1e-5
     _, it_plain, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="fp64")
@@ -226,6 +227,7 @@ def test_mixed_pcg_when_slice_columns_span_beyond_16_bits():
     b = np.random.default_rng(13).standard_normal(n)
     xm, itm, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_mixed")
     assert np.linalg.norm(b - A @ xm) / np.linalg.norm(b) < 1.5 * TOL
+    assert d.precond_index_bytes(name) == 4
     x, it, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
     assert rel(xm, x) < 1e-6 and itm <= 2 * it + 10
     d.close()

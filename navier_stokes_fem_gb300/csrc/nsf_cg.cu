@@ -87,6 +87,19 @@ __global__ void __launch_bounds__(kCgThreads, 4) pcg_mixed_inner_kernel(CgArgs a
     team_pcg_mixed_inner<C16>(t, a, stage, smem, nullptr);
 }
 
+// The same iterations as one 1024-thread CTA per SM, the form the split solver launches: the same 32 warps per
+// SM and 64 registers per thread, a quarter of the grid barrier's arrivals (1.5 % per iteration on the 2048²
+// pressure system, 9-13 % per step on systems of 0.26-1 M rows, where the barriers weigh more).  Two or more
+// colours and a SELL copy only: there is no staging area for the CSR product.
+constexpr int kInnerCtaThreads = 1024;
+template <bool C16>
+__global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_cta1024(CgArgs a) {
+    __shared__ double smem[kSmemSlots];
+    if (!a.sellStart) return;   // (the host never launches it without one)
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_mixed_inner<C16, true>(t, a, nullptr, smem, nullptr);
+}
+
 // The split plain mixed CG for wide (P2) systems: refresh launches (fold, FP64 true residual, tests) at 2 CTAs per
 // SM and FP32 iteration launches at 4.
 static __device__ void team_cg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem) {
@@ -145,6 +158,14 @@ __global__ void __launch_bounds__(kCgThreads, 4) cg_mixed_inner_kernel(CgArgs a)
     NSF_KERNEL_SHARED();
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
     team_cg_mixed_inner(t, a, stage, smem);
+}
+
+// One 1024-thread CTA per SM, as pcg_mixed_inner_kernel_cta1024 (a SELL copy only).
+__global__ void __launch_bounds__(kInnerCtaThreads, 1) cg_mixed_inner_kernel_cta1024(CgArgs a) {
+    __shared__ double smem[kSmemSlots];
+    if (!a.sellStart) return;   // (the host never launches it without one)
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_cg_mixed_inner(t, a, nullptr, smem);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -208,6 +229,15 @@ void cg_configure(CgWorkspace& ws, int device) {
     ws.grid = sms * perSm;
     ws.block = kCgThreads;
     ws.gridInner = sms * std::max(perSm, inner_occupancy());
+    // the 1024-thread inner kernels: one CTA per SM (0 if one of them cannot be resident)
+    int o1024 = 1;
+    for (const void* fn : {(const void*)pcg_mixed_inner_kernel_cta1024<true>,
+                           (const void*)pcg_mixed_inner_kernel_cta1024<false>, (const void*)cg_mixed_inner_kernel_cta1024}) {
+        int o = 0;
+        NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kInnerCtaThreads, 0));
+        o1024 = std::min(o1024, o);
+    }
+    ws.gridInner1024 = sms * o1024;
     ws.partials.alloc((size_t)6 * std::max(ws.grid, ws.gridInner));
     ws.sync.alloc(1);
     ws.info.alloc(4096);
@@ -224,17 +254,23 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStr
 }
 
 // A split solve: the refresh launch, then inner-iteration and refresh launches while the state says so.
-static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t refreshDsm, const void* inner,
-                         cudaStream_t s) {
+// (inner1024: the 1024-thread form, used when given, resident on the device and the matrix has a SELL copy; else
+// inner256 at ws.gridInner CTAs.)
+static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t refreshDsm, const void* inner1024,
+                         const void* inner256, cudaStream_t s) {
     a.loop = ws.loop.get();
-    auto launch = [&](const void* fn, int grid, size_t dsm) {
+    auto launch = [&](const void* fn, int grid, int block, size_t dsm) {
         NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
         void* params[] = {&a};
-        NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(ws.block), params, dsm, s));
+        NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), params, dsm, s));
         count_launch();
     };
+    const bool cta1024 = inner1024 && ws.gridInner1024 > 0 && a.sellStart;
+    const void* inner = cta1024 ? inner1024 : inner256;
+    const int innerGrid = cta1024 ? ws.gridInner1024 : ws.gridInner;
+    const int innerBlock = cta1024 ? kInnerCtaThreads : ws.block;
     a.loopInit = 1;
-    launch(refresh, ws.grid, refreshDsm);
+    launch(refresh, ws.grid, ws.block, refreshDsm);
     a.loopInit = 0;
     // every refresh counts one outer cycle and the solve ends at maxOuter of them, so this loop is bounded
     for (int cycle = 0; cycle <= a.maxOuter + 1; ++cycle) {
@@ -242,39 +278,25 @@ static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t 
         NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
         NSF_CUDA(cudaStreamSynchronize(s));
         if (state != kLoopInner) return;
-        launch(inner, ws.gridInner, 0);
-        launch(refresh, ws.grid, refreshDsm);
+        launch(inner, innerGrid, innerBlock, 0);
+        launch(refresh, ws.grid, ws.block, refreshDsm);
     }
     throw Error{NSF_ERR_CUDA, "mixed-precision solve did not finish within its refresh budget"};
 }
 
 void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
-    split_launch(ws, a, (const void*)cg_mixed_refresh_kernel, 0, (const void*)cg_mixed_inner_kernel, s);
+    split_launch(ws, a, (const void*)cg_mixed_refresh_kernel, 0, (const void*)cg_mixed_inner_kernel_cta1024,
+                 (const void*)cg_mixed_inner_kernel, s);
 }
 
 void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
-    a.loop = ws.loop.get();
-    auto launch = [&](const void* fn, int grid, size_t dsm) {
-        NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
-        void* params[] = {&a};
-        NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(ws.block), params, dsm, s));
-        count_launch();
-    };
-    a.loopInit = 1;
-    launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
-    a.loopInit = 0;
+    // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;
-    const void* inner = c16 ? (const void*)pcg_mixed_inner_kernel<true> : (const void*)pcg_mixed_inner_kernel<false>;
-    // every refresh counts one outer cycle and the solve ends at maxOuter of them, so this loop is bounded
-    for (int cycle = 0; cycle <= a.maxOuter + 1; ++cycle) {
-        int state = 0;
-        NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
-        NSF_CUDA(cudaStreamSynchronize(s));
-        if (state != kLoopInner) return;
-        launch(inner, ws.gridInner, 0);
-        launch((const void*)pcg_mixed_refresh_kernel, ws.grid, kRingBytes);
-    }
-    throw Error{NSF_ERR_CUDA, "preconditioned solve did not finish within its refresh budget"};
+    const void* inner1024 = a.f.colours < 2 ? nullptr
+                            : c16           ? (const void*)pcg_mixed_inner_kernel_cta1024<true>
+                                            : (const void*)pcg_mixed_inner_kernel_cta1024<false>;
+    const void* inner256 = c16 ? (const void*)pcg_mixed_inner_kernel<true> : (const void*)pcg_mixed_inner_kernel<false>;
+    split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner1024, inner256, s);
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.

@@ -260,6 +260,7 @@ struct CgWorkspace {
     int grid = 0;            // persistent grid size (blocks)
     int block = 0;
     int gridInner = 0;       // grid of the split mixed PCG's inner-iteration kernel
+    int gridInner1024 = 0;   // (its one-CTA-per-SM form)
 };
 
 // launch helpers implemented in nsf_cg.cu / nsf_sparse.cu

@@ -711,7 +711,8 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
     pcg_loop_store(t, a, L);
 }
 
-template <bool C16 = false>
+// (FusedOnly: the caller guarantees two or more colours; the one-colour loop and its CSR staging are left out.)
+template <bool C16 = false, bool FusedOnly = false>
 static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
     int where = 400;
     // the fields the inner iterations read or write (the rest of the state stays in memory)
@@ -725,8 +726,10 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.itRef = G.itRef;
     L.flip = G.flip;
     L.rflip = G.rflip;
-    const bool ok = a.f.colours >= 2 ? pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where)
-                                     : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
+    bool ok;
+    if constexpr (FusedOnly) ok = pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where);
+    else ok = a.f.colours >= 2 ? pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where)
+                               : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
     if (t.rank == 0 && threadIdx.x == 0) {
         a.loop->rz = L.rz;

@@ -12,8 +12,9 @@ constexpr int kStage = 128;   // staged (value, gathered x) pairs per warp
 constexpr int kMaxInnerBetweenRefresh = 4000;   // mixed precision: FP32 iterations between FP64 true residuals
 constexpr int kRows = 4;      // rows per thread with their loads in flight in the vector phases
 constexpr int kRowsLean = 2;  // (the kernels that run at 4 CTAs per SM)
-// reduction slots of a CG kernel's shared memory: [0, 16) block_sum, [16, 32) spare, 32 grid_sum, 33 block_scalar
-constexpr int kSmemSlots = 34;
+// reduction slots of a CG kernel's shared memory: [0, 32) block_sum (one per warp), 32 grid_sum, 33 block_scalar,
+// 34-35 a Decision (decision_put / decision_get)
+constexpr int kSmemSlots = 36;
 
 // Shared memory of a CG kernel: reduction slots and the warp-chunked CSR product's staging area (the ring
 // kernels stage in their ring memory instead, NSF_RING_SHARED).
@@ -123,11 +124,9 @@ __device__ __forceinline__ void df_acc(float& hi, float& lo, float a, float b) {
     lo = __fadd_rn(lo, __fadd_rn(se, pe));
 }
 
-// block_sum of a double-float pair (hi + lo, the FP32 dot accumulators): the warp stage adds pairs in FP32
-// (Knuth's two-sum), so only one lane per warp and thread 0 touch the FP64 pipe, which on GB300 is too narrow for
-// per-thread scalar work.  Result valid in thread 0; fixed order -> deterministic.
-static __device__ double block_sum_df(float hi, float lo, double* smem) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// hi + lo += (bh + bl) over the warp's lanes by xor shuffles: the double-float sum of the 32 lanes' pairs, the
+// same in every lane (Knuth's two-sum on FP32 operations, fixed order).
+__device__ __forceinline__ void warp_sum_df(float& hi, float& lo) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float bh = __shfl_xor_sync(0xffffffffu, hi, o);
@@ -138,11 +137,27 @@ static __device__ double block_sum_df(float hi, float lo, double* smem) {
         hi = sh;
         lo = __fadd_rn(__fadd_rn(lo, bl), e);
     }
-    if (lane == 0) smem[warp] = (double)hi + (double)lo;
+}
+
+// block_sum of a double-float pair (hi + lo, the FP32 dot accumulators): both stages (lanes, then the warps'
+// pairs in warp 0) add pairs in FP32 with two-sums, so the FP64 pipe, which on GB300 is too narrow for per-thread
+// scalar work, sees one conversion per block.  Result valid in thread 0; fixed order -> deterministic.
+static __device__ double block_sum_df(float hi, float lo, double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* pair = reinterpret_cast<float*>(smem);   // warp w: (hi, lo) at 2w, 2w + 1 (slots [0, 32))
+    warp_sum_df(hi, lo);
+    if (lane == 0) {
+        pair[2 * warp] = hi;
+        pair[2 * warp + 1] = lo;
+    }
     __syncthreads();
     double t = 0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += smem[w];
+    if (warp == 0) {
+        const bool in = lane < (int)(blockDim.x >> 5);
+        float h = in ? pair[2 * lane] : 0.f, l = in ? pair[2 * lane + 1] : 0.f;
+        warp_sum_df(h, l);
+        if (lane == 0) t = (double)h + (double)l;
+    }
     __syncthreads();
     return t;
 }
@@ -166,6 +181,42 @@ static __device__ double grid_sum(const double* part, int G, double* smem) {
     const double t = smem[32];
     __syncthreads();
     return t;
+}
+
+// A decision of thread 0 handed to every thread of the block: an FP32 coefficient and a code.  The FP32
+// iteration loops use them so that their FP64 state and tests live in thread 0 alone: GB300's FP64 pipe
+// retires about 2 lanes per cycle per SM, so a per-thread FP64 test costs 16 cycles per warp.
+struct Decision {
+    float v;
+    int code;
+};
+
+// The sum of the team's per-CTA partials as grid_sum forms it, valid in thread 0 only (no broadcast).
+static __device__ double grid_sum0(const double* part, int G) {
+    double v = 0.0;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double p[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[k] = lane + 32 * k < G ? ld_cg(part + lane + 32 * k) : 0.0;
+        v = (p[0] + p[1]) + (p[2] + p[3]);
+        for (int i = lane + 128; i < G; i += 32) v += ld_cg(part + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// Thread 0 posts a decision (decision_put); every thread of the block receives it (decision_get).
+__device__ __forceinline__ void decision_put(double* smem, float v, int code) {
+    reinterpret_cast<float*>(smem + 34)[0] = v;
+    reinterpret_cast<int*>(smem + 35)[0] = code;
+}
+__device__ __forceinline__ Decision decision_get(double* smem) {
+    __syncthreads();
+    const Decision d{reinterpret_cast<const float*>(smem + 34)[0], reinterpret_cast<const int*>(smem + 35)[0]};
+    __syncthreads();
+    return d;
 }
 
 // f() evaluated once by thread 0 and handed to every thread of the block (scalar FP64 work such as the CG

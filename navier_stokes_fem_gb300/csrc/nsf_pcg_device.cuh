@@ -502,9 +502,11 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
     float* w = F.w32;
     const float* dinv = F.dinv32;
     L.innerBreakdown = 0;
+    // The tests on p.q and r.r and the coefficient alpha are thread 0's, handed to every thread as decisions; the
+    // r.z test and beta stay per thread (thread 0 alone owning them made the 64-register kernel spill).
     const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
+    float betaf = (float)L.beta;
     while (L.it < a.maxIt) {
-        const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
         float* pc = L.flip ? a.p32a : a.p32b;
         const float* rOld = L.rflip ? a.r32b : a.r32;
@@ -522,9 +524,16 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;
-        const double pqs = grid_sum(a.partials, G, smem);
-        if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
-        const float alphaf = (float)block_scalar(smem, [&] { return L.rz / pqs; });
+        {
+            const double pqs = grid_sum0(a.partials, G);
+            if (threadIdx.x == 0) {
+                const bool bad = !(pqs > 0.0) || isinf(pqs);
+                decision_put(smem, bad ? 0.f : (float)(L.rz / pqs), bad);
+            }
+        }
+        const Decision da = decision_get(smem);
+        if (da.code) { L.innerBreakdown = 1; break; }
+        const float alphaf = da.v;
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
         // colours other than 1: d += alpha p, r -= alpha q; colour 0 also y0 = r / L_00
@@ -590,12 +599,16 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         const double rrn = block_sum_df(rrHi, rrLo, smem);
         if (threadIdx.x == 0) a.partials[G + t.rank] = rrn;
         if (!t.barrier(where++)) return false;
-        const double rrs = grid_sum(a.partials + G, G, smem);
+        {
+            const double rrs = grid_sum0(a.partials + G, G);
+            if (threadIdx.x == 0) decision_put(smem, 0.f, !(rrs == rrs) || isinf(rrs) ? 1 : rrs <= rrStop ? 2 : 0);
+        }
+        const Decision dr = decision_get(smem);
         ++L.it;
         L.flip ^= 1;
         L.rflip ^= 1;
-        if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
-        if (rrs <= rrStop) break;   // time for a true residual
+        if (dr.code == 1) { L.innerBreakdown = 1; break; }
+        if (dr.code == 2) break;   // time for a true residual
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
         double rzs = 0;
         if (!precond_sweeps<float, float, true, C16>(t, a, rNew, w, F.loVal32, F.upVal32, dinv, rzn, smem, where,
@@ -604,6 +617,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
         L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
         L.rz = rzs;
+        betaf = (float)L.beta;
     }
     L.state = kLoopRefresh;
     return true;

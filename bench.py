@@ -350,9 +350,9 @@ def nonzeros(sim, slot):
 
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
-# 4,198,401 rows, whose vectors exceed L2): pcg_mixed_inner_kernel 16.94 GB over 40 iterations (16-bit column
-# copies), cg_fp64_kernel 30.67 GB over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 100.9, "cg_fp64_kernel": 121.7}
+# 4,198,401 rows, whose vectors exceed L2): the mixed PCG's inner kernel (one 1024-thread CTA per SM, 16-bit column
+# copies) 17.49 GB over 40 iterations, cg_fp64_kernel 30.67 GB over 60 iterations (its prologue included).
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 104.1, "cg_fp64_kernel": 121.7}
 
 
 def roofline(sim, arm, args):

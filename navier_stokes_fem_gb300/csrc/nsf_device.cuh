@@ -805,6 +805,10 @@ __device__ __forceinline__ void product32(SellRing* ring, const CgArgs& a, int r
 // entries per lane and chunk of the FP64 residual and right-hand-side passes: 4 in the narrow kernels (register
 // budget), 8 in the wide ones (P2 rows of 9 and 19 entries take 2 and 3 chunks instead of 3 and 5)
 template <bool Wide> constexpr int kResidU = Wide ? 8 : 4;
+// chunk of the FP32 product of a wide system in the mixed CG's iterations: the P2 rows of these meshes have 9
+// entries (edge midpoints, three quarters of the rows) or 19 (vertices), one and two chunks of 10 instead of two
+// and three of 8, and a chunk is a memory latency (12 spills at 64 registers)
+constexpr int kWideChunk32 = 10;
 
 static __device__ void write_info(const Team& t, const CgArgs& a, int it, int status, int outer, double rr, double bb) {
     if (t.rank == 0 && threadIdx.x == 0) {
@@ -1090,7 +1094,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
                 }
             }
             if (!t.barrier(where++)) return false;
-            product32<Wide>(ring, a, rb, re, stage32, [&](int c) { return pc[c]; },
+            product32<Wide, kWideChunk32>(ring, a, rb, re, stage32, [&](int c) { return pc[c]; },
                             [&](int row, float acc, float pi) {
                                 a.q32[row] = acc;
                                 df_acc(pqHi, pqLo, pi, acc);

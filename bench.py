@@ -352,13 +352,14 @@ def nonzeros(sim, slot):
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
 # 4,198,401 rows, whose vectors exceed L2): the mixed PCG's inner kernel (one 1024-thread CTA per SM, 16-bit column
 # copies) 17.49 GB over 40 iterations, cg_fp64_kernel 30.67 GB over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel": 104.1, "cg_fp64_kernel": 121.7}
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_cta1024": 104.1, "cg_fp64_kernel": 121.7}
 
 
 def roofline(sim, arm, args):
     """Algorithmic bytes over every persistent solve of the timed steps / their summed kernel time.  A mixed PCG
-    solve of a narrow system runs as a refresh kernel and inner-iteration kernels; the inner kernel takes over 99%
-    of its time, and the solve is reported under that kernel's name."""
+    solve of a narrow system runs as a refresh kernel and inner-iteration kernels; the inner kernel (one
+    1024-thread CTA per SM on two or more colours) takes over 99% of its time, and the solve is reported under
+    that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
     nzl, idx = {}, {}
@@ -366,7 +367,7 @@ def roofline(sim, arm, args):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
-    names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel", 2: "pcg_mixed_inner_kernel", 3: "pcg_fp64_kernel"}
+    names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel", 2: "pcg_mixed_inner_kernel_cta1024", 3: "pcg_fp64_kernel"}
     bytes_by, ms_by, rowit_by = {}, {}, {}
     for sl, m_, n_, i_, o_, t_ in zip(prof["slot"], prof["mode"], prof["rows"], prof["iterations"], prof["outer"],
                                       prof["ms"]):

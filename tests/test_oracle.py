@@ -87,6 +87,52 @@ def test_cavity_pattern_counts():
         assert o.matrix("pressure_stiffness")[1].size == 7 * n * n + 6 * n + 1
 
 
+def test_manufactured_poisson_solutions_converge_at_the_element_orders():
+    """-lap u = f on the unit square with u = sin(pi x) sin(pi y), u = 0 on the boundary, assembled by the oracle:
+    P2 (stiffness = (diffusion - mass) / (dt nu), load = M f) and P1 (the pressure stiffness, load = the P1
+    vertex rows of M f summed from the P2 mass, which integrates f against the P1 hat functions exactly for P2
+    data).  The nodal errors fall with h at the elements' orders: h^2 for P1 and, at the nodes of this uniform
+    mesh, h^4 for P2 (superconvergent; h^3 in general)."""
+    import scipy.sparse.linalg as spla
+
+    err2, err1 = [], []
+    for n in (8, 16, 32):
+        m = M.cavity(n)
+        m.u_dirichlet, m.p_dirichlet = [], []
+        o = oracle.Oracle(m, 1.0, 1.0)                      # diffusion = M + 1 * 1 * K
+        Mm, D, K1 = (o.scipy_matrix(k).tocsr() for k in ("velocity_mass", "diffusion", "pressure_stiffness"))
+        K2 = (D - Mm).tocsr()
+        xy = m.nodes.astype(np.float64)
+        u = np.sin(np.pi * xy[:, 0]) * np.sin(np.pi * xy[:, 1])
+        on_b = (np.abs(xy[:, 0]) < 1e-12) | (np.abs(xy[:, 0] - 1) < 1e-12) | \
+               (np.abs(xy[:, 1]) < 1e-12) | (np.abs(xy[:, 1] - 1) < 1e-12)
+        b2 = Mm @ (2 * np.pi ** 2 * u)
+        free = np.flatnonzero(~on_b)
+        uh = np.zeros_like(u)
+        uh[free] = spla.spsolve(K2[free][:, free].tocsc(), b2[free])
+        err2.append(np.abs(uh - u).max())
+        # P1 on the vertices: the P1 hat of vertex i is its P2 vertex function plus half of each adjacent
+        # midside function, so the P1 load is (M f)_i + half the load of the midside nodes around it
+        P = m.n_pressure
+        el = m.elements
+        b1 = b2[:P].copy()
+        mids = {}   # midside node -> its edge's vertices (element node order [v0, v1, v2, m12, m02, m01])
+        for e in el:
+            for (i, j, k) in ((e[1], e[2], e[3]), (e[0], e[2], e[4]), (e[0], e[1], e[5])):
+                mids[int(k)] = (int(i), int(j))
+        for k, (i, j) in mids.items():
+            b1[i] += 0.5 * b2[k]
+            b1[j] += 0.5 * b2[k]
+        free1 = np.flatnonzero(~on_b[:P])
+        ph = np.zeros(P)
+        ph[free1] = spla.spsolve(K1[free1][:, free1].tocsc(), b1[free1])
+        err1.append(np.abs(ph - u[:P]).max())
+    r2 = np.log2(np.array(err2[:-1]) / np.array(err2[1:]))
+    r1 = np.log2(np.array(err1[:-1]) / np.array(err1[1:]))
+    assert err2[-1] < 1e-6 and (r2 > 3.5).all(), (err2, r2)   # measured 3.88, 3.96
+    assert err1[-1] < 1e-3 and (r1 > 1.9).all(), (err1, r1)   # measured 2.00, 2.00
+
+
 def test_dirichlet_elimination_structure():
     m = M.cavity(8)
     o = oracle.Oracle(m, 0.01, 0.01)

@@ -133,6 +133,24 @@ def test_manufactured_poisson_solutions_converge_at_the_element_orders():
     assert err1[-1] < 1e-3 and (r1 > 1.9).all(), (err1, r1)   # measured 2.00, 2.00
 
 
+def test_divergence_and_gradient_scalings_on_linear_fields():
+    """The step's operators carry the reference's scalings (include/assembly.h:1302-1475): B = -(1/dt) div and
+    Bp = -dt grad.  With the shape functions summing to one, sum_i (B (x, y))_i = -(1/dt) * 2 * area and
+    sum_j (Bp x)_j = -dt * area in the x block and 0 in the y block (unit square)."""
+    m = M.cavity(8)
+    m.u_dirichlet, m.p_dirichlet = [], []
+    dt = 0.1
+    o = oracle.Oracle(m, 0.5, dt)
+    B, G = o.scipy_matrix("velocity_divergence"), o.scipy_matrix("pressure_divergence")
+    xy = m.nodes.astype(np.float64)
+    nv, P = m.n_nodes, m.n_pressure
+    assert B.shape == (P, 2 * nv) and G.shape == (2 * nv, P)      # y block at column / row offset Nv
+    assert abs((B @ np.concatenate([xy[:, 0], xy[:, 1]])).sum() + 2 / dt) < 1e-11
+    assert abs((B @ np.concatenate([xy[:, 0], 0 * xy[:, 1]])).sum() + 1 / dt) < 1e-11
+    g = G @ xy[:P, 0]
+    assert abs(g[:nv].sum() + dt) < 1e-14 and abs(g[nv:].sum()) < 1e-14
+
+
 def test_advection_reproduces_quadratic_fields_exactly():
     """Semi-Lagrangian self-advection of u = y^2, v = x^2 (both in the P2 space): the departure point of node x is
     x - dt (u, v), and P2 interpolation there reproduces the quadratics, so the new fields are (y - dt x^2)^2 and

@@ -181,6 +181,14 @@ def test_dirichlet_elimination_structure():
     assert abs(D[free][:, bc]).max() == 0
     W = o.scipy_matrix("velocity_dirichlet_weights")      # transposed storage: row = Dirichlet node
     assert set(np.unique(W.tocoo().row)).issubset(set(bc))
+    # the values: the free block is the raw operator's, and W holds the raw couplings of the free rows to the
+    # Dirichlet columns, so D_e x = b_e with b_e[free] = b[free] - (W^T g)[free] is the raw system with x[bc] = g
+    m2 = M.cavity(8)
+    m2.u_dirichlet, m2.p_dirichlet = [], []
+    Dr = oracle.Oracle(m2, 0.01, 0.01).scipy_matrix("diffusion").tocsr()
+    W = W.tocsr()
+    assert abs(D[free][:, free] - Dr[free][:, free]).max() == 0
+    assert abs(W[bc][:, free] - Dr[free][:, bc].T).max() == 0
 
 
 def test_cg_oracle_relative_residual():

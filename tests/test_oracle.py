@@ -151,6 +151,21 @@ def test_divergence_and_gradient_scalings_on_linear_fields():
     assert abs(g[:nv].sum() + dt) < 1e-14 and abs(g[nv:].sum()) < 1e-14
 
 
+def test_uniform_flow_is_a_steady_state_of_the_step():
+    """u = (1, 0) with the same Dirichlet data on every wall: advection moves a constant to itself, the diffusion
+    solve returns it (the stiffness annihilates constants), its divergence is zero so the pressure stays 0 and the
+    projection changes nothing.  Three operator-split steps keep it to rounding."""
+    m = M.cavity(8)
+    m.u_dirichlet = [(g[0], "1", "0") for g in m.u_dirichlet]
+    o = oracle.Oracle(m, 0.01, 0.05)
+    nv = m.n_nodes
+    o.set_fields(np.concatenate([np.ones(nv), np.zeros(nv)]), np.zeros(m.n_pressure))
+    st, _ = o.step(3)
+    uv, p = o.fields()
+    assert st == 0
+    assert np.abs(uv[:nv] - 1).max() < 1e-12 and np.abs(uv[nv:]).max() < 1e-12 and np.abs(p).max() < 1e-12
+
+
 def test_advection_reproduces_quadratic_fields_exactly():
     """Semi-Lagrangian self-advection of u = y^2, v = x^2 (both in the P2 space): the departure point of node x is
     x - dt (u, v), and P2 interpolation there reproduces the quadratics, so the new fields are (y - dt x^2)^2 and

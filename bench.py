@@ -5,15 +5,18 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--solver S] [--precond P] [--impl reference]
 
 The default line is the metric's method on the 2048 x 2048 cavity: mixed-precision PCG with the learned
-preconditioner (trained on the GPU during set-up, untimed), with the plain FP64 CG megakernel timed on the same
-workload in the same run ("plain_fp64_cg").
+preconditioner (trained on the GPU during set-up, untimed); in the same run, over the same steps, the same method
+with IC(0) in place of the learned factor ("ic0_pcg_mixed") and the plain FP64 CG megakernel ("plain_fp64_cg").
 
 A step is one pass of the hot path over the resident fields: advection, two diffusion solves, the pressure solve,
 the gradient product and two mass solves (NavierStokesAssembly::semiLagrangianSolve's loop body,
-include/assembly.h:1516-1556).  `value` is device time per step (CUDA events on the library's stream) with the
-fields resident in HBM; `e2e` is the same step through the C ABI with host fields copied in and out every step.
-`--impl reference` times the CPU oracle (the restated reference path; the reference's own CPU CG lives in an absent
-submodule) on the same workload with every host thread.
+include/assembly.h:1516-1556).  Every arm times steps 1..K of the run from its initial state (u = 0 with the
+Dirichlet values, p = 0), after W warm-up steps whose fields are dropped.  `value` is device time per step (CUDA
+events on the library's stream) with the fields resident in HBM; `e2e` is the same steps through the C ABI with host
+fields copied in and out every step.  `field_check` compares the fields the fast arms end with against the plain
+FP64 arm's; `oracle_check` compares the GPU FP64 step 1 with the FP64 oracle's step 1, which is also the timed CPU
+baseline.  `--impl reference` times whole steps of the CPU oracle (the restated reference path; the reference's own
+CPU CG lives in an absent submodule) on the same workload with every host thread.
 """
 from __future__ import annotations
 
@@ -163,36 +166,11 @@ def max_over_ranks(pg, v):
     return float(t.item())
 
 
-FULL_STEP_LIMIT = 2_000_000     # velocity nodes up to which the CPU oracle runs whole steps
-
-
-def oracle_step_model(o, mesh, iterations_per_step, sample_its=30):
-    """CPU time of one operator-split step of the FP64 oracle, from a bounded sample: one full advection pass plus
-    `sample_its` CG iterations on each system, scaled by the per-step iteration counts (CG time is linear in the
-    iteration count; the right-hand-side products cost about one iteration each).  Returns ms."""
-    rng = np.random.default_rng(1)
-    x, y = mesh.nodes[:, 0].astype(np.float64), mesh.nodes[:, 1].astype(np.float64)
-    u, v = np.sin(np.pi * y) * 0.5, -np.sin(np.pi * x) * 0.5
-    t0 = time.perf_counter()
-    o.advect(u, v)
-    t_adv = time.perf_counter() - t0
-    per_it = {}
-    for name in ("diffusion", "pressure_stiffness", "velocity_mass"):
-        n = mesh.n_pressure if name == "pressure_stiffness" else mesh.n_nodes
-        b = rng.standard_normal(n)
-        t0 = time.perf_counter()
-        o.cg(name, b, np.zeros(n), max_iter=sample_its, tol=1e-30)
-        per_it[name] = (time.perf_counter() - t0) / (sample_its + 1)
-    its = np.asarray(iterations_per_step, np.float64)
-    solve = (its[0] + its[1] + 2) * per_it["diffusion"] + (its[2] + 1) * per_it["pressure_stiffness"] + \
-        (its[3] + its[4] + 2) * per_it["velocity_mass"]
-    return 1e3 * (t_adv + solve)
-
-
-def cpu_baseline(mesh, w, sample_steps, iterations_per_step=None, threads=None):
-    """The FP64 oracle on the host cores.  Meshes up to FULL_STEP_LIMIT velocity nodes: `sample_steps` whole steps
-    timed.  Larger meshes: the bounded per-iteration sample of oracle_step_model, scaled by the GPU run's
-    measured iteration counts (the oracle runs the same CG)."""
+def cpu_oracle_steps(mesh, w, timed_steps, budget_s=None, threads=None):
+    """The FP64 oracle (the restated reference path) on the host cores: whole operator-split steps 1, 2, ... of the
+    run from its initial state, each timed - up to `timed_steps` of them, fewer when the next step would take the
+    timed steps past `budget_s` seconds, but at least one.  Returns the per-step times and iteration counts, the
+    set-up time, and the fields after step 1 (for the GPU FP64 comparison)."""
     import oracle
 
     oracle.build(ref=False)
@@ -202,18 +180,20 @@ def cpu_baseline(mesh, w, sample_steps, iterations_per_step=None, threads=None):
     t0 = time.perf_counter()
     o = oracle.Oracle(mesh, w["nu"], w["dt"])
     setup = time.perf_counter() - t0
-    if mesh.n_nodes <= FULL_STEP_LIMIT or iterations_per_step is None:
+    times, its, f1, status = [], [], None, 0
+    while len(times) < max(1, timed_steps):
         t0 = time.perf_counter()
-        st, it = o.step(sample_steps)
-        ms = 1e3 * (time.perf_counter() - t0) / sample_steps
-        sample = f"FP64 oracle, first {sample_steps} step(s) of the same workload (setup {setup:.1f} s excluded)"
-    else:
-        ms = oracle_step_model(o, mesh, iterations_per_step)
-        sample = ("FP64 oracle on the full-size matrices: one advection pass and 30 CG iterations per system, "
-                  f"scaled by the per-step iteration counts {np.round(iterations_per_step, 1).tolist()} "
-                  f"(setup {setup:.1f} s excluded)")
+        st, it = o.step(1)
+        times.append(time.perf_counter() - t0)
+        its.append(it[0].tolist())
+        status = status or int(st)
+        if f1 is None:
+            f1 = o.fields()
+        if budget_s is not None and sum(times) + times[-1] > budget_s:
+            break
     o.close()
-    return {"ms_per_step": ms, "cores": cores, "setup_s": setup, "sample": sample}
+    return {"times_s": times, "ms_per_step": 1e3 * sum(times) / len(times), "iterations": its, "setup_s": setup,
+            "cores": cores, "status": status, "fields_1": f1}
 
 
 def run_reference(args):
@@ -227,27 +207,28 @@ def run_reference(args):
     oracle.build(ref=False)
     cores = oracle.max_threads()
     if w["kind"] == "batched":
-        # every 8th instance is stepped (a bounded sample); the per-step time is scaled to all instances
+        # every instance's whole step on the host (one oracle per instance, instances one after another, each
+        # using every host thread): one untimed step, then timed steps within the time budget
         probs = batched_problems(w)
-        sample = probs[::8]
-        oracles = [oracle.Oracle(m, nu, dt) for m, nu, dt in sample]
-        for o in oracles:
-            o.step(args.warmup)
+        oracles = [oracle.Oracle(m, nu, dt) for m, nu, dt in probs]
         times, its = [], []
-        for _ in range(args.steps):
+        while len(times) < max(1, args.steps):
             t0 = time.perf_counter()
             per = [o.step(1)[1][0] for o in oracles]
-            times.append((time.perf_counter() - t0) * len(probs) / len(sample))
-            its.append(np.sum(per, axis=0) * len(probs) / len(sample))
+            times.append(time.perf_counter() - t0)
+            its.append(np.sum(per, axis=0))
+            if sum(times) + times[-1] > args.ref_budget_s:
+                break
         for o in oracles:
             o.close()
-        mesh = probs[0][0]
-        sample_txt = (f"every 8th instance ({len(sample)} of {len(probs)}) stepped, time scaled by "
-                      f"{len(probs)}/{len(sample)}; {args.steps} timed steps after {args.warmup} warm-up steps")
-        ms = 1e3 * sum(times) / len(times)
+        k = len(times)
+        sample_txt = (f"all {len(probs)} instances stepped whole on the host; steps 1..{k} from the initial state "
+                      f"timed ({args.steps} requested, time budget {args.ref_budget_s:.0f} s)")
+        ms = 1e3 * sum(times) / k
         line = {
             "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+            "steps": k, "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "instances": len(probs), "solver": "fp64 CG (CPU oracle)"},
             "cg_iterations_per_step": np.mean(its, axis=0).round(1).tolist(),
@@ -259,37 +240,28 @@ def run_reference(args):
         barrier(pg)
         return
     mesh = make_mesh(w)
-    o = oracle.Oracle(mesh, w["nu"], w["dt"])
-    times, its = [], []
-    if mesh.n_nodes <= FULL_STEP_LIMIT:
-        st, _ = o.step(args.warmup)
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            st, it = o.step(1)
-            times.append(time.perf_counter() - t0)
-            its.append(it[0])
-        sample_txt = f"{args.steps} timed steps after {args.warmup} warm-up steps of the full workload"
-    else:
-        # one whole step gives the per-solve iteration counts; every timed step is then the bounded sample of
-        # oracle_step_model (one advection pass, 30 CG iterations per system) scaled by those counts
-        st, it = o.step(1)
-        for _ in range(args.steps):
-            times.append(oracle_step_model(o, mesh, it[0]) / 1e3)
-            its.append(it[0])
-        sample_txt = ("one whole step (untimed) for the iteration counts, then per timed step one advection pass "
-                      "and 30 CG iterations per system on the full-size matrices, scaled by those counts")
-    ms = 1e3 * sum(times) / len(times)
+    # whole steps from rest: one untimed step, then timed whole steps - all args.steps of them when they fit the
+    # arm's time budget, else as many as fit (at least one); `steps` reports the number actually timed
+    cpu = cpu_oracle_steps(mesh, w, args.steps, budget_s=args.ref_budget_s)
+    k = len(cpu["times_s"])
+    ms = cpu["ms_per_step"]
+    sample_txt = (f"whole FP64 oracle steps 1..{k} of the run from its initial state, each timed ({args.steps} "
+                  f"requested, time budget {args.ref_budget_s:.0f} s; no warm-up is needed on the host); set-up "
+                  f"{cpu['setup_s']:.1f} s excluded; all {cpu['cores']} host threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "steps": k, "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_block(args, w, mesh, solver="fp64 CG (CPU oracle)"),
-        "cg_iterations_per_step": np.mean(its, axis=0).round(1).tolist() if its else None,
-        "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": cores, "kind": "port",
+        "cg_iterations_per_step": np.mean(cpu["iterations"], axis=0).round(1).tolist(),
+        "cg_iterations_each_step": cpu["iterations"],
+        "step_times_s": [round(t, 3) for t in cpu["times_s"]],
+        "oracle_status": cpu["status"],
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": cpu["cores"], "kind": "port",
                          "sample": sample_txt},
         "e2e": {"value": round(ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    o.close()
     print(json.dumps(line), flush=True)
     barrier(pg)
 
@@ -313,13 +285,17 @@ def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4):
     return (outer + 1) * refresh + its * it_bytes
 
 
-def time_arm(sim, args, pg):
+def time_arm(sim, args, pg, start=None):
     """Warm-up steps, then args.steps timed steps (CUDA events on the library's stream, L2 flushed in between)
-    with every persistent solve recorded; returns the measurements and the fields the timed steps started from."""
+    with every persistent solve recorded; returns the measurements, the fields the timed steps started from and
+    the fields they ended with.  With `start` (uv, p) the timed steps start from those fields instead of the
+    warm-up's, so that several arms time the same steps."""
     for _ in range(args.warmup):
         sim.flush_l2(256 << 20)
         sim.step(1)
     sim.synchronize()
+    if start is not None:
+        sim.set_fields(*start)
     start_fields = sim.fields()
     clocks = ClockSampler()
     clocks.start()
@@ -340,7 +316,26 @@ def time_arm(sim, args, pg):
     prof = sim.profile_read()
     sim.profile(False)
     return {"ms": max_over_ranks(pg, ms_total / args.steps), "its": np.asarray(its), "prof": prof,
-            "launches": launches, "clocks": clk, "start_fields": start_fields}
+            "launches": launches, "clocks": clk, "start_fields": start_fields, "end_fields": sim.fields()}
+
+
+# Field agreement after the timed steps between the fast method and the plain FP64 CG (both stop every solve at a
+# 1e-8 relative residual, so their solutions may differ by up to about cond(A) * 1e-8 per solve; the pressure
+# system's condition number grows as h^-2), and between the GPU FP64 step and the FP64 oracle's step (the same
+# algorithm, summation order aside).
+FIELD_CHECK_TOL = {"u": 1e-5, "v": 1e-5, "p": 1e-3}
+ORACLE_FIELD_TOL = 1e-6
+
+
+def rel_l2(a, b):
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b))) / (nb if nb > 0 else 1.0)
+
+
+def field_diff(fa, fb, nv):
+    """Relative L2 differences of u, v and p between two (uv, p) field sets."""
+    (uva, pa), (uvb, pb) = fa, fb
+    return {"rel_l2_u": rel_l2(uva[:nv], uvb[:nv]), "rel_l2_v": rel_l2(uva[nv:], uvb[nv:]), "rel_l2_p": rel_l2(pa, pb)}
 
 
 def nonzeros(sim, slot):
@@ -403,6 +398,7 @@ def run_gpu(args):
     sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
                                    inner_tolerance=args.inner_tol)
     setup_s = time.perf_counter() - t0
+    init = sim.fields()        # the run's initial state: u = 0 with the Dirichlet values imposed, p = 0
     learned = None
     t0 = time.perf_counter()
     if args.precond == "ic0":
@@ -418,17 +414,20 @@ def run_gpu(args):
         learner.close()
         trainer.close()
     precond_s = time.perf_counter() - t0
-    arm = time_arm(sim, args, pg)
+    # every arm times steps 1..K of the run from the initial state, after warm-up steps whose fields are dropped
+    arm = time_arm(sim, args, pg, start=init)
     ms, its, clk, launches = arm["ms"], arm["its"], arm["clocks"], arm["launches"]
     roof = roofline(sim, arm, args)
     prof = arm["prof"]
     mixed = (prof["mode"] == 1) | (prof["mode"] == 2)
     mixed_stats = {"mixed_solves": int(mixed.sum()), "finished_in_fp64": int((prof["fallback"] == 1).sum()),
                    "mean_fp64_refreshes": round(float(prof["outer"][mixed].mean()), 2) if mixed.any() else 0}
+    start = arm["start_fields"]
+    nv = mesh.n_nodes
 
     # end to end through the C ABI: host fields copied in and out around every step (pinned buffers), over the
     # same steps as the timed region (from the fields it started with)
-    uv, p = arm["start_fields"]
+    uv, p = start
     uv_in, p_in = sim.pinned(uv.shape), sim.pinned(p.shape)
     uv_out, p_out = sim.pinned(uv.shape), sim.pinned(p.shape)
     uv_in[:] = uv
@@ -442,22 +441,59 @@ def run_gpu(args):
         p_in, p_out = p_out, p_in
     e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / e2e_steps)
     field_bytes = int(uv.nbytes + p.nbytes)
+    e2e_same = bool(np.array_equal(uv_in, arm["end_fields"][0]) and np.array_equal(p_in, arm["end_fields"][1]))
+
+    # the classical preconditioner on the same handle, solver and steps: IC(0) in place of the learned factor
+    ic0 = None
+    if args.precond == "learned" and args.ic0_arm:
+        sim.precond_ic0("pressure_stiffness")
+        iarm = time_arm(sim, args, pg, start=start)
+        ic0 = {"ms_per_step": round(iarm["ms"], 3), "cg_iterations_per_step": iarm["its"].mean(axis=0).round(1).tolist(),
+               "learned_speedup_over_ic0": round(iarm["ms"] / ms, 3), "clocks": iarm["clocks"],
+               "end_fields": iarm["end_fields"]}
     sim.close()
 
-    # the plain FP64 CG megakernel on the same workload and steps, in the same process (the comparison the metric
-    # names); its own warm-up steps are not timed
-    plain = None
+    # the plain FP64 CG megakernel on the same workload, from the same start fields, over the same steps (the
+    # comparison the metric names); its own warm-up steps are not timed
+    plain, plain_sim, field_check = None, None, None
     if args.compare and not (args.solver == "fp64" and args.precond == "none"):
-        ref = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver="fp64")
-        parm = time_arm(ref, args, pg)
-        ref.close()
+        plain_sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver="fp64")
+        parm = time_arm(plain_sim, args, pg, start=start)
         plain = {"ms_per_step": round(parm["ms"], 3), "cg_iterations_per_step": parm["its"].mean(axis=0).round(1).tolist(),
                  "speedup": round(parm["ms"] / ms, 3), "clocks": parm["clocks"]}
+        # both arms ran the same steps from the same fields: how far apart are the fields they ended with
+        tol = FIELD_CHECK_TOL
+        res = {"learned_pcg_mixed" if args.precond == "learned" else args.solver:
+               field_diff(arm["end_fields"], parm["end_fields"], nv)}
+        if ic0 is not None:
+            res["ic0_pcg_mixed"] = field_diff(ic0["end_fields"], parm["end_fields"], nv)
+        ok = all(d["rel_l2_u"] <= tol["u"] and d["rel_l2_v"] <= tol["v"] and d["rel_l2_p"] <= tol["p"]
+                 for d in res.values())
+        field_check = {"against": "plain FP64 CG, the same steps 1..K from the initial state", "steps": args.steps,
+                       "tol": tol, "pass": ok, **res}
+    if ic0 is not None:
+        ic0.pop("end_fields")
 
-    base = None
+    base, oracle_check = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        base = cpu_baseline(mesh, w, args.cpu_steps, iterations_per_step=(plain["cg_iterations_per_step"] if plain
-                                                                           else its.mean(axis=0)))
+        cpu = cpu_oracle_steps(mesh, w, args.cpu_steps)
+        k = len(cpu["times_s"])
+        base = {"value": round(cpu["ms_per_step"], 3), "unit": "ms/step", "cores": cpu["cores"], "kind": "port",
+                "sample": (f"whole FP64 oracle step(s) 1..{k} of the run from its initial state (the GPU arms time "
+                           f"steps 1..{args.steps} of the same run); set-up {cpu['setup_s']:.1f} s excluded; "
+                           f"iterations {cpu['iterations']}"),
+                "status": cpu["status"]}
+        # the GPU FP64 path's step 1 from the initial state against the oracle's
+        if plain_sim is None:
+            plain_sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver="fp64")
+        plain_sim.set_fields(*init)
+        git = plain_sim.step(1)[0]
+        d = field_diff(plain_sim.fields(), cpu["fields_1"], nv)
+        oracle_check = {"against": "FP64 oracle, step 1 from the initial state", "tol": ORACLE_FIELD_TOL, **d,
+                        "pass": max(d.values()) <= ORACLE_FIELD_TOL,
+                        "gpu_iterations": git.tolist(), "oracle_iterations": cpu["iterations"][0]}
+    if plain_sim is not None:
+        plain_sim.close()
     if rank != 0:
         return
     solver = args.solver + ("" if args.precond == "none" else f" + {args.precond} preconditioner")
@@ -470,19 +506,21 @@ def run_gpu(args):
         "cg_iterations_per_step": its.mean(axis=0).round(1).tolist(),
         "cg_solves": ["diffusion u", "diffusion v", "pressure", "mass u", "mass v"],
         "plain_fp64_cg": plain,
+        "ic0_pcg_mixed": ic0,
+        "field_check": field_check,
+        "oracle_check": oracle_check,
         "mixed_precision": mixed_stats if args.solver in ("mixed", "pcg_mixed") else None,
         "learned_preconditioner": learned,
         "setup_s": round(setup_s, 3),
         "preconditioner_setup_s": round(precond_s, 3),
         "roofline": roof,
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": field_bytes,
-                "d2h_bytes_per_step": field_bytes, "steps": e2e_steps},
+                "d2h_bytes_per_step": field_bytes, "steps": e2e_steps, "same_fields_as_timed_steps": e2e_same},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     if base is not None:
-        line["cpu_baseline"] = {"value": round(base["ms_per_step"], 3), "unit": "ms/step", "cores": base["cores"],
-                                "kind": "port", "sample": base["sample"]}
+        line["cpu_baseline"] = base
     print(json.dumps(line), flush=True)
 
 
@@ -555,18 +593,15 @@ def run_batched(args):
         import oracle
 
         oracle.build(ref=False)
-        sample = probs[::8]
         t_cpu = 0.0
-        for m, nu, dt in sample:
+        for m, nu, dt in probs:
             o = oracle.Oracle(m, nu, dt)
             tt = time.perf_counter()
             o.step(1)
             t_cpu += time.perf_counter() - tt
             o.close()
-        base = {"value": round(1e3 * t_cpu * len(probs) / len(sample), 3), "unit": "ms/step",
-                "cores": oracle.max_threads(), "kind": "port",
-                "sample": f"FP64 oracle, first step of every 8th instance ({len(sample)} of {len(probs)}), "
-                          f"scaled by {len(probs)}/{len(sample)}"}
+        base = {"value": round(1e3 * t_cpu, 3), "unit": "ms/step", "cores": oracle.max_threads(), "kind": "port",
+                "sample": f"FP64 oracle, step 1 from the initial state of all {len(probs)} instances"}
     b.close()
     if rank != 0:
         return
@@ -646,7 +681,11 @@ def main():
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the plain FP64 CG run on the same workload")
     ap.add_argument("--inner-tol", type=float, default=-1.0)
-    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--cpu-steps", type=int, default=1, help="whole oracle steps timed for cpu_baseline")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0,
+                    help="--impl reference: time budget of the timed whole CPU steps")
+    ap.add_argument("--no-ic0-arm", dest="ic0_arm", action="store_false",
+                    help="skip the IC(0) run beside the learned preconditioner")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cg-probe", type=int, default=0, help="profiling aid: 2 pressure solves of this many iterations")
     args = ap.parse_args()

@@ -239,10 +239,16 @@ int nsf_flush_l2(nsf_device* h, size_t bytes);
  * caller passes the CSR matrix (int32 indices, columns ascending per row), b, x0 and x in device memory it
  * owns; the solver's work vectors live in an 8 MB array compiled into the library, which every GPU that loads
  * the library holds until exit.  rows <= NSF_NOALLOC_MAX_ROWS, else NSF_ERR_BAD_ARG with a message on stderr.
+ * The matrix is square (rows x rows) with rowptr[0] = 0, rowptr ascending and 0 <= col < rows; these device
+ * arrays are not checked (unlike nsf_upload_matrix_csr), so a column index outside [0, rows) reads outside the
+ * caller's vectors.
  * The first call on each device looks up that array's device address (cudaGetSymbolAddress) with the device
- * current; make that first call before any stream capture.  Calls share the array: calls that overlap on the
+ * current and keeps it for the rest of the process; make that first call before any stream capture.  After a
+ * cudaDeviceReset (or any teardown of the device's primary context) the kept address is stale: do not call this
+ * entry point on that device again in the same process.  Calls share the array: calls that overlap on the
  * GPU (other streams or threads) race, so serialise them.  Runs on `stream` (a cudaStream_t, NULL = default)
- * and returns after the solve finished; statuses as nsf_conjugate_gradient. */
+ * and returns after the solve finished; statuses as nsf_conjugate_gradient, except that the grid-barrier time
+ * limit is fixed at 2 s (nsf_set_barrier_timeout applies to handles only). */
 #define NSF_NOALLOC_MAX_ROWS 262144
 int nsf_conjugate_gradient_noalloc(int rows, const int* rowptr_dev, const int* col_dev, const double* val_dev,
                                    const double* b_dev, const double* x0_dev, double* x_dev, int maxIterations,

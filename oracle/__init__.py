@@ -46,13 +46,15 @@ _lptr = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
 
 
 def build(ref: bool | None = None) -> None:
-    """Compile liboracle.so (and the reference tree when the reference sources are present)."""
+    """Compile liboracle.so, and the reference tree when NSFEM_REFERENCE_DIR names a reference checkout."""
     subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
-    ref_dir = os.environ.get("NSFEM_REFERENCE_DIR", "/root/reference")
+    ref_dir = os.environ.get("NSFEM_REFERENCE_DIR", "")
     if ref is None:
-        ref = os.path.isdir(os.path.join(ref_dir, "cpp"))
+        ref = bool(ref_dir) and os.path.isdir(os.path.join(ref_dir, "cpp"))
     if ref:
-        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref_dir}"], check=True)
+        if not ref_dir:
+            raise RuntimeError("set NSFEM_REFERENCE_DIR to the reference checkout to build the reference tree")
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "ref-int", f"REF={ref_dir}"], check=True)
 
 
 def lib():
@@ -74,6 +76,12 @@ def lib():
         L.orc_cg.argtypes = [_p, _i, _dptr, _dptr, _dptr, _i, _d, ctypes.POINTER(_i), ctypes.POINTER(_d)]
         L.orc_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
         L.orc_tree_size.argtypes = [_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]
+        L.orc_tree_create.restype = _p
+        L.orc_tree_create.argtypes = [_i, _fptr, _i, _iptr]
+        L.orc_tree_destroy.argtypes = [_p]
+        L.orc_tree_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
+        L.orc_tree_stats.argtypes = [_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                     ctypes.POINTER(_i)]
         L.orc_advect.argtypes = [_p, _dptr, _dptr, _dptr, _dptr]
         L.orc_step.restype = _i
         L.orc_step.argtypes = [_p, _i, _iptr]
@@ -96,22 +104,29 @@ def lib():
     return _LIB
 
 
-def ref_available() -> bool:
-    return os.path.exists(os.path.join(_HERE, "_ref", "libref_kdtree.so"))
+_REF_NAMES = {False: "libref_kdtree.so", True: "libref_kdtree_int.so"}
 
 
-def ref_lib():
+def ref_available(int_offsets: bool = False) -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", _REF_NAMES[bool(int_offsets)]))
+
+
+def ref_lib(int_offsets: bool = False):
+    """The reference's tree as compiled from its sources (`make ref`), or the copy whose leaf offsets are read as
+    integers instead of float (`make ref-int`)."""
     global _REF
     if _REF is None:
-        path = os.path.join(_HERE, "_ref", "libref_kdtree.so")
-        L = ctypes.CDLL(path)
+        _REF = {}
+    key = bool(int_offsets)
+    if key not in _REF:
+        L = ctypes.CDLL(os.path.join(_HERE, "_ref", _REF_NAMES[key]))
         L.ref_tree_create.restype = _p
         L.ref_tree_create.argtypes = [_i, _fptr, _i, _iptr, _i]
         L.ref_tree_destroy.argtypes = [_p]
         L.ref_tree_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
         L.ref_grid_bbox.argtypes = [_p, _fptr]
-        _REF = L
-    return _REF
+        _REF[key] = L
+    return _REF[key]
 
 
 # ---------------------------------------------------------------------------------------------------
@@ -334,18 +349,48 @@ class Oracle:
         return uv, p
 
 
-class ReferenceTree:
-    """The reference's own KD tree (oracle/_ref), built over a mesh; only where the reference compiled."""
+class PortTree:
+    """The oracle's restatement of the reference tree (int leaf offsets) without the rest of the oracle."""
 
     def __init__(self, mesh):
-        L = ref_lib()
         nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float32).reshape(-1)
         els = np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1)
-        self._h = L.ref_tree_create(mesh.n_nodes, nodes, mesh.n_elements, els, mesh.n_pressure)
+        self._h = lib().orc_tree_create(mesh.n_nodes, nodes, mesh.n_elements, els)
 
     def close(self):
         if getattr(self, "_h", None):
-            ref_lib().ref_tree_destroy(self._h)
+            lib().orc_tree_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def locate(self, pts):
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 2)
+        n = pts.shape[0]
+        e, xi, eta, nn = np.zeros(n, np.int32), np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.int32)
+        lib().orc_tree_locate(self._h, n, pts.reshape(-1), e, xi, eta, nn)
+        return e, xi, eta, nn
+
+    def stats(self):
+        a, b, d = ctypes.c_int64(), ctypes.c_int64(), _i()
+        lib().orc_tree_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(d))
+        return {"nodes": a.value, "leaf_entries": b.value, "max_depth": d.value}
+
+
+class ReferenceTree:
+    """The reference's own KD tree (oracle/_ref), built over a mesh; only where the reference compiled.
+    ``int_offsets=True`` uses the build whose KDNode::getTriangleOffset returns the integer offset instead of
+    float (gpu_cpu_shared/kd_tree_common.cuh:91,148-150); the two agree while every leaf offset is below 2^24."""
+
+    def __init__(self, mesh, int_offsets: bool = False):
+        self._lib = ref_lib(int_offsets)
+        nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float32).reshape(-1)
+        els = np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1)
+        self._h = self._lib.ref_tree_create(mesh.n_nodes, nodes, mesh.n_elements, els, mesh.n_pressure)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ref_tree_destroy(self._h)
             self._h = None
 
     __del__ = close
@@ -357,12 +402,12 @@ class ReferenceTree:
         xi = np.zeros(n, np.float32)
         eta = np.zeros(n, np.float32)
         nn = np.zeros(n, np.int32)
-        ref_lib().ref_tree_locate(self._h, n, pts.reshape(-1), e, xi, eta, nn)
+        self._lib.ref_tree_locate(self._h, n, pts.reshape(-1), e, xi, eta, nn)
         return e, xi, eta, nn
 
     def bbox(self):
         out = np.zeros(4, np.float32)
-        ref_lib().ref_grid_bbox(self._h, out)
+        self._lib.ref_grid_bbox(self._h, out)
         return out
 
 

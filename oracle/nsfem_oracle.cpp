@@ -154,34 +154,70 @@ template <typename R> struct CSR {
     void scale(R a) { for (auto& v : val) v *= a; }
 };
 
+// Triplets are added from `parts` contiguous element ranges at once (one per thread); part k holds the entries of
+// the k-th range in insertion order, so concatenating the parts in order gives exactly the serial insertion order of
+// the element loop.  to_csr keeps that order within every row (a stable counting sort by row, parts in order), then
+// stable-sorts each row by column and sums duplicates in that order - the same sums, bit for bit, as one serial pass.
 template <typename R> struct Triplets {
+    struct Entry { int row, col; R val; };
     int rows, cols;
-    std::vector<std::vector<std::pair<int, R>>> byRow;
-    Triplets(int r, int c) : rows(r), cols(c), byRow(r) {}
-    void add(int r, int c, R v) { byRow[r].emplace_back(c, v); }
+    std::vector<std::vector<Entry>> parts;
+    Triplets(int r, int c, int nparts) : rows(r), cols(c), parts(nparts) {}
+    void add(int part, int r, int c, R v) { parts[part].push_back(Entry{r, c, v}); }
     CSR<R> to_csr() {
+        const int np = (int)parts.size();
+        // cnt[k*rows + r]: entries of row r in part k, turned into that part's first slot in row r
+        std::vector<int64_t> cnt((size_t)np * rows, 0);
+#pragma omp parallel for schedule(static, 1)
+        for (int k = 0; k < np; ++k)
+            for (const Entry& e : parts[k]) ++cnt[(size_t)k * rows + e.row];
+        std::vector<int64_t> start(rows + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < rows; ++r) {
+            int64_t s = 0;
+            for (int k = 0; k < np; ++k) s += cnt[(size_t)k * rows + r];
+            start[r + 1] = s;
+        }
+        for (int r = 0; r < rows; ++r) start[r + 1] += start[r];
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < rows; ++r) {
+            int64_t o = start[r];
+            for (int k = 0; k < np; ++k) {
+                const int64_t c = cnt[(size_t)k * rows + r];
+                cnt[(size_t)k * rows + r] = o;
+                o += c;
+            }
+        }
+        std::unique_ptr<std::pair<int, R>[]> tmp(new std::pair<int, R>[start[rows]]);
+#pragma omp parallel for schedule(static, 1)
+        for (int k = 0; k < np; ++k) {
+            for (const Entry& e : parts[k]) tmp[cnt[(size_t)k * rows + e.row]++] = {e.col, e.val};
+            std::vector<Entry>().swap(parts[k]);
+        }
+        std::vector<int64_t>().swap(cnt);
+        // per row: stable sort by column, sum duplicates in order (in place), count the distinct columns
+        std::vector<int64_t> uniq(rows + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int r = 0; r < rows; ++r) {
+            auto b = tmp.get() + start[r], e = tmp.get() + start[r + 1];
+            std::stable_sort(b, e, [](const auto& x, const auto& y) { return x.first < y.first; });
+            int64_t w = start[r];
+            for (int64_t q = start[r]; q < start[r + 1]; ++q) {
+                if (w > start[r] && tmp[w - 1].first == tmp[q].first) tmp[w - 1].second += tmp[q].second;
+                else tmp[w++] = tmp[q];
+            }
+            uniq[r + 1] = w - start[r];
+        }
         CSR<R> m;
         m.rows = rows; m.cols = cols;
         m.rowptr.assign(rows + 1, 0);
-        std::vector<std::vector<std::pair<int, R>>> merged(rows);
-#pragma omp parallel for schedule(dynamic, 1024)
-        for (int r = 0; r < rows; ++r) {
-            auto& e = byRow[r];
-            std::stable_sort(e.begin(), e.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
-            auto& out = merged[r];
-            for (size_t k = 0; k < e.size(); ++k) {
-                if (!out.empty() && out.back().first == e[k].first) out.back().second += e[k].second;
-                else out.push_back(e[k]);
-            }
-            std::vector<std::pair<int, R>>().swap(e);
-        }
-        for (int r = 0; r < rows; ++r) m.rowptr[r + 1] = m.rowptr[r] + (int64_t)merged[r].size();
+        for (int r = 0; r < rows; ++r) m.rowptr[r + 1] = m.rowptr[r] + uniq[r + 1];
         m.col.resize(m.rowptr[rows]);
         m.val.resize(m.rowptr[rows]);
 #pragma omp parallel for schedule(static)
         for (int r = 0; r < rows; ++r) {
             int64_t o = m.rowptr[r];
-            for (auto& cv : merged[r]) { m.col[o] = cv.first; m.val[o] = cv.second; ++o; }
+            for (int64_t q = start[r]; q < start[r] + uniq[r + 1]; ++q) { m.col[o] = tmp[q].first; m.val[o] = tmp[q].second; ++o; }
         }
         return m;
     }
@@ -425,8 +461,37 @@ template <typename R> struct Solver : SolverBase {
         std::vector<char> uBC(Nv, 0), pBC(P, 0);
         for (int v : uNodes) uBC[v] = 1;
         for (int v : pNodes) pBC[v] = 1;
-        Triplets<R> M(Nv, Nv), D(Nv, Nv), Wv(Nv, Nv), Kp(P, P), Wp(P, P), Dv(P, 2 * Nv), G(2 * Nv, P);
-        for (int e = 0; e < T; ++e) {
+        // contiguous element ranges in parallel, one triplet part per range (see Triplets)
+        const int parts = std::max(1, std::min(omp_get_max_threads(), T / 4096 + 1));
+        Triplets<R> M(Nv, Nv, parts), D(Nv, Nv, parts), Wv(Nv, Nv, parts), Kp(P, P, parts), Wp(P, P, parts),
+            Dv(P, 2 * Nv, parts), G(2 * Nv, P, parts);
+        // exact sizes per part first (one allocation each instead of repeated growth)
+#pragma omp parallel for schedule(static, 1) num_threads(parts)
+        for (int part = 0; part < parts; ++part) {
+            const int e0 = (int)((int64_t)T * part / parts), e1 = (int)((int64_t)T * (part + 1) / parts);
+            size_t nD = 0, nW = 0, nK = 0, nWp = 0;
+            for (int e = e0; e < e1; ++e) {
+                const int* t = &el[6 * (size_t)e];
+                int fu = 0, fp = 0;
+                for (int i = 0; i < 6; ++i) fu += !uBC[t[i]];
+                for (int i = 0; i < 3; ++i) fp += !pBC[t[i]];
+                nD += (size_t)fu * fu;
+                nW += (size_t)fu * (6 - fu);
+                nK += (size_t)fp * fp;
+                nWp += (size_t)fp * (3 - fp);
+            }
+            const size_t ne = (size_t)(e1 - e0);
+            M.parts[part].reserve(36 * ne);
+            D.parts[part].reserve(nD + (part == parts - 1 ? (size_t)Nv : 0));
+            Wv.parts[part].reserve(nW);
+            Kp.parts[part].reserve(nK + (part == parts - 1 ? (size_t)P : 0));
+            Wp.parts[part].reserve(nWp);
+            Dv.parts[part].reserve(36 * ne);
+            G.parts[part].reserve(36 * ne);
+        }
+#pragma omp parallel for schedule(static, 1) num_threads(parts)
+        for (int part = 0; part < parts; ++part)
+        for (int e = (int)((int64_t)T * part / parts); e < (int)((int64_t)T * (part + 1) / parts); ++e) {
             const int* t = &el[6 * (size_t)e];
             R exy[12];
             element_xy(e, exy);
@@ -438,11 +503,11 @@ template <typename R> struct Solver : SolverBase {
             for (int i = 0; i < 6; ++i) {
                 const bool rb = uBC[t[i]];
                 for (int j = 0; j < 6; ++j) {
-                    M.add(t[i], t[j], mloc[i][j]);
+                    M.add(part, t[i], t[j], mloc[i][j]);
                     const R d = mloc[i][j] + kloc[i][j] * dt * nu;
                     const bool cb = uBC[t[j]];
-                    if (!rb && !cb) D.add(t[i], t[j], d);
-                    else if (!rb && cb) Wv.add(t[j], t[i], d);
+                    if (!rb && !cb) D.add(part, t[i], t[j], d);
+                    else if (!rb && cb) Wv.add(part, t[j], t[i], d);
                 }
             }
             // pressure stiffness (P1) with pressure Dirichlet elimination
@@ -452,8 +517,8 @@ template <typename R> struct Solver : SolverBase {
                 const bool rb = pBC[t[i]];
                 for (int j = 0; j < 3; ++j) {
                     const bool cb = pBC[t[j]];
-                    if (!rb && !cb) Kp.add(t[i], t[j], kp[i][j]);
-                    else if (!rb && cb) Wp.add(t[j], t[i], kp[i][j]);
+                    if (!rb && !cb) Kp.add(part, t[i], t[j], kp[i][j]);
+                    else if (!rb && cb) Wp.add(part, t[j], t[i], kp[i][j]);
                 }
             }
             // divergence blocks (LocalDivergenceFunctor): B rows with the precomputed mixed integrals
@@ -463,20 +528,20 @@ template <typename R> struct Solver : SolverBase {
                 for (int q = 0; q < 6; ++q) {
                     const R dx = B[0][0] * I.divP1P2[pp][q] + B[0][1] * I.divP1P2[pp][q + 6];
                     const R dy = B[1][0] * I.divP1P2[pp][q] + B[1][1] * I.divP1P2[pp][q + 6];
-                    Dv.add(t[pp], t[q], dx);
-                    Dv.add(t[pp], t[q] + Nv, dy);
+                    Dv.add(part, t[pp], t[q], dx);
+                    Dv.add(part, t[pp], t[q] + Nv, dy);
                 }
             for (int q = 0; q < 6; ++q)
                 for (int pp = 0; pp < 3; ++pp) {
                     const R dx = B[0][0] * I.divP2P1[q][pp] + B[0][1] * I.divP2P1[q][pp + 3];
                     const R dy = B[1][0] * I.divP2P1[q][pp] + B[1][1] * I.divP2P1[q][pp + 3];
-                    G.add(t[q], t[pp], dx);
-                    G.add(t[q] + Nv, t[pp], dy);
+                    G.add(part, t[q], t[pp], dx);
+                    G.add(part, t[q] + Nv, t[pp], dy);
                 }
         }
         // BC rows become identity rows, once per distinct BC node (the reference walks an unordered_set)
-        for (int v = 0; v < Nv; ++v) if (uBC[v]) D.add(v, v, R(1));
-        for (int v = 0; v < P; ++v) if (pBC[v]) Kp.add(v, v, R(1));
+        for (int v = 0; v < Nv; ++v) if (uBC[v]) D.add(parts - 1, v, v, R(1));
+        for (int v = 0; v < P; ++v) if (pBC[v]) Kp.add(parts - 1, v, v, R(1));
         mats[VELOCITY_MASS] = M.to_csr();
         mats[DIFFUSION] = D.to_csr();
         mats[VELOCITY_DIRICHLET_WEIGHTS] = Wv.to_csr();
@@ -669,6 +734,38 @@ int orc_tree_size(void* h, int* nNodes, int* nLeafTris, int* maxDepth) {
     *nLeafTris = (int)s->tree.leafTris.size();
     *maxDepth = s->tree.maxDepth;
     return 0;
+}
+// The ported tree alone (no assembly), for point-location checks on large meshes.
+struct TreeOnly {
+    std::vector<float> xy;
+    std::vector<int> el;
+    KDTree tree;
+};
+void* orc_tree_create(int nNodes, const float* nodes, int nEl, const int* elements) {
+    TreeOnly* t = new TreeOnly;
+    t->xy.assign(nodes, nodes + 2 * (size_t)nNodes);
+    t->el.assign(elements, elements + 6 * (size_t)nEl);
+    t->tree.build(t->xy.data(), t->el.data(), nNodes, nEl);
+    return t;
+}
+void orc_tree_destroy(void* h) { delete (TreeOnly*)h; }
+void orc_tree_locate(void* h, int n, const float* pts, int* elem, float* xi, float* eta, int* nearest) {
+    const KDTree& tree = ((TreeOnly*)h)->tree;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < n; ++i) {
+        float a = 0, b = 0;
+        int nn = -1;
+        elem[i] = tree.find(pts[2 * i], pts[2 * i + 1], a, b, nn);
+        xi[i] = a; eta[i] = b;
+        nearest[i] = elem[i] >= 0 ? -1 : nn;
+    }
+}
+// leaf entries (the reference's leafTriangleIndexes length: its largest leaf offset is below it) and tree depth
+void orc_tree_stats(void* h, int64_t* nodes, int64_t* leafEntries, int* maxDepth) {
+    const KDTree& tree = ((TreeOnly*)h)->tree;
+    *nodes = (int64_t)tree.nodes.size();
+    *leafEntries = (int64_t)tree.leafTris.size();
+    *maxDepth = tree.maxDepth;
 }
 void orc_advect(void* h, const double* u, const double* v, double* uo, double* vo) { ((SolverBase*)h)->advect(u, v, uo, vo); }
 int orc_step(void* h, int nsteps, int* iters) { return ((SolverBase*)h)->step(nsteps, iters); }

@@ -54,7 +54,9 @@ void ref_tree_destroy(void* h) { delete (State*)h; }
 
 void ref_tree_locate(void* h, int n, const float* pts, int* elem, float* xi, float* eta, int* nearest) {
     State* s = (State*)h;
-    NSFem::KDTree<NSFem::FemGrid2D> tree = s->owner.getTree();
+    const NSFem::KDTree<NSFem::FemGrid2D> tree = s->owner.getTree();
+    // findElement is const and keeps its traversal stack on the stack: queries are independent
+#pragma omp parallel for schedule(dynamic, 4096)
     for (int i = 0; i < n; ++i) {
         float a = 0, b = 0;
         int nn = -1;

@@ -6,7 +6,8 @@ This script runs them on seeded point sets over three meshes and stores, per poi
 the float barycentrics (xi, eta) and the nearest-node fallback, so that the oracle port and the GPU path can be
 checked against the reference where the reference checkout does not exist.
 
-    python tests/golden/make_golden.py        (needs the reference sources and oracle/_ref)
+    NSFEM_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
+    (needs the reference sources: oracle/_ref is built from them first)
 
 Meshes: the reference's assets/mesh_small.json (stored here as arrays), the 32x32 lid-driven cavity, and a 12x12
 cavity whose interior vertices are randomly perturbed (seed 11) so that no edge is axis-aligned.
@@ -25,7 +26,8 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from navier_stokes_fem_gb300 import mesh as M  # noqa: E402
 
-REF_MESH = os.path.join(os.environ.get("NSFEM_REFERENCE_DIR", "/root/reference"), "assets", "mesh_small.json")
+REF_DIR = os.environ.get("NSFEM_REFERENCE_DIR", "")
+REF_MESH = os.path.join(REF_DIR, "assets", "mesh_small.json")
 
 
 def perturbed_cavity(n: int = 12, seed: int = 11, amp: float = 0.3) -> M.Mesh:
@@ -62,8 +64,9 @@ def point_set(m: M.Mesh, seed: int, n_random: int = 4000) -> np.ndarray:
 
 
 def main():
-    if not oracle.ref_available():
-        raise SystemExit("oracle/_ref/libref_kdtree.so is missing: run `make -C oracle ref` first")
+    if not REF_DIR:
+        raise SystemExit("set NSFEM_REFERENCE_DIR to the reference checkout")
+    oracle.build(ref=True)
     meshes = [M.read_mesh_json(REF_MESH), M.cavity(32), perturbed_cavity()]
     out = {}
     for k, m in enumerate(meshes):

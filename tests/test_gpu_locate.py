@@ -9,7 +9,7 @@ import pytest
 import navier_stokes_fem_gb300 as nsf
 import oracle
 from navier_stokes_fem_gb300 import mesh as M
-from tests._meshes import golden_mesh
+from tests._meshes import departure_points, golden_mesh, lookup_digests, nearest_ties_ok
 
 pytestmark = pytest.mark.gpu
 TAGS = ["mesh_small", "cavity32", "perturbed12"]
@@ -99,3 +99,34 @@ def test_advect_f32_reference_signature(dev):
     gu, gv = dev.advect(u, v, 0.02)
     ru, rv = o.advect(u.astype(np.float64), v.astype(np.float64))
     assert np.array_equal(gu, ru.astype(np.float32)) and np.array_equal(gv, rv.astype(np.float32))
+
+
+@pytest.fixture(scope="module")
+def large_golden():
+    import os
+
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_kdtree_lookup_large.npz"))
+
+
+@pytest.mark.parametrize("n", [256, 1024, 2048])
+def test_locate_departure_points_match_reference_tree_large(dev, large_golden, n):
+    """Every velocity node's departure point on the 256^2, 1024^2 and 2048^2 cavities (0.26 M, 4.2 M and 16.8 M
+    points) against the reference's own tree with its leaf offsets read as integers: element ids and float
+    barycentrics bit-identical (digests over all points, plus an explicit sample), nearest nodes equal up to true
+    ties.  At 1024^2 and 2048^2 the reference's leaf-entry array passes 2^24 entries, where its float offsets round
+    (the fixture records how many points the unchanged reference answers differently)."""
+    m = M.cavity(n)
+    pts = departure_points(m)
+    dev.upload_kd_tree(m)
+    e, xi, eta, nn = dev.locate(pts)
+    s = large_golden[f"n{n}/sample"]
+    assert np.array_equal(e[s], large_golden[f"n{n}/sample_elem"])
+    assert np.array_equal(xi[s].view(np.uint32), large_golden[f"n{n}/sample_xi"].view(np.uint32))
+    assert np.array_equal(eta[s].view(np.uint32), large_golden[f"n{n}/sample_eta"].view(np.uint32))
+    want = [str(d) for d in large_golden[f"n{n}/digests"]]
+    got = lookup_digests(e, xi, eta)
+    bad = [k for k in range(len(want)) if got[k] != want[k]]
+    assert not bad, f"point slices {bad} differ from the reference tree"
+    outside = large_golden[f"n{n}/outside"]
+    assert np.array_equal(np.nonzero(e < 0)[0], outside)
+    nearest_ties_ok(m, pts[outside], nn[outside], large_golden[f"n{n}/outside_nearest"])

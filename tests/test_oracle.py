@@ -276,3 +276,27 @@ def test_mesh_json_roundtrip(tmp_path):
     M.write_scene_json(str(s), "m.json", 1.0, 0.01, 0.01)
     sc = M.read_scene_json(str(s))
     assert sc["mesh_path"] == str(p)
+
+
+@pytest.mark.parametrize("n", [256, 1024])
+def test_oracle_port_tree_matches_large_reference_fixture(n):
+    """The oracle's restatement of the reference tree against the reference's own (int-offset) tree on every
+    departure point of the 256^2 and 1024^2 cavities (digests over all points written from the reference)."""
+    import json
+    import os
+
+    from tests._meshes import departure_points, lookup_digests, nearest_ties_ok
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_kdtree_lookup_large.npz"))
+    m = M.cavity(n)
+    pts = departure_points(m)
+    t = oracle.PortTree(m)
+    e, xi, eta, nn = t.locate(pts)
+    stats = t.stats()
+    t.close()
+    rec = json.loads(str(g[f"n{n}/record"][0]))
+    assert stats["leaf_entries"] == rec["leaf_entries"] and stats["max_depth"] == rec["max_depth"]
+    assert lookup_digests(e, xi, eta) == [str(d) for d in g[f"n{n}/digests"]]
+    outside = g[f"n{n}/outside"]
+    assert np.array_equal(np.nonzero(e < 0)[0], outside)
+    nearest_ties_ok(m, pts[outside], nn[outside], g[f"n{n}/outside_nearest"])

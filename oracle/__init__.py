@@ -54,7 +54,23 @@ def build(ref: bool | None = None) -> None:
     if ref:
         if not ref_dir:
             raise RuntimeError("set NSFEM_REFERENCE_DIR to the reference checkout to build the reference tree")
-        subprocess.run(["make", "-s", "-C", _HERE, "ref", "ref-int", f"REF={ref_dir}"], check=True)
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "ref-int", "ref-assembly", f"REF={ref_dir}"], check=True)
+        with open(os.path.join(_HERE, "_ref", "REFERENCE_DIR"), "w") as f:
+            f.write(os.path.abspath(ref_dir))
+
+
+def reference_dir() -> str | None:
+    """The reference checkout: NSFEM_REFERENCE_DIR, else the one the reference builds in _ref/ were made from; None
+    where neither exists (as on a machine without the checkout)."""
+    cands = [os.environ.get("NSFEM_REFERENCE_DIR", "")]
+    rec = os.path.join(_HERE, "_ref", "REFERENCE_DIR")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            cands.append(f.read().strip())
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "include")):
+            return c
+    return None
 
 
 def lib():
@@ -76,6 +92,7 @@ def lib():
         L.orc_cg.argtypes = [_p, _i, _dptr, _dptr, _dptr, _i, _d, ctypes.POINTER(_i), ctypes.POINTER(_d)]
         L.orc_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
         L.orc_tree_size.argtypes = [_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]
+        L.orc_local_matrices.argtypes = [_i, _i, _fptr] + [_dptr] * 7
         L.orc_tree_create.restype = _p
         L.orc_tree_create.argtypes = [_i, _fptr, _i, _iptr]
         L.orc_tree_destroy.argtypes = [_p]
@@ -347,6 +364,37 @@ class Oracle:
         uv, p = np.zeros(2 * self.nv), np.zeros(self.np_)
         lib().orc_get_fields(self._h, uv, p)
         return uv, p
+
+
+LOCAL_MATRIX_SHAPES = {"mass": (6, 6), "stiffness_p2": (6, 6), "stiffness_p1": (3, 3), "divergence_x": (3, 6),
+                       "divergence_y": (3, 6), "gradient_x": (6, 3), "gradient_y": (6, 3)}
+
+
+def local_matrices(vertices, real_bits: int = 64):
+    """The oracle's local element matrices of triangles given as [n, 6] float32 vertex coordinates (x0 y0 x1 y1 x2 y2),
+    computed in float (real_bits 32) or double: a dict of [n, rows, cols] float64 arrays keyed as
+    LOCAL_MATRIX_SHAPES."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 6)
+    n = v.shape[0]
+    out = {k: np.zeros((n,) + s) for k, s in LOCAL_MATRIX_SHAPES.items()}
+    lib().orc_local_matrices(int(real_bits), n, v.reshape(-1), *[out[k].reshape(-1) for k in LOCAL_MATRIX_SHAPES])
+    return out
+
+
+def ref_local_matrices(vertices):
+    """The same matrices from the reference's own element code (`make ref-assembly`), in float."""
+    path = os.path.join(_HERE, "_ref", "libref_assembly.so")
+    L = ctypes.CDLL(path)
+    L.ref_local_matrices.argtypes = [_i, _fptr] + [_fptr] * 7
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 6)
+    n = v.shape[0]
+    out = {k: np.zeros((n,) + s, np.float32) for k, s in LOCAL_MATRIX_SHAPES.items()}
+    L.ref_local_matrices(n, v.reshape(-1), *[out[k].reshape(-1) for k in LOCAL_MATRIX_SHAPES])
+    return out
+
+
+def ref_assembly_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libref_assembly.so"))
 
 
 class PortTree:

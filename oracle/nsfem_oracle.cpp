@@ -675,6 +675,44 @@ template <typename R> struct Solver : SolverBase {
 
 using namespace oracle;
 
+namespace oracle {
+// Local element matrices of `n` triangles (vertices x0 y0 x1 y1 x2 y2 each), computed the way assemble() computes
+// them, in float (realBits 32, the reference's arithmetic) or double; same layouts as the reference build's
+// ref_local_matrices (oracle/ref_assembly_shim.cpp), which pins them.
+template <typename R>
+static void local_matrices(int n, const float* v, double* mass, double* stiffV, double* stiffP, double* divVx,
+                           double* divVy, double* divPx, double* divPy) {
+    RefIntegrals<R> I;
+    for (int e = 0; e < n; ++e) {
+        R exy[12] = {};
+        for (int k = 0; k < 6; ++k) exy[k] = (R)v[6 * e + k];
+        const R jabs = std::abs(jacobian_det(exy));
+        R kloc[6][6], kp[3][3];
+        local_stiffness<R, 6, 12>(exy, I.delP2, kloc);
+        local_stiffness<R, 3, 6>(exy, I.delP1, kp);
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                mass[36 * e + 6 * i + j] = (double)(I.mass[i][j] * jabs);
+                stiffV[36 * e + 6 * i + j] = (double)kloc[i][j];
+            }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) stiffP[9 * e + 3 * i + j] = (double)kp[i][j];
+        R det, B[2][2];
+        diff_operator(exy, det, B);
+        for (int pp = 0; pp < 3; ++pp)
+            for (int q = 0; q < 6; ++q) {
+                divVx[18 * e + 6 * pp + q] = (double)(B[0][0] * I.divP1P2[pp][q] + B[0][1] * I.divP1P2[pp][q + 6]);
+                divVy[18 * e + 6 * pp + q] = (double)(B[1][0] * I.divP1P2[pp][q] + B[1][1] * I.divP1P2[pp][q + 6]);
+            }
+        for (int q = 0; q < 6; ++q)
+            for (int pp = 0; pp < 3; ++pp) {
+                divPx[18 * e + 3 * q + pp] = (double)(B[0][0] * I.divP2P1[q][pp] + B[0][1] * I.divP2P1[q][pp + 3]);
+                divPy[18 * e + 3 * q + pp] = (double)(B[1][0] * I.divP2P1[q][pp] + B[1][1] * I.divP2P1[q][pp + 3]);
+            }
+    }
+}
+}  // namespace oracle
+
 extern "C" {
 
 // realBits: 64 -> FP64 oracle, 32 -> the reference's FP32 arithmetic.
@@ -735,6 +773,12 @@ int orc_tree_size(void* h, int* nNodes, int* nLeafTris, int* maxDepth) {
     *maxDepth = s->tree.maxDepth;
     return 0;
 }
+void orc_local_matrices(int realBits, int n, const float* v, double* mass, double* stiffV, double* stiffP,
+                        double* divVx, double* divVy, double* divPx, double* divPy) {
+    if (realBits == 32) oracle::local_matrices<float>(n, v, mass, stiffV, stiffP, divVx, divVy, divPx, divPy);
+    else oracle::local_matrices<double>(n, v, mass, stiffV, stiffP, divVx, divVy, divPx, divPy);
+}
+
 // The ported tree alone (no assembly), for point-location checks on large meshes.
 struct TreeOnly {
     std::vector<float> xy;

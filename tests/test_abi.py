@@ -82,3 +82,33 @@ def test_python_bc_occurrences_follow_group_order():
     f = nsf._bc_fast(m)
     for a, b in zip(f, (un, gu, gv, pn, gp)):
         assert np.array_equal(a, b)
+
+
+def test_integration_shim_compiles_against_reference_header(tmp_path):
+    """The C++ shim of INTEGRATION.md section 2 against the reference's own, unmodified
+    include/gpu_simulation_device.h (g++ -fsyntax-only), with declarations standing in for the absent
+    sparse_matrix_math submodule; only where the reference checkout is present."""
+    import re
+    import shutil
+    import subprocess
+
+    import oracle
+
+    ref = oracle.reference_dir()
+    if ref is None or shutil.which("g++") is None:
+        pytest.skip("reference checkout not present here")
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        md = f.read()
+    block = re.search(r"```cpp\n(// gpu_simulation_device_gb300\.cpp.*?)```", md, re.S)
+    assert block, "shim block not found"
+    src = tmp_path / "gpu_simulation_device_gb300.cpp"
+    src.write_text(block.group(1))
+    forced = []
+    for h in ("vector", "string", "cstring", "cinttypes", "cassert", "cmath", "algorithm", "memory", "cstdarg",
+              "cstdio", "cfloat", "cstdint"):
+        forced += ["-include", h]
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-w", *forced, "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "oracle", "stub_include"), "-I", os.path.join(ref, "include"),
+           "-I", os.path.join(ref, "gpu_cpu_shared"), "-I", "/usr/local/cuda/include", str(src)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]

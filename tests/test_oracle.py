@@ -300,3 +300,34 @@ def test_oracle_port_tree_matches_large_reference_fixture(n):
     outside = g[f"n{n}/outside"]
     assert np.array_equal(np.nonzero(e < 0)[0], outside)
     nearest_ties_ok(m, pts[outside], nn[outside], g[f"n{n}/outside_nearest"])
+
+
+def _assembly_fixture():
+    import os
+
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_local_matrices.npz"))
+
+
+def test_local_matrices_match_reference_element_code():
+    """The oracle's local element matrices against the reference's own element code (shape functions, quadrature,
+    Jacobian and local functors of include/assembly.h compiled from its lines): bit-identical in the reference's
+    float arithmetic, and the FP64 oracle within float rounding of them (the stiffness cancels, so 1e-5 of the
+    largest entry)."""
+    g = _assembly_fixture()
+    v = g["vertices"]
+    o32 = oracle.local_matrices(v, 32)
+    o64 = oracle.local_matrices(v, 64)
+    for k in oracle.LOCAL_MATRIX_SHAPES:
+        ref = g[k].astype(np.float64)
+        assert np.array_equal(o32[k], ref), k
+        scale = np.abs(o64[k]).max(axis=(1, 2), keepdims=True)
+        assert (np.abs(o64[k] - ref) <= 1e-5 * scale).all(), k
+
+
+@pytest.mark.skipif(not oracle.ref_assembly_available(), reason="reference element code not compiled here")
+def test_local_matrices_match_reference_element_code_live():
+    g = _assembly_fixture()
+    v = g["vertices"]
+    live = oracle.ref_local_matrices(v)
+    for k in oracle.LOCAL_MATRIX_SHAPES:
+        assert np.array_equal(live[k], g[k]), k

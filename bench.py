@@ -397,6 +397,7 @@ def run_gpu(args):
     t0 = time.perf_counter()
     sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
                                    inner_tolerance=args.inner_tol)
+    sim.set_cg_form(args.cg_form)
     setup_s = time.perf_counter() - t0
     init = sim.fields()        # the run's initial state: u = 0 with the Dirichlet values imposed, p = 0
     learned = None
@@ -458,6 +459,7 @@ def run_gpu(args):
     plain, plain_sim, field_check = None, None, None
     if args.compare and not (args.solver == "fp64" and args.precond == "none"):
         plain_sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver="fp64")
+        plain_sim.set_cg_form(args.cg_form)
         parm = time_arm(plain_sim, args, pg, start=start)
         plain = {"ms_per_step": round(parm["ms"], 3), "cg_iterations_per_step": parm["its"].mean(axis=0).round(1).tolist(),
                  "speedup": round(parm["ms"] / ms, 3), "clocks": parm["clocks"]}
@@ -506,6 +508,7 @@ def run_gpu(args):
         "cg_iterations_per_step": its.mean(axis=0).round(1).tolist(),
         "cg_solves": ["diffusion u", "diffusion v", "pressure", "mass u", "mass v"],
         "plain_fp64_cg": plain,
+        "plain_cg_form": args.cg_form,
         "ic0_pcg_mixed": ic0,
         "field_check": field_check,
         "oracle_check": oracle_check,
@@ -645,6 +648,7 @@ def run_cg_probe(args):
     mat = sim.download_matrix("pressure_stiffness")
     sim.close()
     dev = nsf.GPUSimulationDevice(0)
+    dev.set_cg_form(args.cg_form)
     if args.inner_tol > 0:   # e.g. 1e-6: the mixed solvers' first inner launch then runs the whole probe budget
         dev.set_solver(args.solver, args.inner_tol)
     dev.upload_matrix("pressure_stiffness", *mat)
@@ -684,6 +688,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1, help="whole oracle steps timed for cpu_baseline")
     ap.add_argument("--ref-budget-s", type=float, default=150.0,
                     help="--impl reference: time budget of the timed whole CPU steps")
+    ap.add_argument("--cg-form", default="auto", choices=["auto", "three_sync", "pipelined"],
+                    help="iteration form of the plain FP64 CG (auto: by system size)")
     ap.add_argument("--no-ic0-arm", dest="ic0_arm", action="store_false",
                     help="skip the IC(0) run beside the learned preconditioner")
     ap.add_argument("--no-cpu-baseline", action="store_true")

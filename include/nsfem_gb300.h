@@ -74,6 +74,20 @@ enum nsf_solver {
     NSF_SOLVER_PCG_FP64 = 3    /* FP64 PCG with the slot's preconditioner (plain FP64 CG if it has none) */
 };
 
+/* Iteration form of the plain FP64 CG megakernel (nsf_set_cg_form).  The reference's megakernel joins 4 grid-wide
+ * syncs per iteration (gpu/matrix_math.cu:251-286). */
+enum nsf_cg_form {
+    NSF_CG_FORM_AUTO = 0,       /* pipelined below NSF_CG_PIPELINED_MAX_ROWS rows, three barriers above */
+    NSF_CG_FORM_THREE_SYNC = 1, /* q = A p and p.q | x, r and r.r | p = r + beta p: three grid barriers */
+    NSF_CG_FORM_PIPELINED = 2   /* one grid barrier per iteration: the recurrences of pipelined CG (Ghysels and
+                                 * Vanroose 2014) carry A r, A p and A A p, so the one product per iteration acts on
+                                 * a vector finished before the barrier; two more vector passes and about five more
+                                 * FP64 operations per row, and a final true-residual check */
+};
+
+/* NSF_CG_FORM_AUTO's crossover, from GB300 measurements of both forms on the cavity and channel systems */
+#define NSF_CG_PIPELINED_MAX_ROWS 2000000
+
 /* preconditioner kinds (nsf_precond_kind) */
 enum nsf_precond {
     NSF_PRECOND_NONE = 0,
@@ -166,6 +180,11 @@ int nsf_learn_apply(nsf_learner* L, nsf_device* target, int slot);
  * rounded to BF16, FP32 accumulation; epilogue 0 none, 1 ReLU; K and N multiples of 16 up to 128. */
 int nsf_tc_dense(nsf_device* h, int rows, int K, int N, const float* X, const float* W, const float* bias,
                  int epilogue, float* Y);
+/* A dense layer's weight gradients on the tensor cores, on host arrays: dW[K x N] = X^T G and db[N] = the column
+ * sums of G, for X[rows x K] and G[rows x N] rounded to BF16, FP32 accumulation; K + 1 <= 128, N a multiple of 16
+ * up to 128. */
+int nsf_tc_weight_gradient(nsf_device* h, int rows, int K, int N, const float* X, const float* G, float* dW,
+                           float* db);
 
 /* ---- mesh, point location and advection (uploadKDTree; advect; KDTree::findElement) ------------------ */
 /* Uploads the mesh and builds the point-location tree on the GPU over triangle centroids. */
@@ -215,6 +234,9 @@ int nsf_batch_plan(nsf_device* h, int* blocks, int* gridBlocks, float* trialMs, 
 /* ---- configuration, timing, pinned memory ------------------------------------------------------------ */
 int nsf_set_tolerance(nsf_device* h, double eps);
 int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);
+/* form: nsf_cg_form; applies to the plain FP64 CG solves of this handle (the iteration count is that of CG up to
+ * rounding: the pipelined recurrences may take a few more iterations on ill-conditioned systems). */
+int nsf_set_cg_form(nsf_device* h, int form);
 int nsf_set_barrier_timeout(nsf_device* h, double seconds);
 /* Records CUDA events around every persistent CG launch while enabled (clears previous records). */
 int nsf_profile(nsf_device* h, int enable);

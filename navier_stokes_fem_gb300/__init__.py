@@ -36,6 +36,7 @@ STATUS = {0: "NSF_OK", 1: "NSF_ERR_CUDA", 2: "NSF_ERR_NOT_CONVERGED", 3: "NSF_ER
           4: "NSF_ERR_BARRIER_TIMEOUT", 5: "NSF_ERR_BAD_ARG", 6: "NSF_ERR_STATE", 7: "NSF_ERR_NO_DEVICE"}
 SLOT = {"pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
         "pressure_divergence": 4, "velocity_lift": 5, "pressure_lift": 6}
+CG_FORM = {"auto": 0, "three_sync": 1, "pipelined": 2}
 SOLVER = {"fp64": 0, "mixed": 1, "pcg_mixed": 2, "pcg_fp64": 3}
 PRECOND = {0: "none", 1: "ic0", 2: "learned"}
 
@@ -86,6 +87,7 @@ _SIGS = {
     "nsf_sim_step_host": (_i, [_v, _v, _v, _i, _v, _v, _v]),
     "nsf_set_tolerance": (_i, [_v, _d]),
     "nsf_set_solver": (_i, [_v, _i, _d]),
+    "nsf_set_cg_form": (_i, [_v, _i]),
     "nsf_set_barrier_timeout": (_i, [_v, _d]),
     "nsf_profile": (_i, [_v, _i]),
     "nsf_profile_read": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.int32), _arr(np.int32),
@@ -100,6 +102,8 @@ _SIGS = {
     "nsf_precond_clear": (_i, [_v, _i]),
     "nsf_precond_cap": (_i, [_v, _i, _i]),
     "nsf_tc_dense": (_i, [_v, _i, _i, _i, _arr(np.float32), _arr(np.float32), _v, _i, _arr(np.float32)]),
+    "nsf_tc_weight_gradient": (_i, [_v, _i, _i, _i, _arr(np.float32), _arr(np.float32), _arr(np.float32),
+                                    _arr(np.float32)]),
     "nsf_learn_create": (_i, [_v, ctypes.c_uint64, _P(_v)]),
     "nsf_learn_destroy": (None, [_v]),
     "nsf_learn_last_error": (ctypes.c_char_p, [_v]),
@@ -359,6 +363,10 @@ class GPUSimulationDevice:
     def set_solver(self, solver="fp64", inner_tolerance=-1.0):
         self._check(library().nsf_set_solver(self._h, SOLVER[solver], float(inner_tolerance)))
 
+    def set_cg_form(self, form="auto"):
+        """Iteration form of the plain FP64 CG: "auto", "three_sync" or "pipelined" (one grid barrier)."""
+        self._check(library().nsf_set_cg_form(self._h, CG_FORM[form]))
+
     def set_barrier_timeout(self, seconds):
         self._check(library().nsf_set_barrier_timeout(self._h, float(seconds)))
 
@@ -543,6 +551,19 @@ def tc_dense(device, X, W, bias=None, relu=False):
                                 b.ctypes.data_as(_v) if b is not None else None, 1 if relu else 0, Y.reshape(-1))
     device._check(st)
     return Y
+
+
+def tc_weight_gradient(device, X, G):
+    """A dense layer's weight gradients on the tensor cores (BF16 operands, FP32 accumulation): (X^T G, colsum G)."""
+    X = np.ascontiguousarray(X, np.float32)
+    G = np.ascontiguousarray(G, np.float32)
+    rows, K = X.shape
+    N = G.shape[1]
+    dW = np.zeros((K, N), np.float32)
+    db = np.zeros(N, np.float32)
+    device._check(library().nsf_tc_weight_gradient(device._h, rows, K, N, X.reshape(-1), G.reshape(-1),
+                                                   dW.reshape(-1), db))
+    return dW, db
 
 
 class NavierStokesAssembly(GPUSimulationDevice):

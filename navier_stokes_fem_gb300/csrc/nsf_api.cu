@@ -183,6 +183,16 @@ cudaEvent_t pool_event(nsf_device* h) {
     return h->evPool[h->evUsed++];
 }
 
+// The plain FP64 CG form for a system: pipelined (one grid barrier per iteration) where the barriers are a
+// measurable share of an iteration, the three-barrier form on large systems, where the pipelined form's two extra
+// vector passes and extra FP64 operations per row cost more than two barriers.
+bool use_pipelined_cg(const nsf_device* h, const Csr& S) {
+    if (!h->ws.pipeOk || !S.sellStart.get()) return false;
+    if (h->cgForm == NSF_CG_FORM_PIPELINED) return true;
+    if (h->cgForm == NSF_CG_FORM_THREE_SYNC) return false;
+    return S.rows < NSF_CG_PIPELINED_MAX_ROWS;
+}
+
 // Launch one persistent solve; returns the index of its CgInfo slot.
 int launch_solve(nsf_device* h, int slot, int mode, const double* b, const double* x0, double* x, int maxIt,
                  double tol, const CgArgs* fused) {
@@ -264,6 +274,8 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
         pcg_mixed_split_launch(ws, a, h->stream);
     else if (mode == NSF_SOLVER_MIXED && wide)
         cg_mixed_split_launch(ws, a, h->stream);
+    else if (mode == NSF_SOLVER_FP64 && use_pipelined_cg(h, S))
+        cg_pipe_launch(ws, a, wide, h->stream);
     else
         cg_launch(ws, a, mode, wide, h->stream);
     if (h->profile) {
@@ -880,6 +892,13 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
         for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) prepare_matrix(h->mats[slot], true, h->stream);
         NSF_CUDA(cudaStreamSynchronize(h->stream));
     }
+    NSF_END(h)
+}
+
+int nsf_set_cg_form(nsf_device* h, int form) {
+    NSF_BEGIN(h)
+    if (form < NSF_CG_FORM_AUTO || form > NSF_CG_FORM_PIPELINED) throw bad_arg("unknown CG form");
+    h->cgForm = form;
     NSF_END(h)
 }
 

@@ -39,6 +39,14 @@ __global__ void __launch_bounds__(kCgThreads, 2) cg_fp64_kernel(CgArgs a) {
     team_cg_fp64<Wide>(t, a, stage, smem);
 }
 
+// The FP64 CG with one grid barrier per iteration (pipelined recurrences; needs the matrix's SELL copy).
+template <bool Wide>
+__global__ void __launch_bounds__(kCgThreads, 2) cg_fp64_pipe_kernel(CgArgs a) {
+    NSF_KERNEL_SHARED();
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_cg_fp64_pipelined<Wide>(t, a, stage, smem);
+}
+
 // The narrow mixed kernel streams its FP32 matrix through per-warp TMA rings (kRingBytes of dynamic shared memory).
 template <bool Wide>
 __global__ void __launch_bounds__(kCgThreads, 2) cg_mixed_kernel(CgArgs a) {
@@ -238,10 +246,28 @@ void cg_configure(CgWorkspace& ws, int device) {
         o1024 = std::min(o1024, o);
     }
     ws.gridInner1024 = sms * o1024;
+    // the pipelined FP64 CG runs on the same grid; it is offered only where that grid is co-resident for it
+    ws.pipeOk = true;
+    for (const void* fn : {(const void*)cg_fp64_pipe_kernel<false>, (const void*)cg_fp64_pipe_kernel<true>}) {
+        int o = 0;
+        NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kCgThreads, 0));
+        if (o < perSm) ws.pipeOk = false;
+    }
     ws.partials.alloc((size_t)6 * std::max(ws.grid, ws.gridInner));
     ws.sync.alloc(1);
     ws.info.alloc(4096);
     ws.loop.alloc(1);
+}
+
+void cg_pipe_launch(CgWorkspace& ws, const CgArgs& args, bool wide, cudaStream_t s) {
+    NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
+    CgArgs a = args;
+    a.wbuf0 = ws.w.get();
+    a.wbuf1 = ws.bp.get();
+    void* params[] = {&a};
+    const void* fn = wide ? (const void*)cg_fp64_pipe_kernel<true> : (const void*)cg_fp64_pipe_kernel<false>;
+    NSF_CUDA(cudaLaunchCooperativeKernel(fn, dim3(ws.grid), dim3(ws.block), params, 0, s));
+    count_launch();
 }
 
 void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStream_t s) {

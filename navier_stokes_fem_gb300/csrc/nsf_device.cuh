@@ -944,6 +944,156 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 }
 
 // ---------------------------------------------------------------------------------------------------
+// FP64 pipelined CG: one grid barrier per iteration (Ghysels & Vanroose, "Hiding global synchronization latency
+// in the preconditioned Conjugate Gradient algorithm", Parallel Computing 40, 2014; here without a preconditioner).
+// Besides x, r and p it carries s = A p, w = A r and z = A s as recurrences, so the only product of an iteration
+// is q = A w_i on a vector finished before the previous barrier, and every other update is row-local:
+//     gamma = r.r, delta = w.r (summed from the previous iteration's partials)
+//     beta = gamma / gamma_prev, alpha = gamma / (delta - beta gamma / alpha_prev)   (beta = 0, alpha = gamma / delta
+//                                                                                    at the first iteration)
+//     z = A w + beta z,  s = w + beta s,  p = r + beta p,  x += alpha p,  r -= alpha s,  w' = w - alpha z,
+// with the partials of r'.r' and w'.r' formed in the same pass.  In exact arithmetic it is the CG of team_cg_fp64;
+// in floating point its recurrences drift a little further from the true residual, so the solve finishes with
+// r = b - A x recomputed and tested, and continues (from that residual) when the drift left it above tolerance.
+// w is written to the other of two buffers (the product of this iteration still gathers the current one), and the
+// partials alternate between region pairs {0, 1} and {2, 3}: one barrier separates an iteration's partial writes
+// from the next iteration's reads, and the next writes go to the other pair.  Regions 4 and 5: b.b and r0.r0.
+// Vectors: r = a.r, s = a.q, p = a.pbuf0, z = a.pbuf1, w = a.wbuf0 / a.wbuf1.  Needs the SELL copy.
+// ---------------------------------------------------------------------------------------------------
+struct PipeRow {
+    double z, s, p, r, x, w;
+};
+
+template <bool Wide = false>
+static __device__ int team_cg_fp64_pipelined(Team& t, const CgArgs& a, double* stage, double* smem) {
+    const int G = t.size;
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    const double* b = a.bRowptr ? a.bOut : a.b;
+    build_rhs<Wide>(a, rb, re, stage);
+    int it = 0, status = NSF_ERR_NOT_CONVERGED, where = 1, restarts = 0;
+    double rr = 0, bb = 0, target = 0;
+    const double* xsrc = a.x0;
+    // (re)start: r = b - A x (x = x0 the first time), test it, then w = A r with the partials of r.r and w.r
+    for (;;) {
+        double rrp = 0, bbp = 0;
+        matrix_product<double, double, false, kResidU<Wide>, Wide>(
+            a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xsrc[c]; },
+            [&](int row, double acc, double xi) {
+                const double bi = b[row];
+                const double ri = bi - acc;
+                a.r[row] = ri;
+                if (a.x != xsrc) a.x[row] = xi;
+                rrp = fma(ri, ri, rrp);
+                bbp = fma(bi, bi, bbp);
+            });
+        rrp = block_sum(rrp, smem);
+        bbp = block_sum(bbp, smem);
+        if (threadIdx.x == 0) { a.partials[4 * G + t.rank] = bbp; a.partials[5 * G + t.rank] = rrp; }
+        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+        bb = grid_sum(a.partials + 4 * G, G, smem);
+        rr = grid_sum(a.partials + 5 * G, G, smem);
+        target = bb > 0 ? a.tol2 * bb : (restarts == 0 ? a.tol2 * rr : target);
+        if (!(rr == rr) || !(bb == bb) || isinf(rr) || isinf(bb)) { status = NSF_ERR_BREAKDOWN; break; }
+        if (rr <= target) { status = NSF_OK; break; }
+        if (it >= a.maxIt || restarts > 8) break;
+        double gp = 0, dp = 0;
+        matrix_product<double, double, false, kResidU<Wide>, Wide>(
+            a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.r[c]; },
+            [&](int row, double acc, double ri) {
+                a.wbuf0[row] = acc;
+                gp = fma(ri, ri, gp);
+                dp = fma(acc, ri, dp);
+            });
+        gp = block_sum(gp, smem);
+        dp = block_sum(dp, smem);
+        if (threadIdx.x == 0) { a.partials[t.rank] = gp; a.partials[G + t.rank] = dp; }
+        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+        xsrc = a.x;
+        // the iterations; k counts them since this (re)start (its parity picks the w buffer and the partial pair)
+        double gammaPrev = 1.0, alphaPrev = 1.0;
+        bool drifted = false;
+        for (int k = 0;; ++k) {
+            const int par = k & 1;
+            const double gamma = grid_sum(a.partials + (2 * par) * G, G, smem);
+            const double delta = grid_sum(a.partials + (2 * par + 1) * G, G, smem);
+            if (!(gamma == gamma) || isinf(gamma)) { status = NSF_ERR_BREAKDOWN; break; }
+            if (gamma <= target) { drifted = true; break; }     // confirmed against the true residual below
+            if (it >= a.maxIt) break;
+            const double beta = k == 0 ? 0.0 : gamma / gammaPrev;
+            const double den = k == 0 ? delta : delta - beta * gamma / alphaPrev;
+            if (!(den > 0.0) || isinf(den)) { status = NSF_ERR_BREAKDOWN; break; }
+            const double alpha = block_scalar(smem, [&] { return gamma / den; });
+            const double* wc = par ? a.wbuf1 : a.wbuf0;
+            double* wn = par ? a.wbuf0 : a.wbuf1;
+            double gn = 0, dn = 0;
+            auto gw = [&](int c) { return wc[c]; };
+            auto pre = [&](int row) {
+                PipeRow q;
+                q.r = a.r[row];
+                q.x = a.x[row];
+                q.w = wc[row];
+                if (k > 0) { q.z = a.pbuf1[row]; q.s = a.q[row]; q.p = a.pbuf0[row]; }
+                else { q.z = 0.0; q.s = 0.0; q.p = 0.0; }
+                return q;
+            };
+            auto epi = [&](int row, double acc, const PipeRow& q) {
+                const double z = fma(beta, q.z, acc);
+                const double sv = fma(beta, q.s, q.w);
+                const double pv = fma(beta, q.p, q.r);
+                a.pbuf1[row] = z;
+                a.q[row] = sv;
+                a.pbuf0[row] = pv;
+                a.x[row] = fma(alpha, pv, q.x);
+                const double rn = fma(-alpha, sv, q.r);
+                const double wv = fma(-alpha, z, q.w);
+                a.r[row] = rn;
+                wn[row] = wv;
+                gn = fma(rn, rn, gn);
+                dn = fma(wv, rn, dn);
+            };
+            if constexpr (Wide) sell_rows_wide<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal,
+                                                                               rb, re, gw, pre, epi);
+            else if (a.sellMaxW <= 5) sell_rows<double, double, false, 1, 5>(a.sellStart, a.sellCol, a.sellVal, rb,
+                                                                            re, gw, pre, epi);
+            else sell_rows<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal, rb, re, gw, pre, epi);
+            gn = block_sum(gn, smem);
+            dn = block_sum(dn, smem);
+            const int np = (k + 1) & 1;
+            if (threadIdx.x == 0) { a.partials[(2 * np) * G + t.rank] = gn; a.partials[(2 * np + 1) * G + t.rank] = dn; }
+            if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, gamma, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+            ++it;
+            gammaPrev = gamma;
+            alphaPrev = alpha;
+        }
+        if (status == NSF_ERR_BREAKDOWN || (!drifted && it >= a.maxIt)) {
+            if (it >= a.maxIt && status != NSF_ERR_BREAKDOWN) {
+                // out of budget: report the true residual of the last iterate
+                xsrc = a.x;
+                double rrp2 = 0;
+                matrix_product<double, double, false, kResidU<Wide>, Wide>(
+                    a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
+                    [&](int c) { return a.x[c]; }, [&](int row, double acc, double) {
+                        const double ri = b[row] - acc;
+                        rrp2 = fma(ri, ri, rrp2);
+                    });
+                rrp2 = block_sum(rrp2, smem);
+                if (threadIdx.x == 0) a.partials[5 * G + t.rank] = rrp2;
+                if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
+                rr = grid_sum(a.partials + 5 * G, G, smem);
+                if (rr <= target) status = NSF_OK;
+            }
+            break;
+        }
+        // the recursive residual met the tolerance: recompute r = b - A x and test it (the loop head); a drifted
+        // recurrence restarts from the true residual
+        ++restarts;
+    }
+    write_info(t, a, it, status, 1 + restarts, rr, bb);
+    return status;
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Mixed precision: FP32 CG with FP64 reliable updates.
 // The search direction p, the product q = A32 p, the residual r32 and the accumulated correction d32 are FP32;
 // the dot products and alpha/beta are FP64.  x, b and the true residual stay FP64: whenever the FP32 residual

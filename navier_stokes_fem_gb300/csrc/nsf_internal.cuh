@@ -247,6 +247,8 @@ struct CgArgs {
     const unsigned char* bcMask;
     const double* bcValue;
     double* bOut;
+    double* wbuf0;           // FP64 pipelined CG: the two buffers of w = A r
+    double* wbuf1;
 };
 
 // the workspace shared by every solve on a handle (sized for the largest system)
@@ -261,6 +263,7 @@ struct CgWorkspace {
     int block = 0;
     int gridInner = 0;       // grid of the split mixed PCG's inner-iteration kernel
     int gridInner1024 = 0;   // (its one-CTA-per-SM form)
+    bool pipeOk = false;     // the pipelined FP64 CG kernels are co-resident on `grid`
 };
 
 // launch helpers implemented in nsf_cg.cu / nsf_sparse.cu
@@ -268,6 +271,8 @@ void cg_configure(CgWorkspace& ws, int device);
 // wide: the matrix has slices wider than kSellChunk entries per row (the kernels' pipelined product for them)
 constexpr int kSellChunk = 8;
 void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, bool wide, cudaStream_t s);
+// The FP64 CG with one grid barrier per iteration (pipelined recurrences; the matrix must have its SELL copy).
+void cg_pipe_launch(CgWorkspace& ws, const CgArgs& a, bool wide, cudaStream_t s);
 // The split mixed PCG (narrow matrices): refresh kernel, then inner-iteration and refresh kernels until the solve
 // is done; one small device-to-host read per refresh cycle.
 void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
@@ -384,6 +389,7 @@ struct nsf_device {
     double innerTol = 0.1;   // mixed precision: FP32 residual reduction between FP64 true residuals
     long long timeoutNs = 2000000000LL;
     int solverMode = NSF_SOLVER_FP64;
+    int cgForm = NSF_CG_FORM_AUTO;   // plain FP64 CG: three barriers per iteration or pipelined (one)
     bool mixedOff[NSF_SLOT_COUNT] = {};   // systems whose mixed solve stalled once: solved in FP64 from then on
     nsf::Factor factors[NSF_SLOT_COUNT];  // preconditioners
     int pcgCap[NSF_SLOT_COUNT] = {};      // iteration cap of a preconditioned solve (0: rows)

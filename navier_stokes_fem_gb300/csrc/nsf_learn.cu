@@ -12,8 +12,9 @@
 //               h += relu([h, m] W1n + b1n) W2n + b2n                            (tensor cores)
 //     L^_cp = e . wde + bde,  L^_ii = softplus(h . wdn + bdn),  L = D^1/2 L^
 //     loss = || L^ L^T x^ - b^ ||^2 / || b^ ||^2 with x^ = D^1/2 x, b^ = D^-1/2 b (x a solution of A x = b)
-// The input-gradient products of the backward pass run on the tensor cores too; weight gradients are FP32
-// reductions with a fixed order (deterministic).  Every gather of the message passing is a fixed-order loop
+// The backward pass's input-gradient products and the message-passing layers' weight gradients run on the tensor
+// cores too (BF16 operands, FP32 accumulation; the 4-feature embeddings and the 1-output decoders keep FP32
+// reductions); every reduction has a fixed order (deterministic).  Every gather of the message passing is a fixed-order loop
 // over incidence lists, so forward and backward are deterministic as well.
 #include <algorithm>
 #include <cmath>
@@ -514,6 +515,32 @@ struct Learner {
         count_launch();
     }
 
+    // The message-passing layers' weight gradients on the tensor cores: bf16(X)^T bf16(G) and the bias colsum,
+    // FP32 accumulation in TMEM, per-CTA partials summed in a fixed order.
+    void wgrad_tc(TcSeg a, TcSeg b, TcSeg c, int nseg, int rows, const float* G, int N, const PT& w,
+                  const PT& bias) {
+        if (rows <= 0) return;
+        TcWgradArgs t{};
+        t.seg[0] = a;
+        t.seg[1] = b;
+        t.seg[2] = c;
+        t.nseg = nseg;
+        t.K = a.width + (nseg > 1 ? b.width : 0) + (nseg > 2 ? c.width : 0);
+        t.rows = rows;
+        t.G = G;
+        t.N = N;
+        const size_t outs = (size_t)(t.K + 1) * N;
+        L->part.ensure(outs * tc_wgrad_blocks(rows, sms));
+        t.part = L->part.get();
+        t.error = L->err.get();
+        t.timeoutNs = L->h->timeoutNs;
+        const int blocks = tc_wgrad(t, s, sms);
+        wgrad_reduce_kernel<<<grid_for(outs, 128), 128, 0, s>>>(blocks, t.K, N, L->part.get(), L->grad.get(), w.off,
+                                                                bias.off);
+        NSF_CUDA(cudaGetLastError());
+        count_launch();
+    }
+
     double dot(int n, const float* x, const float* y) {
         dot_partial_kernel<<<kDotBlocks, 256, 0, s>>>(n, x, y, L->dots.get());
         NSF_CUDA(cudaGetLastError());
@@ -606,10 +633,11 @@ struct Learner {
         for (int l = kLayers - 1; l >= 0; --l) {
             const auto& y = N.L[l];
             // node update: h' = h + relu([h, m] W1n + b1n) W2n + b2n
-            wgrad({T.V[l].get(), nullptr, kH}, none, none, 1, n, T.dH.get(), kH, y.W2n, y.b2n);
+            wgrad_tc({T.V[l].get(), nullptr, kH}, none, none, 1, n, T.dH.get(), kH, y.W2n, y.b2n);
             dense({T.dH.get(), nullptr, kH}, none, none, 1, n, wbwd(l, 3), kH, nullptr, TC_EPI_RELU_MASK,
                   T.PV[l].get(), T.dPV.get(), nullptr, nullptr);
-            wgrad({T.H[l].get(), nullptr, kH}, {T.MG[l].get(), nullptr, kH}, none, 2, n, T.dPV.get(), kH, y.W1n, y.b1n);
+            wgrad_tc({T.H[l].get(), nullptr, kH}, {T.MG[l].get(), nullptr, kH}, none, 2, n, T.dPV.get(), kH, y.W1n,
+                     y.b1n);
             dense({T.dPV.get(), nullptr, kH}, none, none, 1, n, wbwd(l, 2), 2 * kH, nullptr, TC_EPI_NONE, nullptr,
                   T.dY.get(), nullptr, nullptr);
             slice_kernel<<<grid_for((int64_t)n * kH, 256), 256, 0, s>>>(n, T.dH.get(), kH, 0, T.dH2.get(), 0);
@@ -623,11 +651,11 @@ struct Learner {
                 NSF_CUDA(cudaGetLastError());
                 count_launch();
                 // edge update: e' = e + relu([e, h_c, h_p] W1e + b1e) W2e + b2e
-                wgrad({T.U[l].get(), nullptr, kH}, none, none, 1, m, T.dE.get(), kH, y.W2e, y.b2e);
+                wgrad_tc({T.U[l].get(), nullptr, kH}, none, none, 1, m, T.dE.get(), kH, y.W2e, y.b2e);
                 dense({T.dE.get(), nullptr, kH}, none, none, 1, m, wbwd(l, 1), kH, nullptr, TC_EPI_RELU_MASK,
                       T.PU[l].get(), T.dPU.get(), nullptr, nullptr);
-                wgrad({T.E[l].get(), nullptr, kH}, {T.H[l].get(), S.c.get(), kH}, {T.H[l].get(), S.p.get(), kH}, 3, m,
-                      T.dPU.get(), kH, y.W1e, y.b1e);
+                wgrad_tc({T.E[l].get(), nullptr, kH}, {T.H[l].get(), S.c.get(), kH}, {T.H[l].get(), S.p.get(), kH},
+                         3, m, T.dPU.get(), kH, y.W1e, y.b1e);
                 dense({T.dPU.get(), nullptr, kH}, none, none, 1, m, wbwd(l, 0), 3 * kH, nullptr, TC_EPI_NONE,
                       nullptr, T.dX.get(), nullptr, nullptr);
                 slice_kernel<<<grid_for((int64_t)m * kH, 256), 256, 0, s>>>(m, T.dE.get(), kH, 0, T.dE2.get(), 0);

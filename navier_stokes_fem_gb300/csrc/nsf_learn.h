@@ -41,4 +41,22 @@ struct TcArgs {
 
 void tc_dense(const TcArgs& a, cudaStream_t s, int sms);
 
+// Weight gradients of a dense layer: part[b][k][o] = sum over CTA b's rows of bf16(X[r][k]) bf16(G[r][o]) (k < K)
+// and part[b][K][o] = sum of bf16(G[r][o]) (the bias), FP32 accumulation on the tensor cores.
+struct TcWgradArgs {
+    TcSeg seg[3];
+    int nseg;
+    int K;                        // sum of the segment widths, K + 1 <= 128
+    int rows;
+    const float* G;               // rows x N
+    int N;                        // multiple of 16 (<= 128)
+    int chunk;                    // rows per CTA (set by tc_wgrad)
+    float* part;                  // CTAs x (K + 1) x N
+    int* error;                   // raised on a time-out
+    long long timeoutNs;
+};
+int tc_wgrad(const TcWgradArgs& a, cudaStream_t s, int sms);
+// CTAs (= partial rows) tc_wgrad uses for `rows` rows on `sms` SMs
+int tc_wgrad_blocks(int rows, int sms);
+
 }  // namespace nsf

@@ -191,6 +191,179 @@ void tc_dense(const TcArgs& a, cudaStream_t s, int sms) {
     count_launch();
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Weight gradients of a dense layer on the tensor cores:
+//     part[b][k][o] = sum over CTA b's rows r of bf16(X[r][k]) * bf16(G[r][o])   (k < K)
+//     part[b][K][o] = sum over the same rows of bf16(G[r][o])                      (the bias)
+// with FP32 accumulation in TMEM.  The MMA's M dimension is the input feature (K + 1 <= 128, the rows above K stay
+// zero), N the layer's outputs, and its reduction dimension the edges or nodes: a CTA walks its rows in chunks of
+// kWgR, stages each chunk of X^T (features x rows) and G^T (outputs x rows) transposed into the K-major core-matrix
+// layout - two buffers, so that one chunk is staged while the MMAs of the previous one run - and one thread issues
+// kWgR / 16 MMAs per chunk and commits them to that buffer's mbarrier.  Bounded waits; TMEM freed on every path.
+// ---------------------------------------------------------------------------------------------------
+namespace {
+constexpr int kWgR = 128;                  // rows per chunk: the MMAs' reduction extent
+constexpr int kWgM = 128;                  // MMA rows: input features plus the bias row, zero-padded
+constexpr size_t kWgABytes = (size_t)kWgM * kWgR * 2;
+
+__device__ __forceinline__ void stage8(__nv_bfloat16* dst, const float (&v)[8]) {
+    union {
+        __nv_bfloat162 h[4];
+        uint4 u;
+    } pk;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) pk.h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+    *reinterpret_cast<uint4*>(dst) = pk.u;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kTcThreads, 1) tc_wgrad_kernel(TcWgradArgs g) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmemBase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int K = g.K, N = g.N;
+    const size_t bBytes = (size_t)N * kWgR * 2;
+    const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : 128u);
+    if (warp == 0) tc::tmem_alloc(&tmemBase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
+    // both A buffers zero once: the feature rows above K are never written again
+    for (size_t e = tid; e < 2 * kWgABytes / 16; e += kTcThreads)
+        reinterpret_cast<uint4*>(sm)[e] = make_uint4(0u, 0u, 0u, 0u);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmemBase;
+    const uint32_t idesc = tc::idesc_bf16(kWgM, N);
+    const uint32_t sbo = (uint32_t)kWgR * 16u;
+    const int r0 = blockIdx.x * g.chunk, r1 = min(g.rows, r0 + g.chunk);
+    const int nChunks = r1 > r0 ? (r1 - r0 + kWgR - 1) / kWgR : 0;
+    bool ok = true;
+    int last = -1;                     // the last chunk whose MMAs were issued
+    for (int c = 0; c < nChunks && ok; ++c) {
+        const int buf = c & 1;
+        if (c >= 2 && !tc::mbar_wait(&mbar[buf], ((c - 2) >> 1) & 1, g.timeoutNs)) ok = false;   // buffer free
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        const int rb = r0 + c * kWgR;
+        __nv_bfloat16* const tA = reinterpret_cast<__nv_bfloat16*>(sm + (buf ? kWgABytes : 0));
+        __nv_bfloat16* const tB = reinterpret_cast<__nv_bfloat16*>(sm + 2 * kWgABytes + (buf ? bBytes : 0));
+        // X^T: item (k, group of 8 rows): 8 values of feature k, contiguous along the reduction in the layout;
+        // lanes take consecutive features of the same rows, so each of the 8 loads is one coalesced row segment
+        const int itemsA = (K + 1) * (kWgR / 8);
+        for (int it = tid; it < itemsA; it += kTcThreads) {
+            const int rg = it / (K + 1), k = it - rg * (K + 1);
+            float v[8];
+            // the segment holding feature k, picked by selects (no dynamically indexed local array)
+            const int w0 = g.seg[0].width, w1 = g.nseg > 1 ? g.seg[1].width : 0;
+            const int sgi = k < w0 ? 0 : (k < w0 + w1 || g.nseg < 3 ? 1 : 2);
+            const int kk = sgi == 0 ? k : (sgi == 1 ? k - w0 : k - w0 - w1);
+            const float* const base = sgi == 0 ? g.seg[0].base : (sgi == 1 ? g.seg[1].base : g.seg[2].base);
+            const int* const index = sgi == 0 ? g.seg[0].index : (sgi == 1 ? g.seg[1].index : g.seg[2].index);
+            const int width = sgi == 0 ? w0 : (sgi == 1 ? w1 : g.seg[2].width);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int row = rb + 8 * rg + j;
+                float x = 0.0f;
+                if (row < r1) {
+                    if (k == K) {
+                        x = 1.0f;
+                    } else {
+                        const int src = index ? index[row] : row;
+                        x = src >= 0 ? base[(size_t)src * width + kk] : 0.0f;
+                    }
+                }
+                v[j] = x;
+            }
+            stage8(tA + tc::core_offset(k, 8 * rg, kWgR), v);
+        }
+        // G^T: item (output o, group of 8 rows)
+        const int itemsB = N * (kWgR / 8);
+        for (int it = tid; it < itemsB; it += kTcThreads) {
+            const int rg = it / N, o = it - rg * N;
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int row = rb + 8 * rg + j;
+                v[j] = row < r1 ? g.G[(size_t)row * N + o] : 0.0f;
+            }
+            stage8(tB + tc::core_offset(o, 8 * rg, kWgR), v);
+        }
+        tc::fence_proxy_async();   // generic-proxy stores -> visible to the tensor core (async proxy)
+        tc::fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t aBase = tc::smem_u32(tA), bBase = tc::smem_u32(tB);
+            for (int s = 0; s < kWgR / 16; ++s)
+                tc::mma_bf16(tmem, tc::smem_desc(aBase + s * 256u, 128u, sbo),
+                             tc::smem_desc(bBase + s * 256u, 128u, sbo), idesc, c > 0 || s > 0);
+            tc::mma_commit(&mbar[buf]);
+        }
+        last = c;
+    }
+    if (ok && last >= 0 && !tc::mbar_wait(&mbar[last & 1], (last >> 1) & 1, g.timeoutNs)) ok = false;
+    if (__syncthreads_or(!ok)) ok = false;
+    if (ok) {
+        tc::fence_after();
+        const int f = warp * 32 + lane;          // TMEM lane = MMA row = input feature
+        float* out = g.part + (size_t)blockIdx.x * (K + 1) * N;
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            float v[32];
+            if (nChunks > 0) tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            else
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+            if (f <= K)
+#pragma unroll
+                for (int j = 0; j < 32; ++j) out[(size_t)f * N + c0 + j] = v[j];
+        }
+    } else {
+        if (tid == 0) atomicExch(g.error, 1);
+        if (last >= 0) tc::mbar_wait(&mbar[last & 1], (last >> 1) & 1, g.timeoutNs);   // MMAs in flight (bounded)
+        __syncthreads();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
+int tc_wgrad_blocks(int rows, int sms) {
+    const int chunks = (rows + kWgR - 1) / kWgR;
+    return std::max(1, std::min(chunks, std::max(sms, 1)));
+}
+
+// Per-CTA weight-gradient partials of X^T G (and colsum G) on the tensor cores; returns the number of CTAs (rows of
+// partials).  N a multiple of 16 (<= 128), K + 1 <= 128.
+int tc_wgrad(const TcWgradArgs& a, cudaStream_t s, int sms) {
+    if (a.N % 16 || a.N <= 0 || a.N > 128 || a.K <= 0 || a.K + 1 > kWgM) throw bad_arg("weight-gradient shape");
+    if (a.rows <= 0) return 0;
+    int w = 0;
+    for (int i = 0; i < a.nseg; ++i) w += a.seg[i].width;
+    if (w != a.K) throw bad_arg("segment widths must add up to K");
+    const int chunks = (a.rows + kWgR - 1) / kWgR;
+    const int blocks = tc_wgrad_blocks(a.rows, sms);
+    TcWgradArgs b = a;
+    b.chunk = ((chunks + blocks - 1) / blocks) * kWgR;
+    b.timeoutNs = std::max(a.timeoutNs, 200000000LL);
+    const size_t smem = 2 * kWgABytes + 2 * (size_t)a.N * kWgR * 2;
+    static bool attr = false;
+    if (!attr) {
+        NSF_CUDA(cudaFuncSetAttribute(tc_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+        attr = true;
+    }
+    tc_wgrad_kernel<<<blocks, kTcThreads, smem, s>>>(b);
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+    return blocks;
+}
+
 }  // namespace nsf
 
 // ---------------------------------------------------------------------------------------------------
@@ -233,6 +406,52 @@ extern "C" int nsf_tc_dense(nsf_device* h, int rows, int K, int N, const float* 
         NSF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, h->stream));
         NSF_CUDA(cudaStreamSynchronize(h->stream));
         if (e) throw nsf::Error{NSF_ERR_BARRIER_TIMEOUT, "tensor-core layer timed out"};
+        return NSF_OK;
+    } catch (const nsf::Error& e) {
+        h->lastError = e.msg;
+        return e.status;
+    }
+}
+
+// The weight-gradient kernel on host arrays: its known-answer check.
+extern "C" int nsf_tc_weight_gradient(nsf_device* h, int rows, int K, int N, const float* X, const float* G, float* dW,
+                                      float* db) {
+    if (!h || !X || !G || !dW || !db || rows <= 0) return NSF_ERR_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    try {
+        NSF_CUDA(cudaSetDevice(h->device));
+        nsf::DevBuf<float> x, g, part;
+        nsf::DevBuf<int> err;
+        x.upload(X, (size_t)rows * K, h->stream);
+        g.upload(G, (size_t)rows * N, h->stream);
+        const int blocks = nsf::tc_wgrad_blocks(rows, h->smCount);
+        part.alloc((size_t)blocks * (K + 1) * N);
+        err.alloc(1);
+        err.zero(h->stream);
+        nsf::TcWgradArgs a{};
+        a.seg[0] = {x.get(), nullptr, K};
+        a.nseg = 1;
+        a.K = K;
+        a.rows = rows;
+        a.G = g.get();
+        a.N = N;
+        a.part = part.get();
+        a.error = err.get();
+        a.timeoutNs = h->timeoutNs;
+        const int used = nsf::tc_wgrad(a, h->stream, h->smCount);
+        std::vector<float> hp((size_t)used * (K + 1) * N);
+        int e = 0;
+        NSF_CUDA(cudaMemcpyAsync(hp.data(), part.get(), sizeof(float) * hp.size(), cudaMemcpyDeviceToHost, h->stream));
+        NSF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        if (e) throw nsf::Error{NSF_ERR_BARRIER_TIMEOUT, "tensor-core weight gradient timed out"};
+        for (int k = 0; k <= K; ++k)
+            for (int o = 0; o < N; ++o) {
+                double sum = 0.0;
+                for (int b = 0; b < used; ++b) sum += hp[((size_t)b * (K + 1) + k) * N + o];
+                if (k < K) dW[(size_t)k * N + o] = (float)sum;
+                else db[o] = (float)sum;
+            }
         return NSF_OK;
     } catch (const nsf::Error& e) {
         h->lastError = e.msg;

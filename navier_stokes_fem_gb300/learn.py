@@ -8,6 +8,13 @@ precondition at all (a held-out 24 x 24 cavity needed more iterations than plain
 the probe-trained one against 65 for incomplete Cholesky and 147 for Jacobi).
 
     python -m navier_stokes_fem_gb300.learn --steps 1000 --eval-n 512      (prints one JSON line)
+
+The configured study - 4000 training systems (pressure and diffusion matrices of cavities with n uniform in
+[64, 256] and viscosity log-uniform in [1e-3, 1e-1]), 20 000 Adam steps at lr 1e-3, evaluation on 200 held-out
+cavities at n = 512 - is
+
+    python -m navier_stokes_fem_gb300.learn --cavities 250 --probes 8 --slots pressure_stiffness,diffusion \
+        --n-lo 64 --n-hi 256 --steps 20000 --lr 1e-3 --eval-n 512 --eval-seeds 200
 """
 from __future__ import annotations
 
@@ -71,31 +78,63 @@ def train(device: GPUSimulationDevice, seed: int = 0, cavities: int = 6, probes:
     return learner, stats
 
 
+def _timed_solve(device, slot, b, x0, tol, solver):
+    """One solve with its CUDA-event time (the persistent solver launches only)."""
+    device.profile(True)
+    x, it, _ = device.conjugate_gradient(slot, b, x0, eps=tol, solver=solver)
+    ms = float(device.profile_read()["ms"].sum())
+    device.profile(False)
+    return x, int(it), ms
+
+
 def evaluate(device: GPUSimulationDevice, learner: Learner, n: int, seeds=(1001, 1002, 1003), steps: int = 2,
-             tol: float = 1e-8):
-    """Pressure solves of held-out cavities of size n (right-hand sides from steps of the plain method): CG
-    iterations of plain CG, incomplete-Cholesky PCG and learned PCG, FP64, to the same relative residual."""
+             tol: float = 1e-8, slots=("pressure_stiffness",), solver: str = "pcg_fp64"):
+    """Solves of held-out cavities of size n, right-hand sides b = A u from the fields after `steps` steps of the
+    plain method (u: the pressure for the pressure system, the x velocity for the diffusion system), from a zero
+    initial guess: iterations and solve time of plain CG, incomplete-Cholesky PCG and learned PCG to the same
+    relative residual (`solver`: the preconditioned solver's precision; plain CG matches it)."""
+    plain = "fp64" if solver == "pcg_fp64" else "mixed"
     rows = []
     for s in seeds:
         c = training_cavities(1, s, n, n)[0]
         sim = NavierStokesAssembly(M.cavity(n, lid_u=repr(c["lid"])), c["nu"], c["dt"])
         sim.step(steps)
-        _, p = sim.fields()
-        mat = sim.download_matrix("pressure_stiffness")
+        uv, p = sim.fields()
+        mats = {slot: sim.download_matrix(slot) for slot in slots}
         sim.close()
-        device.upload_matrix("pressure_stiffness", *mat)
-        A = device.scipy_matrix("pressure_stiffness")
-        b = A @ p
-        x0 = np.zeros_like(b)
-        row = {"seed": s}
-        _, row["plain"], _ = device.conjugate_gradient("pressure_stiffness", b, x0, eps=tol, solver="fp64")
-        device.precond_ic0("pressure_stiffness")
-        _, row["ic0"], _ = device.conjugate_gradient("pressure_stiffness", b, x0, eps=tol, solver="pcg_fp64")
-        learner.apply("pressure_stiffness", device)
-        x, row["learned"], _ = device.conjugate_gradient("pressure_stiffness", b, x0, eps=tol, solver="pcg_fp64")
-        row["learned_relres"] = float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
-        rows.append(row)
+        for slot in slots:
+            device.upload_matrix(slot, *mats[slot])
+            A = device.scipy_matrix(slot)
+            u = p if slot == "pressure_stiffness" else uv[:A.shape[0]]
+            b = A @ u
+            x0 = np.zeros_like(b)
+            row = {"seed": s, "slot": slot}
+            _, row["plain"], row["plain_ms"] = _timed_solve(device, slot, b, x0, tol, plain)
+            device.precond_ic0(slot)
+            _, row["ic0"], row["ic0_ms"] = _timed_solve(device, slot, b, x0, tol, solver)
+            learner.apply(slot, device)
+            x, row["learned"], row["learned_ms"] = _timed_solve(device, slot, b, x0, tol, solver)
+            row["learned_relres"] = float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+            device.precond_clear(slot)
+            rows.append(row)
     return rows
+
+
+def summarise(rows):
+    """Per slot: mean iterations and ms of each method, learned over IC(0) and over plain, and the worst residual."""
+    out = {}
+    for slot in sorted({r["slot"] for r in rows}):
+        rs = [r for r in rows if r["slot"] == slot]
+        m = {k: float(np.mean([r[k] for r in rs])) for k in ("plain", "ic0", "learned", "plain_ms", "ic0_ms",
+                                                                 "learned_ms")}
+        m["systems"] = len(rs)
+        m["learned_fewer_iterations_than_ic0"] = int(sum(r["learned"] < r["ic0"] for r in rs))
+        m["learned_fewer_iterations_than_plain"] = int(sum(r["learned"] < r["plain"] for r in rs))
+        m["learned_over_ic0_iterations"] = m["learned"] / m["ic0"]
+        m["learned_over_plain_ms"] = m["learned_ms"] / m["plain_ms"]
+        m["worst_learned_relres"] = float(max(r["learned_relres"] for r in rs))
+        out[slot] = m
+    return out
 
 
 def main():
@@ -103,17 +142,30 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cavities", type=int, default=6)
     ap.add_argument("--probes", type=int, default=4)
+    ap.add_argument("--slots", default="pressure_stiffness", help="comma-separated: pressure_stiffness,diffusion")
+    ap.add_argument("--n-lo", type=int, default=64)
+    ap.add_argument("--n-hi", type=int, default=160)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--batch", type=int, default=2)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--eval-n", type=int, default=512)
     ap.add_argument("--eval-seeds", type=int, default=3)
+    ap.add_argument("--eval-solver", default="pcg_fp64", choices=["pcg_fp64", "pcg_mixed"])
+    ap.add_argument("--rows", action="store_true", help="also print every evaluated system")
     args = ap.parse_args()
+    slots = tuple(s for s in args.slots.split(",") if s)
     d = GPUSimulationDevice(0)
-    learner, stats = train(d, args.seed, args.cavities, args.probes, args.steps, args.batch, args.lr)
-    rows = evaluate(d, learner, args.eval_n, seeds=tuple(1000 + k for k in range(args.eval_seeds)))
-    mean = {k: float(np.mean([r[k] for r in rows])) for k in ("plain", "ic0", "learned")}
-    print(json.dumps({"train": stats, "eval_n": args.eval_n, "eval": rows, "mean_iterations": mean}))
+    learner, stats = train(d, args.seed, args.cavities, args.probes, args.steps, args.batch, args.lr, args.n_lo,
+                           args.n_hi, slots)
+    t0 = time.perf_counter()
+    rows = evaluate(d, learner, args.eval_n, seeds=tuple(1000 + k for k in range(args.eval_seeds)), slots=slots,
+                    solver=args.eval_solver)
+    out = {"train": stats, "training_slots": list(slots), "n_range": [args.n_lo, args.n_hi], "eval_n": args.eval_n,
+           "eval_seeds": args.eval_seeds, "eval_solver": args.eval_solver, "eval_s": round(time.perf_counter() - t0, 1),
+           "summary": summarise(rows)}
+    if args.rows:
+        out["eval"] = rows
+    print(json.dumps(out))
     learner.close()
     d.close()
 

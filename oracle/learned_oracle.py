@@ -171,23 +171,23 @@ def loss_and_grad(theta, g, x, b, bf16=False):
     inv = 1.0 / np.maximum(g.deg_l, 1)
     for l in reversed(range(LAYERS)):
         e, h, X, pu, u_, e_new, m, Y, pv, v = t[l]
-        # node update h_new = h + relu(pv) W2n + b2n.  On the GPU the input-gradient products run on the tensor
-        # cores (BF16 operands) and the weight gradients on the FP32 cores; bf16 reproduces that split.
-        G[f"W2n{l}"] = v.T @ dh
-        G[f"b2n{l}"] = dh.sum(axis=0)
+        # node update h_new = h + relu(pv) W2n + b2n.  On the GPU the input-gradient products and these layers'
+        # weight gradients (with their bias sums) run on the tensor cores with BF16 operands; bf16 reproduces that.
+        G[f"W2n{l}"] = _bf(v, bf16).T @ _bf(dh, bf16)
+        G[f"b2n{l}"] = _bf(dh, bf16).sum(axis=0)
         dpv = (_bf(dh, bf16) @ _bf(P[f"W2n{l}"], bf16).T) * (pv > 0)
-        G[f"W1n{l}"] = Y.T @ dpv
-        G[f"b1n{l}"] = dpv.sum(axis=0)
+        G[f"W1n{l}"] = _bf(Y, bf16).T @ _bf(dpv, bf16)
+        G[f"b1n{l}"] = _bf(dpv, bf16).sum(axis=0)
         dY = _bf(dpv, bf16) @ _bf(P[f"W1n{l}"], bf16).T
         dh_prev = dh + dY[:, :H]
         dm = dY[:, H:] * inv[:, None]
         de_new = de + dm[g.c] + dm[g.p]
         # edge update e_new = e + relu(pu) W2e + b2e
-        G[f"W2e{l}"] = u_.T @ de_new
-        G[f"b2e{l}"] = de_new.sum(axis=0)
+        G[f"W2e{l}"] = _bf(u_, bf16).T @ _bf(de_new, bf16)
+        G[f"b2e{l}"] = _bf(de_new, bf16).sum(axis=0)
         dpu = (_bf(de_new, bf16) @ _bf(P[f"W2e{l}"], bf16).T) * (pu > 0)
-        G[f"W1e{l}"] = X.T @ dpu
-        G[f"b1e{l}"] = dpu.sum(axis=0)
+        G[f"W1e{l}"] = _bf(X, bf16).T @ _bf(dpu, bf16)
+        G[f"b1e{l}"] = _bf(dpu, bf16).sum(axis=0)
         dX = _bf(dpu, bf16) @ _bf(P[f"W1e{l}"], bf16).T
         de = de_new + dX[:, :H]
         np.add.at(dh_prev, g.c, dX[:, H:2 * H])

@@ -1,0 +1,61 @@
+"""The workloads at their own sizes, each against the FP64 path on the same GPU:
+
+* the batched form: 64 cavities with n uniform in [16, 256] (seed 20261203), FP64 at tolerance 1e-8, one persistent
+  launch per step - every instance against the single-instance FP64 path after the same steps;
+* the channel 4 x 1 on 1024 x 256 cells with the obstacle removed (about 520 k triangles), nu = 1e-3, dt = 2e-3, its
+  200 steps - the mixed-precision solvers (with the IC(0) pressure factor) against the FP64 solvers.
+
+Two solvers that stop every solve at a 1e-8 relative residual may differ by about cond(A) * 1e-8 per solve; over
+200 steps those differences are carried along, so the mixed form is held to 1e-5 in the velocity and 1e-3 in the
+pressure (the pressure system's condition number grows as h^-2)."""
+import numpy as np
+import pytest
+
+import navier_stokes_fem_gb300 as nsf
+from navier_stokes_fem_gb300 import mesh as M
+from tests._meshes import rel
+
+pytestmark = pytest.mark.gpu
+BATCH_TOL = 1e-8          # the same FP64 CG in a team of CTAs instead of the whole grid: rounding only
+MIXED_TOL_UV = 1e-5
+MIXED_TOL_P = 1e-3
+
+
+def test_batched64_every_instance_matches_single_instance_path():
+    prms = M.batched_cavity_params(64, seed=20261203, n_lo=16, n_hi=256)
+    probs = [(M.cavity(p["n"], lid_u=repr(p["lid"])), p["nu"], p["dt"]) for p in prms]
+    steps = 3
+    b = nsf.BatchedNavierStokes(probs, autotune_rounds=1)
+    it = b.step(steps)
+    assert it.shape == (steps, 64, 5)
+    worst = 0.0
+    for i, (m, nu, dt) in enumerate(probs):
+        s = nsf.NavierStokesAssembly(m, nu, dt)
+        s.step(steps)
+        suv, sp = s.fields()
+        s.close()
+        uv, p = b.fields(i)
+        e = max(rel(uv, suv), rel(p, sp))
+        worst = max(worst, e)
+        assert e < BATCH_TOL, (i, prms[i], e)
+    b.close()
+    print(f"batched64: worst instance rel L2 {worst:.2e}")
+
+
+def test_channel_1024x256_200_steps_mixed_against_fp64():
+    m = M.channel_with_obstacle(1024, 256)
+    steps = 200
+    fp = nsf.NavierStokesAssembly(m, 1e-3, 2e-3, solver="fp64")
+    fp.step(steps)
+    uv64, p64 = fp.fields()
+    fp.close()
+    mx = nsf.NavierStokesAssembly(m, 1e-3, 2e-3, solver="pcg_mixed")
+    mx.precond_ic0("pressure_stiffness")
+    mx.step(steps)
+    uv, p = mx.fields()
+    mx.close()
+    nv = m.n_nodes
+    eu, ev, ep = rel(uv[:nv], uv64[:nv]), rel(uv[nv:], uv64[nv:]), rel(p, p64)
+    print(f"channel 1024x256, 200 steps: mixed vs FP64 rel L2 u {eu:.2e} v {ev:.2e} p {ep:.2e}")
+    assert np.isfinite(uv).all() and np.isfinite(p).all()
+    assert eu < MIXED_TOL_UV and ev < MIXED_TOL_UV and ep < MIXED_TOL_P

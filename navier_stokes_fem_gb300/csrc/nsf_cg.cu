@@ -253,7 +253,7 @@ void cg_configure(CgWorkspace& ws, int device) {
         NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kCgThreads, 0));
         if (o < perSm) ws.pipeOk = false;
     }
-    ws.partials.alloc((size_t)6 * std::max(ws.grid, ws.gridInner));
+    ws.partials.alloc((size_t)9 * std::max(ws.grid, ws.gridInner));   // (the pipelined FP64 CG uses 9 regions)
     ws.sync.alloc(1);
     ws.info.alloc(4096);
     ws.loop.alloc(1);

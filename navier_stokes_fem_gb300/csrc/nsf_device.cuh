@@ -953,16 +953,32 @@ static __device__ int team_cg_fp64(Team& t, const CgArgs& a, double* stage, doub
 //                                                                                    at the first iteration)
 //     z = A w + beta z,  s = w + beta s,  p = r + beta p,  x += alpha p,  r -= alpha s,  w' = w - alpha z,
 // with the partials of r'.r' and w'.r' formed in the same pass.  In exact arithmetic it is the CG of team_cg_fp64;
-// in floating point its recurrences drift a little further from the true residual, so the solve finishes with
-// r = b - A x recomputed and tested, and continues (from that residual) when the drift left it above tolerance.
+// in floating point its recurrences drift from the true residual, so every kPipeReplaceEvery iterations, and
+// whenever the recursive residual meets the tolerance, r, w, s and z are replaced by b - A x, A r, A p and A s
+// (residual replacement, after Cools, Yetkin, Agullo, Giraud and Vanroose 2018) and the recurrence continues; the
+// replacement's true residual is also the stopping test.
 // w is written to the other of two buffers (the product of this iteration still gathers the current one), and the
 // partials alternate between region pairs {0, 1} and {2, 3}: one barrier separates an iteration's partial writes
-// from the next iteration's reads, and the next writes go to the other pair.  Regions 4 and 5: b.b and r0.r0.
+// from the next iteration's reads, and the next writes go to the other pair.  Regions 4 and 5: b.b and r.r;
+// 6, 7 and 8: r.s, p.w and p.s after a replacement.
 // Vectors: r = a.r, s = a.q, p = a.pbuf0, z = a.pbuf1, w = a.wbuf0 / a.wbuf1.  Needs the SELL copy.
 // ---------------------------------------------------------------------------------------------------
 struct PipeRow {
     double z, s, p, r, x, w;
 };
+
+constexpr int kPipeMaxChecks = 16;      // replacements after the recursive residual met the tolerance, per solve
+// Iterations between residual replacements.  Left alone, the recurrences drift: on the 256^2 cavity's pressure
+// system the recursive residual met 1e-8 after 1562 iterations with the true one at 1.5e-7 (plain CG: 1557
+// iterations).  Replaced every 25 to 400 iterations the pipelined form took exactly plain CG's 1557 (a NumPy model
+// of this routine); a replacement costs four products and two barriers.
+constexpr int kPipeReplaceEvery = 100;
+
+template <bool Wide = false, typename Gather, typename Epi>
+__device__ __forceinline__ void pipe_product(const CgArgs& a, int rb, int re, double* stage, Gather gather, Epi epi) {
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col,
+                                                               a.val, rb, re, stage, gather, epi);
+}
 
 template <bool Wide = false>
 static __device__ int team_cg_fp64_pipelined(Team& t, const CgArgs& a, double* stage, double* smem) {
@@ -971,125 +987,179 @@ static __device__ int team_cg_fp64_pipelined(Team& t, const CgArgs& a, double* s
     team_rows(a.n, t, rb, re);
     const double* b = a.bRowptr ? a.bOut : a.b;
     build_rhs<Wide>(a, rb, re, stage);
-    int it = 0, status = NSF_ERR_NOT_CONVERGED, where = 1, restarts = 0;
-    double rr = 0, bb = 0, target = 0;
-    const double* xsrc = a.x0;
-    // (re)start: r = b - A x (x = x0 the first time), test it, then w = A r with the partials of r.r and w.r
-    for (;;) {
+    int it = 0, where = 1, checks = 0;
+#define NSF_PIPE_BARRIER()                                                                        \
+    if (!t.barrier(where++)) {                                                                    \
+        write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1 + checks, rr, bb);                        \
+        return NSF_ERR_BARRIER_TIMEOUT;                                                           \
+    }
+    double rr = 0, bb = 0;
+    // r = b - A x (x = x0 first, copied to x), its r.r in region 5 (and b.b in region 4 the first time)
+    auto true_residual = [&](const double* xs, bool first) {
         double rrp = 0, bbp = 0;
-        matrix_product<double, double, false, kResidU<Wide>, Wide>(
-            a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return xsrc[c]; },
-            [&](int row, double acc, double xi) {
-                const double bi = b[row];
-                const double ri = bi - acc;
-                a.r[row] = ri;
-                if (a.x != xsrc) a.x[row] = xi;
-                rrp = fma(ri, ri, rrp);
-                bbp = fma(bi, bi, bbp);
-            });
+        pipe_product<Wide>(a, rb, re, stage, [&](int c) { return xs[c]; }, [&](int row, double acc, double xi) {
+            const double bi = b[row];
+            const double ri = bi - acc;
+            a.r[row] = ri;
+            if (first && a.x != xs) a.x[row] = xi;
+            rrp = fma(ri, ri, rrp);
+            bbp = fma(bi, bi, bbp);
+        });
         rrp = block_sum(rrp, smem);
         bbp = block_sum(bbp, smem);
-        if (threadIdx.x == 0) { a.partials[4 * G + t.rank] = bbp; a.partials[5 * G + t.rank] = rrp; }
-        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-        bb = grid_sum(a.partials + 4 * G, G, smem);
-        rr = grid_sum(a.partials + 5 * G, G, smem);
-        target = bb > 0 ? a.tol2 * bb : (restarts == 0 ? a.tol2 * rr : target);
-        if (!(rr == rr) || !(bb == bb) || isinf(rr) || isinf(bb)) { status = NSF_ERR_BREAKDOWN; break; }
-        if (rr <= target) { status = NSF_OK; break; }
-        if (it >= a.maxIt || restarts > 8) break;
+        if (threadIdx.x == 0) {
+            a.partials[5 * G + t.rank] = rrp;
+            if (first) a.partials[4 * G + t.rank] = bbp;
+        }
+    };
+    true_residual(a.x0, true);
+    NSF_PIPE_BARRIER();
+    bb = grid_sum(a.partials + 4 * G, G, smem);
+    rr = grid_sum(a.partials + 5 * G, G, smem);
+    const double target = bb > 0 ? a.tol2 * bb : a.tol2 * rr;
+    if (!(rr == rr) || !(bb == bb) || isinf(rr) || isinf(bb)) {
+        write_info(t, a, 0, NSF_ERR_BREAKDOWN, 1, rr, bb);
+        return NSF_ERR_BREAKDOWN;
+    }
+    if (rr <= target || a.maxIt <= 0) {
+        const int st = rr <= target ? NSF_OK : NSF_ERR_NOT_CONVERGED;
+        write_info(t, a, 0, st, 1, rr, bb);
+        return st;
+    }
+    // w = A r into the buffer the first iteration reads, with the partials of r.r and w.r in pair 0
+    {
         double gp = 0, dp = 0;
-        matrix_product<double, double, false, kResidU<Wide>, Wide>(
-            a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return a.r[c]; },
-            [&](int row, double acc, double ri) {
-                a.wbuf0[row] = acc;
-                gp = fma(ri, ri, gp);
-                dp = fma(acc, ri, dp);
-            });
+        pipe_product<Wide>(a, rb, re, stage, [&](int c) { return a.r[c]; }, [&](int row, double acc, double ri) {
+            a.wbuf0[row] = acc;
+            gp = fma(ri, ri, gp);
+            dp = fma(acc, ri, dp);
+        });
         gp = block_sum(gp, smem);
         dp = block_sum(dp, smem);
         if (threadIdx.x == 0) { a.partials[t.rank] = gp; a.partials[G + t.rank] = dp; }
-        if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-        xsrc = a.x;
-        // the iterations; k counts them since this (re)start (its parity picks the w buffer and the partial pair)
-        double gammaPrev = 1.0, alphaPrev = 1.0;
-        bool drifted = false;
-        for (int k = 0;; ++k) {
-            const int par = k & 1;
-            const double gamma = grid_sum(a.partials + (2 * par) * G, G, smem);
-            const double delta = grid_sum(a.partials + (2 * par + 1) * G, G, smem);
-            if (!(gamma == gamma) || isinf(gamma)) { status = NSF_ERR_BREAKDOWN; break; }
-            if (gamma <= target) { drifted = true; break; }     // confirmed against the true residual below
-            if (it >= a.maxIt) break;
-            const double beta = k == 0 ? 0.0 : gamma / gammaPrev;
-            const double den = k == 0 ? delta : delta - beta * gamma / alphaPrev;
-            if (!(den > 0.0) || isinf(den)) { status = NSF_ERR_BREAKDOWN; break; }
-            const double alpha = block_scalar(smem, [&] { return gamma / den; });
-            const double* wc = par ? a.wbuf1 : a.wbuf0;
-            double* wn = par ? a.wbuf0 : a.wbuf1;
-            double gn = 0, dn = 0;
-            auto gw = [&](int c) { return wc[c]; };
-            auto pre = [&](int row) {
-                PipeRow q;
-                q.r = a.r[row];
-                q.x = a.x[row];
-                q.w = wc[row];
-                if (k > 0) { q.z = a.pbuf1[row]; q.s = a.q[row]; q.p = a.pbuf0[row]; }
-                else { q.z = 0.0; q.s = 0.0; q.p = 0.0; }
-                return q;
-            };
-            auto epi = [&](int row, double acc, const PipeRow& q) {
-                const double z = fma(beta, q.z, acc);
-                const double sv = fma(beta, q.s, q.w);
-                const double pv = fma(beta, q.p, q.r);
-                a.pbuf1[row] = z;
-                a.q[row] = sv;
-                a.pbuf0[row] = pv;
-                a.x[row] = fma(alpha, pv, q.x);
-                const double rn = fma(-alpha, sv, q.r);
-                const double wv = fma(-alpha, z, q.w);
-                a.r[row] = rn;
-                wn[row] = wv;
-                gn = fma(rn, rn, gn);
-                dn = fma(wv, rn, dn);
-            };
-            if constexpr (Wide) sell_rows_wide<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal,
-                                                                               rb, re, gw, pre, epi);
-            else if (a.sellMaxW <= 5) sell_rows<double, double, false, 1, 5>(a.sellStart, a.sellCol, a.sellVal, rb,
-                                                                            re, gw, pre, epi);
-            else sell_rows<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal, rb, re, gw, pre, epi);
-            gn = block_sum(gn, smem);
-            dn = block_sum(dn, smem);
-            const int np = (k + 1) & 1;
-            if (threadIdx.x == 0) { a.partials[(2 * np) * G + t.rank] = gn; a.partials[(2 * np + 1) * G + t.rank] = dn; }
-            if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, gamma, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-            ++it;
-            gammaPrev = gamma;
-            alphaPrev = alpha;
-        }
-        if (status == NSF_ERR_BREAKDOWN || (!drifted && it >= a.maxIt)) {
-            if (it >= a.maxIt && status != NSF_ERR_BREAKDOWN) {
-                // out of budget: report the true residual of the last iterate
-                xsrc = a.x;
-                double rrp2 = 0;
-                matrix_product<double, double, false, kResidU<Wide>, Wide>(
-                    a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage,
-                    [&](int c) { return a.x[c]; }, [&](int row, double acc, double) {
-                        const double ri = b[row] - acc;
-                        rrp2 = fma(ri, ri, rrp2);
-                    });
-                rrp2 = block_sum(rrp2, smem);
-                if (threadIdx.x == 0) a.partials[5 * G + t.rank] = rrp2;
-                if (!t.barrier(where++)) { write_info(t, a, it, NSF_ERR_BARRIER_TIMEOUT, 1, rr, bb); return NSF_ERR_BARRIER_TIMEOUT; }
-                rr = grid_sum(a.partials + 5 * G, G, smem);
-                if (rr <= target) status = NSF_OK;
-            }
-            break;
-        }
-        // the recursive residual met the tolerance: recompute r = b - A x and test it (the loop head); a drifted
-        // recurrence restarts from the true residual
-        ++restarts;
+        NSF_PIPE_BARRIER();
     }
-    write_info(t, a, it, status, 1 + restarts, rr, bb);
+    int status = NSF_ERR_NOT_CONVERGED;
+    double gammaPrev = 1.0, alphaPrev = 1.0;
+    bool explicitDen = false;
+    int lastReplaced = 0;
+    for (int k = 0;;) {
+        const int par = k & 1;
+        const double gamma = grid_sum(a.partials + (2 * par) * G, G, smem);
+        const double delta = grid_sum(a.partials + (2 * par + 1) * G, G, smem);
+        if (!(gamma == gamma) || isinf(gamma)) { status = NSF_ERR_BREAKDOWN; break; }
+        double* wc = par ? a.wbuf1 : a.wbuf0;
+        const bool met = gamma <= target;
+        if (met || it >= a.maxIt || (k > 0 && it - lastReplaced >= kPipeReplaceEvery)) {
+            // replacement: r = b - A x and s = A p (p is the recurrence's once an iteration has run) ...
+            double rrp = 0;
+            pipe_product<Wide>(a, rb, re, stage, [&](int c) { return a.x[c]; }, [&](int row, double acc, double) {
+                const double ri = b[row] - acc;
+                a.r[row] = ri;
+                rrp = fma(ri, ri, rrp);
+            });
+            if (k > 0)
+                pipe_product<Wide>(a, rb, re, stage, [&](int c) { return a.pbuf0[c]; },
+                                   [&](int row, double acc, double) { a.q[row] = acc; });
+            rrp = block_sum(rrp, smem);
+            if (threadIdx.x == 0) a.partials[5 * G + t.rank] = rrp;
+            NSF_PIPE_BARRIER();
+            rr = grid_sum(a.partials + 5 * G, G, smem);
+            if (met) ++checks;
+            if (!(rr == rr) || isinf(rr)) { status = NSF_ERR_BREAKDOWN; break; }
+            if (rr <= target) { status = NSF_OK; break; }
+            if (it >= a.maxIt || checks >= kPipeMaxChecks) break;
+            // ... then w = A r and z = A s with r.r and w.r for this k, and, since the short form of p.Ap below
+            // rests on orthogonality relations the replacement breaks, r.s, p.w and p.s for the explicit
+            // p.Ap = (r + beta p).(w + beta s) of the next iteration (regions 6, 7, 8)
+            pipe_product<Wide>(a, rb, re, stage, [&](int c) { return a.r[c]; },
+                               [&](int row, double acc, double) { wc[row] = acc; });
+            double gp = 0, dp = 0, rsp = 0, pwp = 0, psp = 0;
+            pipe_product<Wide>(a, rb, re, stage, [&](int c) { return k > 0 ? a.q[c] : 0.0; },
+                               [&](int row, double acc, double) {
+                                   const double ri = a.r[row], wi = wc[row];
+                                   gp = fma(ri, ri, gp);
+                                   dp = fma(wi, ri, dp);
+                                   if (k > 0) {
+                                       a.pbuf1[row] = acc;
+                                       const double si = a.q[row], pi = a.pbuf0[row];
+                                       rsp = fma(ri, si, rsp);
+                                       pwp = fma(pi, wi, pwp);
+                                       psp = fma(pi, si, psp);
+                                   }
+                               });
+            gp = block_sum(gp, smem);
+            dp = block_sum(dp, smem);
+            rsp = block_sum(rsp, smem);
+            pwp = block_sum(pwp, smem);
+            psp = block_sum(psp, smem);
+            if (threadIdx.x == 0) {
+                a.partials[(2 * par) * G + t.rank] = gp;
+                a.partials[(2 * par + 1) * G + t.rank] = dp;
+                a.partials[6 * G + t.rank] = rsp;
+                a.partials[7 * G + t.rank] = pwp;
+                a.partials[8 * G + t.rank] = psp;
+            }
+            NSF_PIPE_BARRIER();
+            explicitDen = k > 0;
+            lastReplaced = it;
+            continue;   // the same k: its gamma and delta are the replaced ones
+        }
+        const double beta = k == 0 ? 0.0 : gamma / gammaPrev;
+        double den = k == 0 ? delta : delta - beta * gamma / alphaPrev;
+        if (explicitDen) {
+            const double rs = grid_sum(a.partials + 6 * G, G, smem);
+            const double pw = grid_sum(a.partials + 7 * G, G, smem);
+            const double ps = grid_sum(a.partials + 8 * G, G, smem);
+            den = delta + beta * (rs + pw) + beta * beta * ps;
+            explicitDen = false;
+        }
+        if (!(den > 0.0) || isinf(den)) { status = NSF_ERR_BREAKDOWN; break; }
+        const double alpha = block_scalar(smem, [&] { return gamma / den; });
+        double* wn = par ? a.wbuf0 : a.wbuf1;
+        double gn = 0, dn = 0;
+        auto gw = [&](int c) { return wc[c]; };
+        auto pre = [&](int row) {
+            PipeRow q;
+            q.r = a.r[row];
+            q.x = a.x[row];
+            q.w = wc[row];
+            if (k > 0) { q.z = a.pbuf1[row]; q.s = a.q[row]; q.p = a.pbuf0[row]; }
+            else { q.z = 0.0; q.s = 0.0; q.p = 0.0; }
+            return q;
+        };
+        auto epi = [&](int row, double acc, const PipeRow& q) {
+            const double z = fma(beta, q.z, acc);
+            const double sv = fma(beta, q.s, q.w);
+            const double pv = fma(beta, q.p, q.r);
+            a.pbuf1[row] = z;
+            a.q[row] = sv;
+            a.pbuf0[row] = pv;
+            a.x[row] = fma(alpha, pv, q.x);
+            const double rn = fma(-alpha, sv, q.r);
+            const double wv = fma(-alpha, z, q.w);
+            a.r[row] = rn;
+            wn[row] = wv;
+            gn = fma(rn, rn, gn);
+            dn = fma(wv, rn, dn);
+        };
+        if constexpr (Wide) sell_rows_wide<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal, rb,
+                                                                           re, gw, pre, epi);
+        else if (a.sellMaxW <= 5) sell_rows<double, double, false, 1, 5>(a.sellStart, a.sellCol, a.sellVal, rb, re,
+                                                                        gw, pre, epi);
+        else sell_rows<double, double, false, 1, kUnroll>(a.sellStart, a.sellCol, a.sellVal, rb, re, gw, pre, epi);
+        gn = block_sum(gn, smem);
+        dn = block_sum(dn, smem);
+        const int np = (k + 1) & 1;
+        if (threadIdx.x == 0) { a.partials[(2 * np) * G + t.rank] = gn; a.partials[(2 * np + 1) * G + t.rank] = dn; }
+        NSF_PIPE_BARRIER();
+        ++it;
+        ++k;
+        gammaPrev = gamma;
+        alphaPrev = alpha;
+    }
+#undef NSF_PIPE_BARRIER
+    write_info(t, a, it, status, 1 + checks, rr, bb);
     return status;
 }
 

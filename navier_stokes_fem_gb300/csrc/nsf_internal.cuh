@@ -222,7 +222,7 @@ struct CgArgs {
     float* q32;
     float* p32a;
     float* p32b;
-    double* partials;   // 4 * gridDim.x
+    double* partials;   // per-CTA partial sums: up to 9 regions of gridDim.x entries
     GridSync* sync;
     CgInfo* info;
     int maxIt;

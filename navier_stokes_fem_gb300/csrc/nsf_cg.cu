@@ -108,6 +108,26 @@ __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_ct
     team_pcg_mixed_inner<C16, true>(t, a, nullptr, smem, nullptr);
 }
 
+// The same 1024-thread form with the row state only its CTA reads (the FP32 correction, and r and q of its colour-1
+// rows) in dynamic shared memory for the whole launch: two colours only, and only where that state fits.
+template <bool C16>
+__global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_resident(CgArgs a) {
+    __shared__ double smem[kSmemSlots];
+    if (!a.sellStart || a.f.colours != 2) return;   // (the host never launches it otherwise)
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_mixed_inner<C16, true, true>(t, a, nullptr, smem, nullptr);
+}
+
+// Shared-memory bytes pcg_mixed_inner_kernel_resident needs on `grid` CTAs for a factor's colour blocks: per CTA
+// its share of each block (team_block's rule) as d, plus r and q of its colour-1 share.
+static size_t resident_bytes(const FactorView& f, int grid) {
+    auto share = [&](int c) {
+        const int slices = (f.colourRow[c + 1] - f.colourRow[c]) / kSlice;
+        return (size_t)((slices + grid - 1) / grid) * kSlice;
+    };
+    return sizeof(float) * (share(0) + 3 * share(1));
+}
+
 // The split plain mixed CG for wide (P2) systems: refresh launches (fold, FP64 true residual, tests) at 2 CTAs per
 // SM and FP32 iteration launches at 4.
 static __device__ void team_cg_mixed_refresh(Team& t, const CgArgs& a, double* stage, double* smem) {
@@ -246,6 +266,25 @@ void cg_configure(CgWorkspace& ws, int device) {
         o1024 = std::min(o1024, o);
     }
     ws.gridInner1024 = sms * o1024;
+    // the resident form: the largest dynamic shared memory at which it still runs one 1024-thread CTA per SM
+    ws.residentMaxBytes = 0;
+    if (o1024 == 1) {
+        int optin = 0;
+        NSF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        size_t best = 0;
+        for (const void* fn : {(const void*)pcg_mixed_inner_kernel_resident<true>,
+                               (const void*)pcg_mixed_inner_kernel_resident<false>}) {
+            cudaFuncAttributes fa{};
+            NSF_CUDA(cudaFuncGetAttributes(&fa, fn));
+            const int dyn = optin - (int)fa.sharedSizeBytes;
+            NSF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+            int o = 0;
+            NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kInnerCtaThreads, (size_t)dyn));
+            const size_t ok = o >= 1 ? (size_t)dyn : 0;
+            best = best == 0 ? ok : std::min(best, ok);
+        }
+        ws.residentMaxBytes = best;
+    }
     // the pipelined FP64 CG runs on the same grid; it is offered only where that grid is co-resident for it
     ws.pipeOk = true;
     for (const void* fn : {(const void*)cg_fp64_pipe_kernel<false>, (const void*)cg_fp64_pipe_kernel<true>}) {
@@ -283,7 +322,7 @@ void cg_launch(CgWorkspace& ws, const CgArgs& args, int mode, bool wide, cudaStr
 // (inner1024: the 1024-thread form, used when given, resident on the device and the matrix has a SELL copy; else
 // inner256 at ws.gridInner CTAs.)
 static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t refreshDsm, const void* inner1024,
-                         const void* inner256, cudaStream_t s) {
+                         const void* inner256, cudaStream_t s, size_t inner1024Dsm = 0) {
     a.loop = ws.loop.get();
     auto launch = [&](const void* fn, int grid, int block, size_t dsm) {
         NSF_CUDA(cudaMemsetAsync(ws.sync.get(), 0, sizeof(GridSync), s));
@@ -304,7 +343,7 @@ static void split_launch(CgWorkspace& ws, CgArgs a, const void* refresh, size_t 
         NSF_CUDA(cudaMemcpyAsync(&state, &a.loop->state, sizeof(int), cudaMemcpyDeviceToHost, s));
         NSF_CUDA(cudaStreamSynchronize(s));
         if (state != kLoopInner) return;
-        launch(inner, innerGrid, innerBlock, 0);
+        launch(inner, innerGrid, innerBlock, cta1024 ? inner1024Dsm : 0);
         launch(refresh, ws.grid, ws.block, refreshDsm);
     }
     throw Error{NSF_ERR_CUDA, "mixed-precision solve did not finish within its refresh budget"};
@@ -322,7 +361,17 @@ void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
                             : c16           ? (const void*)pcg_mixed_inner_kernel_cta1024<true>
                                             : (const void*)pcg_mixed_inner_kernel_cta1024<false>;
     const void* inner256 = c16 ? (const void*)pcg_mixed_inner_kernel<true> : (const void*)pcg_mixed_inner_kernel<false>;
-    split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner1024, inner256, s);
+    // two colours and the row state fits one CTA per SM: the resident form
+    size_t dsm = 0;
+    if (a.f.colours == 2 && a.sellStart && ws.gridInner1024 > 0 && ws.residentMaxBytes > 0) {
+        const size_t need = resident_bytes(a.f, ws.gridInner1024);
+        if (need <= ws.residentMaxBytes) {
+            inner1024 = c16 ? (const void*)pcg_mixed_inner_kernel_resident<true>
+                            : (const void*)pcg_mixed_inner_kernel_resident<false>;
+            dsm = need;
+        }
+    }
+    split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner1024, inner256, s, dsm);
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.

@@ -264,6 +264,7 @@ struct CgWorkspace {
     int gridInner = 0;       // grid of the split mixed PCG's inner-iteration kernel
     int gridInner1024 = 0;   // (its one-CTA-per-SM form)
     bool pipeOk = false;     // the pipelined FP64 CG kernels are co-resident on `grid`
+    size_t residentMaxBytes = 0;   // shared memory the resident inner PCG kernel may take (0: not offered)
 };
 
 // launch helpers implemented in nsf_cg.cu / nsf_sparse.cu

@@ -492,7 +492,17 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
 // (the same arithmetic as the stored y0, so the sweep sees the same values); rows of colours >= 2 update d and r.  The residual alternates between two buffers, since the neighbours' previous r is read while the
 // own rows' new r is written.  On two colours an iteration has 3 grid barriers instead of 4.
 // (C16: the product and the sweeps read the 16-bit column copies of the matrix and of both factor parts.)
-template <bool C16 = false>
+//
+// Resident (two colours only, one CTA per SM): the rows a CTA updates are the same in every phase - its share of
+// each colour block, the product included - so the state only that CTA reads lives in its shared memory `rs` for
+// the whole launch instead of in HBM: the FP32 correction d of all its rows, and r and q of its colour-1 rows
+// (no other CTA gathers them: the colour-1 sweep gathers colour-0 neighbours only, and with two colours the
+// backward sweep is colour 0's).  Layout in nsf_row_state: d of the colour-0 rows, d of the colour-1 rows, r1, q1.  d and r1 are
+// loaded when the launch starts and written back when it ends; 16 of the about 118 bytes per row and iteration
+// that the iterations move stay on the chip.
+extern __shared__ __align__(16) float nsf_row_state[];   // the resident form's dynamic shared memory
+
+template <bool C16 = false, bool Resident = false>
 static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
                                              PcgLoop& L, int& where) {
     const FactorView& F = a.f;
@@ -502,6 +512,24 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
     float* w = F.w32;
     const float* dinv = F.dinv32;
     L.innerBreakdown = 0;
+    // Resident: this CTA's colour-0 rows [c0b, c0b + n0) and colour-1 rows [c1b, c1b + n1); their state is indexed
+    // in the kernel's dynamic shared memory (nsf_row_state) by 32-bit offsets: d0 at [0, n0), d1 at [n0, n0 + n1),
+    // r1 at n0 + n1, q1 at n0 + 2 n1
+    int c0b = 0, c1b = 0, n0 = 0, n1 = 0;
+    if constexpr (Resident) {
+        int e0, e1;
+        team_block(F.colourRow[0], F.colourRow[1], t, c0b, e0);
+        team_block(F.colourRow[1], F.colourRow[2], t, c1b, e1);
+        n0 = e0 - c0b;
+        n1 = e1 - c1b;
+        const float* rCur = L.rflip ? a.r32b : a.r32;
+        for (int k = threadIdx.x; k < n0; k += bs) nsf_row_state[k] = a.d32[c0b + k];
+        for (int k = threadIdx.x; k < n1; k += bs) {
+            nsf_row_state[n0 + k] = a.d32[c1b + k];
+            nsf_row_state[n0 + n1 + k] = rCur[c1b + k];
+        }
+        __syncthreads();
+    }
     // The tests on p.q and r.r and the coefficient alpha are thread 0's, handed to every thread as decisions; the
     // r.z test and beta stay per thread (thread 0 alone owning them made the 64-register kernel spill).
     const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
@@ -519,8 +547,25 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
             df_acc(pqHi, pqLo, pi, acc);
         };
         // chunks as wide as the widest slice when that is 5 (a structured P1 system without its exact zeros)
-        if (a.sellMaxW <= 5) product32<false, 5, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
-        else product32<false, 6, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        if constexpr (Resident) {
+            // this CTA's colour-0 share, then its colour-1 share, whose q stays in shared memory
+            auto ep1 = [&](int row, float acc, float pi) {
+                pc[row] = pi;
+                nsf_row_state[n0 + 2 * n1 + row - c1b] = acc;
+                df_acc(pqHi, pqLo, pi, acc);
+            };
+            if (a.sellMaxW <= 5) {
+                product32<false, 5, C16>(ring, a, c0b, c0b + n0, reinterpret_cast<float*>(stage), gp, ep);
+                product32<false, 5, C16>(ring, a, c1b, c1b + n1, reinterpret_cast<float*>(stage), gp, ep1);
+            } else {
+                product32<false, 6, C16>(ring, a, c0b, c0b + n0, reinterpret_cast<float*>(stage), gp, ep);
+                product32<false, 6, C16>(ring, a, c1b, c1b + n1, reinterpret_cast<float*>(stage), gp, ep1);
+            }
+        } else if (a.sellMaxW <= 5) {
+            product32<false, 5, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        } else {
+            product32<false, 6, C16>(ring, a, rb, re, reinterpret_cast<float*>(stage), gp, ep);
+        }
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;
@@ -549,7 +594,8 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                     if (i < r1) {
                         pi[u] = pc[i];
                         qi[u] = a.q32[i];
-                        di[u] = a.d32[i];
+                        if constexpr (Resident) di[u] = nsf_row_state[i - c0b];   // (Resident: c == 0 only)
+                        else di[u] = a.d32[i];
                         ri[u] = rOld[i];
                         vi[u] = c == 0 ? dinv[i] : 0.0f;
                     }
@@ -558,7 +604,8 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                 for (int u = 0; u < kRowsLean; ++u) {
                     const int i = i0 + u * bs;
                     if (i < r1) {
-                        a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                        if constexpr (Resident) nsf_row_state[i - c0b] = fmaf(alphaf, pi[u], di[u]);
+                        else a.d32[i] = fmaf(alphaf, pi[u], di[u]);
                         const float rn = fmaf(-alphaf, qi[u], ri[u]);
                         rNew[i] = rn;
                         df_acc(rrHi, rrLo, rn, rn);
@@ -581,9 +628,17 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                 F.loStart, loCol, F.loVal32, r0, r1,
                 [&](int j) { return fmaf(-alphaf, a.q32[j], rOld[j]) * dinv[j]; },
                 [&](int i) {
-                    const float rn = fmaf(-alphaf, a.q32[i], rOld[i]);
-                    a.d32[i] = fmaf(alphaf, pc[i], a.d32[i]);
-                    rNew[i] = rn;
+                    float rn;
+                    if constexpr (Resident) {
+                        const int k = i - c1b;
+                        rn = fmaf(-alphaf, nsf_row_state[n0 + 2 * n1 + k], nsf_row_state[n0 + n1 + k]);
+                        nsf_row_state[n0 + k] = fmaf(alphaf, pc[i], nsf_row_state[n0 + k]);
+                        nsf_row_state[n0 + n1 + k] = rn;
+                    } else {
+                        rn = fmaf(-alphaf, a.q32[i], rOld[i]);
+                        a.d32[i] = fmaf(alphaf, pc[i], a.d32[i]);
+                        rNew[i] = rn;
+                    }
                     df_acc(rrHi, rrLo, rn, rn);
                     return SweepRow<float>{rn, dinv[i], 0.0f};
                 },
@@ -618,6 +673,15 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
         L.rz = rzs;
         betaf = (float)L.beta;
+    }
+    if constexpr (Resident) {   // d of every own row and r of the colour-1 rows back to their global copies
+        __syncthreads();
+        float* rCur = L.rflip ? a.r32b : a.r32;
+        for (int k = threadIdx.x; k < n0; k += bs) a.d32[c0b + k] = nsf_row_state[k];
+        for (int k = threadIdx.x; k < n1; k += bs) {
+            a.d32[c1b + k] = nsf_row_state[n0 + k];
+            rCur[c1b + k] = nsf_row_state[n0 + n1 + k];
+        }
     }
     L.state = kLoopRefresh;
     return true;
@@ -725,8 +789,9 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
     pcg_loop_store(t, a, L);
 }
 
-// (FusedOnly: the caller guarantees two or more colours; the one-colour loop and its CSR staging are left out.)
-template <bool C16 = false, bool FusedOnly = false>
+// (FusedOnly: the caller guarantees two or more colours; the one-colour loop and its CSR staging are left out.
+// Resident: the caller guarantees exactly two colours and dynamic shared memory for the row state.)
+template <bool C16 = false, bool FusedOnly = false, bool Resident = false>
 static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
     int where = 400;
     // the fields the inner iterations read or write (the rest of the state stays in memory)
@@ -741,7 +806,8 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.flip = G.flip;
     L.rflip = G.rflip;
     bool ok;
-    if constexpr (FusedOnly) ok = pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where);
+    if constexpr (Resident) ok = pcg_mixed_inner_fused<C16, true>(t, a, stage, smem, ring, L, where);
+    else if constexpr (FusedOnly) ok = pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where);
     else ok = a.f.colours >= 2 ? pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where)
                                : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);

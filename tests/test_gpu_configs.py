@@ -16,7 +16,7 @@ from navier_stokes_fem_gb300 import mesh as M
 from tests._meshes import rel
 
 pytestmark = pytest.mark.gpu
-BATCH_TOL = 1e-8          # the same FP64 CG in a team of CTAs instead of the whole grid: rounding only
+BATCH_TOL = 1e-8          # the same (three-barrier) FP64 CG in a team of CTAs instead of the whole grid: rounding only
 MIXED_TOL_UV = 1e-5
 MIXED_TOL_P = 1e-3
 
@@ -31,6 +31,7 @@ def test_batched64_every_instance_matches_single_instance_path():
     worst = 0.0
     for i, (m, nu, dt) in enumerate(probs):
         s = nsf.NavierStokesAssembly(m, nu, dt)
+        s.set_cg_form("three_sync")   # the batched step kernel's form of the FP64 CG
         s.step(steps)
         suv, sp = s.fields()
         s.close()

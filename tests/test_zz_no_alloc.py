@@ -44,6 +44,7 @@ def test_noalloc_matches_regular_entry_point_twice():
     o = oracle.Oracle(m, 0.01, 0.01)
     A = o.scipy_matrix("pressure_stiffness")
     d = nsf.GPUSimulationDevice(0)
+    d.set_cg_form("three_sync")       # the regular entry point's form of the same FP64 CG the allocation-free one runs
     d.upload_matrix("pressure_stiffness", A.indptr.astype(np.int32), A.indices, A.data, A.shape)
     rng = np.random.default_rng(21)
     for call in range(2):

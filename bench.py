@@ -60,6 +60,15 @@ def make_mesh(w):
     return M.channel_with_obstacle(w["nx"], w["ny"])
 
 
+def header_constant(name):
+    """An integer #define of the library's C header."""
+    with open(os.path.join(ROOT, "include", "nsfem_gb300.h")) as f:
+        for line in f:
+            if line.startswith("#define " + name + " "):
+                return int(line.split()[2])
+    raise KeyError(name)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -121,17 +130,22 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def algorithmic_bytes(mode, n, nnz, its, outer):
+def algorithmic_bytes(mode, n, nnz, its, outer, pipelined=False):
     """Minimal DRAM bytes of one persistent CG launch (int32 indices).
 
     FP64 iteration: nnz*(8+4) + 4(n+1) + 11 vector passes of 8n (SpMV gathers p and writes q, dot fused; x and r
     read+write with p and q reads; p update reads r, p and writes p).  Prologue: one SpMV with x0 plus b, r, p, x.
+    The pipelined FP64 form moves 13 passes (its product gathers w; z, s, p, x, r and w read and written), and
+    every replacement (outer - 1 of them) four products.
     Mixed: inner FP32 iterations nnz*(4+4) + 4(n+1) + 11*4n; every refinement sweep one FP64 residual
     nnz*(8+4) + 4(n+1) + 28n and an x += d pass of 20n.
     """
     if mode == 0:
-        it_bytes = 12 * nnz + 4 * (n + 1) + 88 * n
-        return (12 * nnz + 4 * (n + 1) + 40 * n) + its * it_bytes
+        passes = 13 if pipelined else 11
+        it_bytes = 12 * nnz + 4 * (n + 1) + 8 * passes * n
+        prologue = 12 * nnz + 4 * (n + 1) + 40 * n
+        extra = max(outer - 1, 0) * 4 * (12 * nnz + 4 * (n + 1) + 24 * n) if pipelined else 0
+        return prologue + extra + its * it_bytes
     inner = 8 * nnz + 4 * (n + 1) + 44 * n
     sweep = 12 * nnz + 4 * (n + 1) + 28 * n
     return (outer + 1) * sweep + outer * 20 * n + its * inner
@@ -273,14 +287,16 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4):
+def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False):
     """Minimal DRAM bytes of one preconditioned solve: per iteration the product with the non-zeros of A and both
     triangular sweeps over the factor's nzl strictly lower entries (values + idx-byte column indices: 2 where the
     mixed iterations read 16-bit column copies), plus about 15 vector passes (product gathers and outputs, the x/r
-    update, the sweeps' right-hand sides, inverse diagonals and in-place results).  The mixed form moves FP32
-    values and vectors and adds an FP64 residual (int32 indices) per refresh."""
+    update, the sweeps' right-hand sides, inverse diagonals and in-place results), 11 when the inner kernel keeps
+    the correction (read and written every iteration) and the colour-1 rows' r and q (half the rows) in shared
+    memory.  The mixed form moves FP32 values and vectors and adds an FP64 residual (int32 indices) per refresh."""
     v = 4 if mixed else 8
-    it_bytes = (v + idx) * (nz + 2 * nzl) + 4 * (n + 1) + 15 * v * n
+    passes = 11 if resident else 15
+    it_bytes = (v + idx) * (nz + 2 * nzl) + 4 * (n + 1) + passes * v * n
     refresh = 12 * nz + 4 * (n + 1) + 28 * n
     return (outer + 1) * refresh + its * it_bytes
 
@@ -357,27 +373,38 @@ def roofline(sim, arm, args):
     that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
-    nzl, idx = {}, {}
+    nzl, idx, res = {}, {}, {}
     for slot in (0, 1, 2):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
-    names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel", 2: "pcg_mixed_inner_kernel_cta1024", 3: "pcg_fp64_kernel"}
+            res[slot] = sim.precond_inner_form(slot) == "resident"
+    resident = any(res.values())
+    names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel",
+             2: "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
+             3: "pcg_fp64_kernel"}
+    form = getattr(args, "cg_form", "auto")
+    pipe_max = header_constant("NSF_CG_PIPELINED_MAX_ROWS")
     bytes_by, ms_by, rowit_by = {}, {}, {}
     for sl, m_, n_, i_, o_, t_ in zip(prof["slot"], prof["mode"], prof["rows"], prof["iterations"], prof["outer"],
                                       prof["ms"]):
         m_, sl = int(m_), int(sl)
+        pipe = m_ == 0 and (form == "pipelined" or (form == "auto" and int(n_) < pipe_max))
         if m_ in (2, 3):
-            b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4)
+            b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4,
+                          res.get(sl, False) and m_ == 2)
         else:
-            b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_))
-        bytes_by[names[m_]] = bytes_by.get(names[m_], 0.0) + b
-        ms_by[names[m_]] = ms_by.get(names[m_], 0.0) + float(t_)
-        rowit_by[names[m_]] = rowit_by.get(names[m_], 0.0) + float(n_) * float(i_)
+            b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_), pipe)
+        name = "cg_fp64_pipe_kernel" if pipe else names[m_]
+        bytes_by[name] = bytes_by.get(name, 0.0) + b
+        ms_by[name] = ms_by.get(name, 0.0) + float(t_)
+        rowit_by[name] = rowit_by.get(name, 0.0) + float(n_) * float(i_)
     top = max(ms_by, key=ms_by.get)
     peak, peak_kind = peaks()
     achieved = bytes_by[top] / (ms_by[top] * 1e-3) / 1e9 if ms_by[top] > 0 else 0.0
-    launches = int(sum(1 for m_ in prof["mode"] if names[int(m_)] == top))
+    launches = int(sum(1 for m_, n_ in zip(prof["mode"], prof["rows"])
+                       if ("cg_fp64_pipe_kernel" if int(m_) == 0 and (form == "pipelined" or (
+                           form == "auto" and int(n_) < pipe_max)) else names[int(m_)]) == top))
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs", "kernel": top,
             "launches": launches, "kernel_ms_per_step": round(ms_by[top] / args.steps, 3),

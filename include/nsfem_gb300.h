@@ -146,6 +146,10 @@ int nsf_precond_kind(nsf_device* h, int slot);
  * and both factor parts have 16-bit column copies (every 32-row slice's columns within 65535 of each other; decided
  * by the slot's first mixed PCG solve), else 4. */
 int nsf_precond_index_bytes(nsf_device* h, int slot);
+/* The inner-iteration kernel the slot's last split mixed PCG solve ran: 0 four 256-thread CTAs per SM (one colour),
+ * 1 one 1024-thread CTA per SM, 2 the same with the row state only a CTA reads resident in its shared memory (two
+ * colours, where it fits); -1 before the slot's first such solve. */
+int nsf_precond_inner_form(nsf_device* h, int slot, int* form);
 int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
 int nsf_precond_cap(nsf_device* h, int slot, int maxIterations);

@@ -99,6 +99,7 @@ _SIGS = {
     "nsf_precond_get": (_i, [_v, _i, _arr(np.float64), _arr(np.float64)]),
     "nsf_precond_kind": (_i, [_v, _i]),
     "nsf_precond_index_bytes": (_i, [_v, _i]),
+    "nsf_precond_inner_form": (_i, [_v, _i, ctypes.POINTER(_i)]),
     "nsf_precond_clear": (_i, [_v, _i]),
     "nsf_precond_cap": (_i, [_v, _i, _i]),
     "nsf_tc_dense": (_i, [_v, _i, _i, _i, _arr(np.float32), _arr(np.float32), _v, _i, _arr(np.float32)]),
@@ -426,6 +427,13 @@ class GPUSimulationDevice:
         if k < 0:
             self._check(-k)
         return k
+
+    def precond_inner_form(self, slot) -> str:
+        """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident" or
+        "none" (no such solve yet)."""
+        k = _i()
+        self._check(library().nsf_precond_inner_form(self._h, _slot(slot), ctypes.byref(k)))
+        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident"}[k.value]
 
     def precond_clear(self, slot):
         self._check(library().nsf_precond_clear(self._h, _slot(slot)))

@@ -271,7 +271,7 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     }
     const bool wide = S.maxWidth > kSellChunk;
     if (mode == NSF_SOLVER_PCG_MIXED && !wide)
-        pcg_mixed_split_launch(ws, a, h->stream);
+        h->innerForm[slot] = pcg_mixed_split_launch(ws, a, h->stream);
     else if (mode == NSF_SOLVER_MIXED && wide)
         cg_mixed_split_launch(ws, a, h->stream);
     else if (mode == NSF_SOLVER_FP64 && use_pipelined_cg(h, S))
@@ -974,6 +974,14 @@ int nsf_precond_index_bytes(nsf_device* h, int slot) {
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     const Factor& F = h->factors[slot];
     return F.ready && F.colours >= 2 && F.col16 && F.Ap.hasCol16 ? 2 : 4;
+}
+
+int nsf_precond_inner_form(nsf_device* h, int slot, int* form) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    if (!form) throw bad_arg("null output pointer");
+    *form = h->innerForm[slot];
+    NSF_END(h)
 }
 
 int nsf_precond_clear(nsf_device* h, int slot) {

@@ -354,7 +354,7 @@ void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
                  (const void*)cg_mixed_inner_kernel, s);
 }
 
-void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
+int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;
     const void* inner1024 = a.f.colours < 2 ? nullptr
@@ -372,6 +372,8 @@ void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
         }
     }
     split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner1024, inner256, s, dsm);
+    if (!(inner1024 && ws.gridInner1024 > 0 && a.sellStart)) return 0;
+    return dsm > 0 ? 2 : 1;
 }
 
 // The FP64 solver's persistent grid for `device`, by the same rule as cg_configure, touching no device memory.

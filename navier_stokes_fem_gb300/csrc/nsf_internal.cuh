@@ -276,7 +276,8 @@ void cg_launch(CgWorkspace& ws, const CgArgs& a, int mode, bool wide, cudaStream
 void cg_pipe_launch(CgWorkspace& ws, const CgArgs& a, bool wide, cudaStream_t s);
 // The split mixed PCG (narrow matrices): refresh kernel, then inner-iteration and refresh kernels until the solve
 // is done; one small device-to-host read per refresh cycle.
-void pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
+// Returns the inner-iteration kernel it ran (nsf_precond_inner_form's values).
+int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
 // The split plain mixed CG (wide systems): the same launch pattern.
 void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s);
 void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
@@ -394,6 +395,7 @@ struct nsf_device {
     bool mixedOff[NSF_SLOT_COUNT] = {};   // systems whose mixed solve stalled once: solved in FP64 from then on
     nsf::Factor factors[NSF_SLOT_COUNT];  // preconditioners
     int pcgCap[NSF_SLOT_COUNT] = {};      // iteration cap of a preconditioned solve (0: rows)
+    int innerForm[NSF_SLOT_COUNT] = {-1, -1, -1, -1, -1, -1, -1};   // the last split mixed PCG's inner kernel
     bool pcgOff[NSF_SLOT_COUNT] = {};     // systems whose preconditioned solve fell back: plain CG from then on
     // per-solve records (profiling of the persistent CG kernels)
     bool profile = false;

@@ -18,9 +18,13 @@ def _csr(n, per_row):
 
 
 class FakeSim:
-    def __init__(self, idx):
+    def __init__(self, idx, form="cta1024"):
         self.mats = {0: _csr(1000, 7), 1: _csr(4000, 12), 2: _csr(4000, 12)}
         self.idx = idx
+        self.form = form
+
+    def precond_inner_form(self, slot):
+        return self.form
 
     def download_matrix(self, slot):
         return self.mats[slot]
@@ -35,24 +39,29 @@ class FakeSim:
         return self.idx
 
 
-@pytest.mark.parametrize("idx", [2, 4])
-def test_roofline_accounts_the_mixed_pcg_under_its_inner_kernel(idx):
-    sim = FakeSim(idx)
+@pytest.mark.parametrize("idx,form", [(2, "cta1024"), (4, "cta1024"), (2, "resident")])
+def test_roofline_accounts_the_mixed_pcg_under_its_inner_kernel(idx, form):
+    sim = FakeSim(idx, form)
     prof = {"slot": np.array([0, 0, 1, 2]), "mode": np.array([2, 2, 1, 1]),
             "rows": np.array([1000, 1000, 4000, 4000]), "iterations": np.array([300, 320, 30, 14]),
             "outer": np.array([6, 7, 4, 4]), "ms": np.array([5.0, 6.0, 1.0, 0.5], np.float32)}
     r = bench.roofline(sim, {"prof": prof}, types.SimpleNamespace(steps=2))
-    assert r["kernel"] == "pcg_mixed_inner_kernel_cta1024" and r["launches"] == 2
+    resident = form == "resident"
+    kernel = "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024"
+    assert r["kernel"] == kernel and r["launches"] == 2
     nz, nzl = 1000 * 6, 2000
-    want = bench.pcg_bytes(True, 1000, nz, nzl, 300, 6, idx) + bench.pcg_bytes(True, 1000, nz, nzl, 320, 7, idx)
+    want = bench.pcg_bytes(True, 1000, nz, nzl, 300, 6, idx, resident) + \
+        bench.pcg_bytes(True, 1000, nz, nzl, 320, 7, idx, resident)
     assert r["algorithmic_bytes_per_launch"] == round(want / 2)
-    per_it = (4 + idx) * (nz + 2 * nzl) + 4 * 1001 + 60 * 1000
-    assert bench.pcg_bytes(True, 1000, nz, nzl, 1, 0, idx) - bench.pcg_bytes(True, 1000, nz, nzl, 0, 0, idx) == per_it
+    # the resident form keeps 16 of the 60 vector bytes per row on the chip
+    per_it = (4 + idx) * (nz + 2 * nzl) + 4 * 1001 + (44 if resident else 60) * 1000
+    assert bench.pcg_bytes(True, 1000, nz, nzl, 1, 0, idx, resident) - \
+        bench.pcg_bytes(True, 1000, nz, nzl, 0, 0, idx, resident) == per_it
     assert r["achieved"] == pytest.approx(want / 11e-3 / 1e9, abs=0.05)   # GB/s, rounded to 0.1
     peak, _ = bench.peaks()
     assert r["frac"] == pytest.approx(r["achieved"] / peak, abs=1e-4)
-    rate = bench.DRAM_BYTES_PER_ROW_ITERATION["pcg_mixed_inner_kernel_cta1024"]
-    assert r["traffic"] == round(rate * 1000 * 620 / 2)
+    rate = bench.DRAM_BYTES_PER_ROW_ITERATION.get(kernel)
+    assert r["traffic"] == (round(rate * 1000 * 620 / 2) if rate else None)
     assert r["kernel_ms_per_step"] == pytest.approx(5.5, abs=1e-3)
     assert r["kernel_share_of_solver_time"] == pytest.approx(11.0 / 12.5, abs=1e-3)
 
@@ -64,3 +73,6 @@ def test_plain_cg_bytes_match_the_per_unit_figures():
     assert 630e6 < fp64 < 645e6
     mixed = bench.algorithmic_bytes(1, n, nnz, 1, 0) - bench.algorithmic_bytes(1, n, nnz, 0, 0)
     assert mixed == 8 * nnz + 4 * (n + 1) + 44 * n
+    pipe = bench.algorithmic_bytes(0, n, nnz, 1, 1, True) - bench.algorithmic_bytes(0, n, nnz, 0, 1, True)
+    assert pipe == 12 * nnz + 4 * (n + 1) + 104 * n        # the pipelined form: 13 vector passes
+    assert bench.header_constant("NSF_CG_PIPELINED_MAX_ROWS") > 0

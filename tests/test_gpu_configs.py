@@ -1,7 +1,8 @@
 """The workloads at their own sizes, each against the FP64 path on the same GPU:
 
 * the batched form: 64 cavities with n uniform in [16, 256] (seed 20261203), FP64 at tolerance 1e-8, one persistent
-  launch per step - every instance against the single-instance FP64 path after the same steps;
+  launch per step - every instance against the single-instance FP64 path after the same steps, within the bound
+  two solvers stopped at the same residual can differ by;
 * the channel 4 x 1 on 1024 x 256 cells with the obstacle removed (about 520 k triangles), nu = 1e-3, dt = 2e-3, its
   200 steps - the mixed-precision solvers (with the IC(0) pressure factor) against the FP64 solvers.
 
@@ -16,7 +17,12 @@ from navier_stokes_fem_gb300 import mesh as M
 from tests._meshes import rel
 
 pytestmark = pytest.mark.gpu
-BATCH_TOL = 1e-8          # the same (three-barrier) FP64 CG in a team of CTAs instead of the whole grid: rounding only
+# The batched kernel runs the same three-barrier FP64 CG as the single-instance path, but in a team of a few CTAs, so
+# its sums are formed in another order; a solve may then stop an iteration earlier or later, and two solutions that
+# both meet the 1e-8 relative residual differ by up to about cond(A) * 1e-8 - about 2.6e-4 for the pressure system
+# of a 256 x 256 cavity (cond ~ 0.4 n^2) - per step.  (On the small cavities of test_gpu_batched.py they agree to
+# 1e-9.)
+BATCH_TOL = 2e-3
 MIXED_TOL_UV = 1e-5
 MIXED_TOL_P = 1e-3
 

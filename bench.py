@@ -287,16 +287,18 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False):
+def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None):
     """Minimal DRAM bytes of one preconditioned solve: per iteration the product with the non-zeros of A and both
     triangular sweeps over the factor's nzl strictly lower entries (values + idx-byte column indices: 2 where the
     mixed iterations read 16-bit column copies), plus about 15 vector passes (product gathers and outputs, the x/r
     update, the sweeps' right-hand sides, inverse diagonals and in-place results), 11 when the inner kernel keeps
     the correction (read and written every iteration) and the colour-1 rows' r and q (half the rows) in shared
-    memory.  The mixed form moves FP32 values and vectors and adds an FP64 residual (int32 indices) per refresh."""
+    memory.  The mixed form moves FP32 values and vectors - the factor's values in FP16 where the factor keeps FP16
+    copies (fvb = 2 bytes per factor value) - and adds an FP64 residual (int32 indices) per refresh."""
     v = 4 if mixed else 8
+    fv = v if fvb is None or not mixed else fvb
     passes = 11 if resident else 15
-    it_bytes = (v + idx) * (nz + 2 * nzl) + 4 * (n + 1) + passes * v * n
+    it_bytes = (v + idx) * nz + (fv + idx) * 2 * nzl + 4 * (n + 1) + passes * v * n
     refresh = 12 * nz + 4 * (n + 1) + 28 * n
     return (outer + 1) * refresh + its * it_bytes
 
@@ -373,12 +375,13 @@ def roofline(sim, arm, args):
     that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
-    nzl, idx, res = {}, {}, {}
+    nzl, idx, res, fvb = {}, {}, {}, {}
     for slot in (0, 1, 2):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
             res[slot] = sim.precond_inner_form(slot) == "resident"
+            fvb[slot] = sim.precond_value_bytes(slot)
     resident = any(res.values())
     names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel",
              2: "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
@@ -392,7 +395,7 @@ def roofline(sim, arm, args):
         pipe = m_ == 0 and (form == "pipelined" or (form == "auto" and int(n_) < pipe_max))
         if m_ in (2, 3):
             b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4,
-                          res.get(sl, False) and m_ == 2)
+                          res.get(sl, False) and m_ == 2, fvb.get(sl))
         else:
             b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_), pipe)
         name = "cg_fp64_pipe_kernel" if pipe else names[m_]

@@ -146,6 +146,10 @@ int nsf_precond_kind(nsf_device* h, int slot);
  * and both factor parts have 16-bit column copies (every 32-row slice's columns within 65535 of each other; decided
  * by the slot's first mixed PCG solve), else 4. */
 int nsf_precond_index_bytes(nsf_device* h, int slot);
+/* Bytes per factor value that the mixed PCG's FP32 iterations read: 2 when every factor value fits FP16's normal
+ * range (the factor then keeps FP16 copies, and its FP32 copies hold the same rounded values, so that every FP32
+ * sweep applies the same M), else 4. */
+int nsf_precond_value_bytes(nsf_device* h, int slot);
 /* The inner-iteration kernel the slot's last split mixed PCG solve ran: 0 four 256-thread CTAs per SM (one colour),
  * 1 one 1024-thread CTA per SM, 2 the same with the row state only a CTA reads resident in its shared memory (two
  * colours, where it fits); -1 before the slot's first such solve. */

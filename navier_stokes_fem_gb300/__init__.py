@@ -100,6 +100,7 @@ _SIGS = {
     "nsf_precond_kind": (_i, [_v, _i]),
     "nsf_precond_index_bytes": (_i, [_v, _i]),
     "nsf_precond_inner_form": (_i, [_v, _i, ctypes.POINTER(_i)]),
+    "nsf_precond_value_bytes": (_i, [_v, _i]),
     "nsf_precond_clear": (_i, [_v, _i]),
     "nsf_precond_cap": (_i, [_v, _i, _i]),
     "nsf_tc_dense": (_i, [_v, _i, _i, _i, _arr(np.float32), _arr(np.float32), _v, _i, _arr(np.float32)]),
@@ -424,6 +425,13 @@ class GPUSimulationDevice:
     def precond_index_bytes(self, slot) -> int:
         """Bytes per column index the slot's mixed PCG iterations read (2: 16-bit column copies, else 4)."""
         k = library().nsf_precond_index_bytes(self._h, _slot(slot))
+        if k < 0:
+            self._check(-k)
+        return k
+
+    def precond_value_bytes(self, slot) -> int:
+        """Bytes per factor value the slot's mixed PCG iterations read (2: FP16 copies, else 4)."""
+        k = library().nsf_precond_value_bytes(self._h, _slot(slot))
         if k < 0:
             self._check(-k)
         return k

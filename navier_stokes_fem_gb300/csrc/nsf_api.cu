@@ -976,6 +976,13 @@ int nsf_precond_index_bytes(nsf_device* h, int slot) {
     return F.ready && F.colours >= 2 && F.col16 && F.Ap.hasCol16 ? 2 : 4;
 }
 
+int nsf_precond_value_bytes(nsf_device* h, int slot) {
+    if (!h || slot < 0 || slot >= NSF_SLOT_COUNT) return -NSF_ERR_BAD_ARG;
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    const Factor& F = h->factors[slot];
+    return F.ready && F.has16 ? 2 : 4;
+}
+
 int nsf_precond_inner_form(nsf_device* h, int slot, int* form) {
     NSF_BEGIN(h)
     check_slot(slot);

@@ -100,22 +100,23 @@ __global__ void __launch_bounds__(kCgThreads, 4) pcg_mixed_inner_kernel(CgArgs a
 // pressure system, 9-13 % per step on systems of 0.26-1 M rows, where the barriers weigh more).  Two or more
 // colours and a SELL copy only: there is no staging area for the CSR product.
 constexpr int kInnerCtaThreads = 1024;
-template <bool C16>
+// (H16: the factor's FP16 value copies, with C16.)
+template <bool C16, bool H16 = false>
 __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_cta1024(CgArgs a) {
     __shared__ double smem[kSmemSlots];
     if (!a.sellStart) return;   // (the host never launches it without one)
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed_inner<C16, true>(t, a, nullptr, smem, nullptr);
+    team_pcg_mixed_inner<C16, true, false, H16>(t, a, nullptr, smem, nullptr);
 }
 
 // The same 1024-thread form with the row state only its CTA reads (the FP32 correction, and r and q of its colour-1
 // rows) in dynamic shared memory for the whole launch: two colours only, and only where that state fits.
-template <bool C16>
+template <bool C16, bool H16 = false>
 __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_resident(CgArgs a) {
     __shared__ double smem[kSmemSlots];
     if (!a.sellStart || a.f.colours != 2) return;   // (the host never launches it otherwise)
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed_inner<C16, true, true>(t, a, nullptr, smem, nullptr);
+    team_pcg_mixed_inner<C16, true, true, H16>(t, a, nullptr, smem, nullptr);
 }
 
 // Shared-memory bytes pcg_mixed_inner_kernel_resident needs on `grid` CTAs for a factor's colour blocks: per CTA
@@ -259,7 +260,8 @@ void cg_configure(CgWorkspace& ws, int device) {
     ws.gridInner = sms * std::max(perSm, inner_occupancy());
     // the 1024-thread inner kernels: one CTA per SM (0 if one of them cannot be resident)
     int o1024 = 1;
-    for (const void* fn : {(const void*)pcg_mixed_inner_kernel_cta1024<true>,
+    for (const void* fn : {(const void*)pcg_mixed_inner_kernel_cta1024<true, true>,
+                           (const void*)pcg_mixed_inner_kernel_cta1024<true>,
                            (const void*)pcg_mixed_inner_kernel_cta1024<false>, (const void*)cg_mixed_inner_kernel_cta1024}) {
         int o = 0;
         NSF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, kInnerCtaThreads, 0));
@@ -272,7 +274,8 @@ void cg_configure(CgWorkspace& ws, int device) {
         int optin = 0;
         NSF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
         size_t best = 0;
-        for (const void* fn : {(const void*)pcg_mixed_inner_kernel_resident<true>,
+        for (const void* fn : {(const void*)pcg_mixed_inner_kernel_resident<true, true>,
+                               (const void*)pcg_mixed_inner_kernel_resident<true>,
                                (const void*)pcg_mixed_inner_kernel_resident<false>}) {
             cudaFuncAttributes fa{};
             NSF_CUDA(cudaFuncGetAttributes(&fa, fn));
@@ -357,7 +360,9 @@ void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
 int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;
+    const bool h16 = c16 && a.f.loVal16 && a.f.upVal16;   // FP16 factor values (16-bit columns only)
     const void* inner1024 = a.f.colours < 2 ? nullptr
+                            : h16           ? (const void*)pcg_mixed_inner_kernel_cta1024<true, true>
                             : c16           ? (const void*)pcg_mixed_inner_kernel_cta1024<true>
                                             : (const void*)pcg_mixed_inner_kernel_cta1024<false>;
     const void* inner256 = c16 ? (const void*)pcg_mixed_inner_kernel<true> : (const void*)pcg_mixed_inner_kernel<false>;
@@ -366,8 +371,9 @@ int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     if (a.f.colours == 2 && a.sellStart && ws.gridInner1024 > 0 && ws.residentMaxBytes > 0) {
         const size_t need = resident_bytes(a.f, ws.gridInner1024);
         if (need <= ws.residentMaxBytes) {
-            inner1024 = c16 ? (const void*)pcg_mixed_inner_kernel_resident<true>
-                            : (const void*)pcg_mixed_inner_kernel_resident<false>;
+            inner1024 = h16   ? (const void*)pcg_mixed_inner_kernel_resident<true, true>
+                        : c16 ? (const void*)pcg_mixed_inner_kernel_resident<true>
+                              : (const void*)pcg_mixed_inner_kernel_resident<false>;
             dsm = need;
         }
     }

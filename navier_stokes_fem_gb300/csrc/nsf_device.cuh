@@ -52,6 +52,9 @@ __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ unsigned short ld_stream(const unsigned short* p) { return __ldcs(p); }
+__device__ __forceinline__ __half ld_stream(const __half* p) {
+    return __ushort_as_half(__ldcs(reinterpret_cast<const unsigned short*>(p)));
+}
 
 // A team: `size` consecutive CTAs of a persistent launch that cooperate on one system (the whole grid for a
 // single solve; a share of the grid per instance in the batched step).  Its barrier is a monotone arrival

@@ -1,6 +1,7 @@
 // Internal declarations shared by the GB300 solver's translation units.  Not part of the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
@@ -122,6 +123,8 @@ struct FactorView {
     const int* upCol = nullptr;
     const double* upVal = nullptr;
     const float* upVal32 = nullptr;
+    const __half* loVal16 = nullptr;          // FP16 copies of both parts' values (null: a value is outside FP16's
+    const __half* upVal16 = nullptr;          // normal range); the FP32 copies then hold the same rounded values
     const unsigned short* loCol16 = nullptr;  // 16-bit column copies of both parts (null: not built, or a slice's
     const int* loColBase = nullptr;           // columns span 65535 or more)
     const unsigned short* upCol16 = nullptr;
@@ -159,6 +162,9 @@ struct Factor {
     int loMaxW = 0, upMaxW = 0;
     DevBuf<double> loVal, upVal, dinv;
     DevBuf<float> loVal32, upVal32, dinv32;
+    DevBuf<__half> loVal16, upVal16;           // FP16 copies of the values (see FactorView)
+    DevBuf<int> range16;                       // set by factor_fill when a value does not fit FP16's normal range
+    bool has16 = false;
     int kind = 0;                              // NSF_PRECOND_NONE / IC0 / LEARNED
     double shift = 0.0;                        // diagonal shift the incomplete factorisation needed
     bool ready = false;

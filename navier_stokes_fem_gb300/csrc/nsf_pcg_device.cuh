@@ -502,9 +502,20 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
 // that the iterations move stay on the chip.
 extern __shared__ __align__(16) float nsf_row_state[];   // the resident form's dynamic shared memory
 
-template <bool C16 = false, bool Resident = false>
+// (H16: the factor's FP16 value copies, with C16.)
+template <bool C16 = false, bool Resident = false, bool H16 = false>
 static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring,
                                              PcgLoop& L, int& where) {
+    using TF = std::conditional_t<H16, __half, float>;   // the factor values the sweeps read
+    const TF* loV;
+    const TF* upV;
+    if constexpr (H16) {
+        loV = a.f.loVal16;
+        upV = a.f.upVal16;
+    } else {
+        loV = a.f.loVal32;
+        upV = a.f.upVal32;
+    }
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x, C = F.colours;
     int rb, re;
@@ -624,8 +635,8 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
             const TC* loCol;
             if constexpr (C16) loCol = F.loCol16;
             else loCol = F.loCol;
-            sell_rows<float, float, false, 1, 4, TC>(
-                F.loStart, loCol, F.loVal32, r0, r1,
+            sell_rows<TF, float, false, 1, 4, TC>(
+                F.loStart, loCol, loV, r0, r1,
                 [&](int j) { return fmaf(-alphaf, a.q32[j], rOld[j]) * dinv[j]; },
                 [&](int i) {
                     float rn;
@@ -666,7 +677,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         if (dr.code == 2) break;   // time for a true residual
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
         double rzs = 0;
-        if (!precond_sweeps<float, float, true, C16>(t, a, rNew, w, F.loVal32, F.upVal32, dinv, rzn, smem, where,
+        if (!precond_sweeps<TF, float, true, C16>(t, a, rNew, w, loV, upV, dinv, rzn, smem, where,
                                                      rzs, ring, 2))
             return false;
         if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
@@ -791,7 +802,7 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
 
 // (FusedOnly: the caller guarantees two or more colours; the one-colour loop and its CSR staging are left out.
 // Resident: the caller guarantees exactly two colours and dynamic shared memory for the row state.)
-template <bool C16 = false, bool FusedOnly = false, bool Resident = false>
+template <bool C16 = false, bool FusedOnly = false, bool Resident = false, bool H16 = false>
 static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, double* smem, SellRing* ring) {
     int where = 400;
     // the fields the inner iterations read or write (the rest of the state stays in memory)
@@ -806,8 +817,8 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.flip = G.flip;
     L.rflip = G.rflip;
     bool ok;
-    if constexpr (Resident) ok = pcg_mixed_inner_fused<C16, true>(t, a, stage, smem, ring, L, where);
-    else if constexpr (FusedOnly) ok = pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where);
+    if constexpr (Resident) ok = pcg_mixed_inner_fused<C16, true, H16>(t, a, stage, smem, ring, L, where);
+    else if constexpr (FusedOnly) ok = pcg_mixed_inner_fused<C16, false, H16>(t, a, stage, smem, ring, L, where);
     else ok = a.f.colours >= 2 ? pcg_mixed_inner_fused<C16>(t, a, stage, smem, ring, L, where)
                                : pcg_mixed_inner<false, true>(t, a, stage, smem, ring, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);

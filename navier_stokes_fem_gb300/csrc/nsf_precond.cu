@@ -244,6 +244,9 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
     F.loVal32.alloc(std::max<size_t>(lo.col.size(), 1));
     F.upVal.alloc(std::max<size_t>(up.col.size(), 1));
     F.upVal32.alloc(std::max<size_t>(up.col.size(), 1));
+    F.loVal16.alloc(std::max<size_t>(lo.col.size(), 1));
+    F.upVal16.alloc(std::max<size_t>(up.col.size(), 1));
+    F.range16.alloc(1);
     F.dinv.alloc((size_t)np);
     F.dinv32.alloc((size_t)np);
     // the permuted matrix, its values gathered from A, and its SELL copies (FP64 and FP32)
@@ -304,25 +307,45 @@ __global__ void ic0_colour_kernel(int r0, int r1, const int* __restrict__ perm, 
     }
 }
 
+// A value's FP16 copy, and whether it is outside FP16's normal range (a non-zero magnitude below 2^-14, where
+// subnormals lose precision, or above 65504).
+__device__ __forceinline__ __half to_half_checked(double v, int* range16) {
+    const double m = fabs(v);
+    if (m != 0.0 && (m < 6.103515625e-05 || m > 65504.0)) atomicExch(range16, 1);
+    return __double2half(v);
+}
+
+// FP32 copy of a value: the FP16 value widened when the factor keeps FP16 copies (every consumer of the FP32 values,
+// the refresh kernel's sweeps included, then applies the same M as the FP16 inner iterations), else the value
+// rounded once.
 __global__ void factor_fill_kernel(int64_t nLo, int64_t nUp, int n, const int* __restrict__ perm,
                                    const int* __restrict__ loFrom, const int* __restrict__ upFrom,
                                    const double* __restrict__ lVal,
                                    const double* __restrict__ diag, double* loVal, float* loVal32, double* upVal,
-                                   float* upVal32, double* dinv, float* dinv32) {
+                                   float* upVal32, double* dinv, float* dinv32, __half* loVal16, __half* upVal16,
+                                   int* range16, int pass) {
     const int64_t total = nLo + nUp + n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < nLo) {
             const int f = loFrom[i];
             const double v = f >= 0 ? lVal[f] : 0.0;
-            loVal[i] = v;
-            loVal32[i] = (float)v;
+            if (pass == 0) {
+                loVal[i] = v;
+                loVal16[i] = to_half_checked(v, range16);
+            } else {
+                loVal32[i] = pass == 2 ? __half2float(loVal16[i]) : (float)v;
+            }
         } else if (i < nLo + nUp) {
             const int64_t k = i - nLo;
             const int f = upFrom[k];
             const double v = f >= 0 ? lVal[f] : 0.0;
-            upVal[k] = v;
-            upVal32[k] = (float)v;
-        } else {
+            if (pass == 0) {
+                upVal[k] = v;
+                upVal16[k] = to_half_checked(v, range16);
+            } else {
+                upVal32[k] = pass == 2 ? __half2float(upVal16[k]) : (float)v;
+            }
+        } else if (pass == 0) {
             const int64_t r = i - nLo - nUp;
             const int o = perm[r];
             const double d = o >= 0 ? 1.0 / diag[o] : 1.0;
@@ -333,13 +356,25 @@ __global__ void factor_fill_kernel(int64_t nLo, int64_t nUp, int n, const int* _
 }
 
 // Copies the canonical factor values into the sweep layouts (FP64 and FP32) and 1 / L_ii.
+// With FP16 copies when every value fits FP16's normal range (pass 0 writes FP64, FP16 and 1 / L_ii and checks
+// the range; pass 1 or 2 then writes the FP32 copies from the FP64 or the FP16 values).
 void factor_fill(Factor& F, cudaStream_t s) {
     const int64_t nLo = (int64_t)F.loCol.n, nUp = (int64_t)F.upCol.n;
-    factor_fill_kernel<<<grid_for(nLo + nUp + F.nPerm, 256), 256, 0, s>>>(
-        nLo, nUp, F.nPerm, F.perm.get(), F.loFrom.get(), F.upFrom.get(), F.lVal.get(), F.diag.get(), F.loVal.get(), F.loVal32.get(),
-        F.upVal.get(), F.upVal32.get(), F.dinv.get(), F.dinv32.get());
-    NSF_CUDA(cudaGetLastError());
-    count_launch();
+    F.range16.zero(s);
+    auto launch = [&](int pass) {
+        factor_fill_kernel<<<grid_for(nLo + nUp + F.nPerm, 256), 256, 0, s>>>(
+            nLo, nUp, F.nPerm, F.perm.get(), F.loFrom.get(), F.upFrom.get(), F.lVal.get(), F.diag.get(),
+            F.loVal.get(), F.loVal32.get(), F.upVal.get(), F.upVal32.get(), F.dinv.get(), F.dinv32.get(),
+            F.loVal16.get(), F.upVal16.get(), F.range16.get(), pass);
+        NSF_CUDA(cudaGetLastError());
+        count_launch();
+    };
+    launch(0);
+    int outOfRange = 0;
+    NSF_CUDA(cudaMemcpyAsync(&outOfRange, F.range16.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSF_CUDA(cudaStreamSynchronize(s));
+    F.has16 = outOfRange == 0;
+    launch(F.has16 ? 2 : 1);
     F.ready = true;
 }
 
@@ -388,6 +423,8 @@ FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     v.upCol = F.upCol.get();
     v.upVal = F.upVal.get();
     v.upVal32 = F.upVal32.get();
+    v.loVal16 = F.has16 ? F.loVal16.get() : nullptr;
+    v.upVal16 = F.has16 ? F.upVal16.get() : nullptr;
     if (F.col16) {
         v.loCol16 = F.loCol16.get();
         v.loColBase = F.loColBase.get();

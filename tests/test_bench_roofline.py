@@ -18,13 +18,17 @@ def _csr(n, per_row):
 
 
 class FakeSim:
-    def __init__(self, idx, form="cta1024"):
+    def __init__(self, idx, form="cta1024", fvb=4):
         self.mats = {0: _csr(1000, 7), 1: _csr(4000, 12), 2: _csr(4000, 12)}
         self.idx = idx
         self.form = form
+        self.fvb = fvb
 
     def precond_inner_form(self, slot):
         return self.form
+
+    def precond_value_bytes(self, slot):
+        return self.fvb
 
     def download_matrix(self, slot):
         return self.mats[slot]
@@ -39,9 +43,9 @@ class FakeSim:
         return self.idx
 
 
-@pytest.mark.parametrize("idx,form", [(2, "cta1024"), (4, "cta1024"), (2, "resident")])
-def test_roofline_accounts_the_mixed_pcg_under_its_inner_kernel(idx, form):
-    sim = FakeSim(idx, form)
+@pytest.mark.parametrize("idx,form,fvb", [(2, "cta1024", 4), (4, "cta1024", 4), (2, "resident", 4), (2, "resident", 2)])
+def test_roofline_accounts_the_mixed_pcg_under_its_inner_kernel(idx, form, fvb):
+    sim = FakeSim(idx, form, fvb)
     prof = {"slot": np.array([0, 0, 1, 2]), "mode": np.array([2, 2, 1, 1]),
             "rows": np.array([1000, 1000, 4000, 4000]), "iterations": np.array([300, 320, 30, 14]),
             "outer": np.array([6, 7, 4, 4]), "ms": np.array([5.0, 6.0, 1.0, 0.5], np.float32)}
@@ -50,13 +54,13 @@ def test_roofline_accounts_the_mixed_pcg_under_its_inner_kernel(idx, form):
     kernel = "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024"
     assert r["kernel"] == kernel and r["launches"] == 2
     nz, nzl = 1000 * 6, 2000
-    want = bench.pcg_bytes(True, 1000, nz, nzl, 300, 6, idx, resident) + \
-        bench.pcg_bytes(True, 1000, nz, nzl, 320, 7, idx, resident)
+    want = bench.pcg_bytes(True, 1000, nz, nzl, 300, 6, idx, resident, fvb) + \
+        bench.pcg_bytes(True, 1000, nz, nzl, 320, 7, idx, resident, fvb)
     assert r["algorithmic_bytes_per_launch"] == round(want / 2)
-    # the resident form keeps 16 of the 60 vector bytes per row on the chip
-    per_it = (4 + idx) * (nz + 2 * nzl) + 4 * 1001 + (44 if resident else 60) * 1000
-    assert bench.pcg_bytes(True, 1000, nz, nzl, 1, 0, idx, resident) - \
-        bench.pcg_bytes(True, 1000, nz, nzl, 0, 0, idx, resident) == per_it
+    # the resident form keeps 16 of the 60 vector bytes per row on the chip; FP16 factor values save 2 per entry
+    per_it = (4 + idx) * nz + (fvb + idx) * 2 * nzl + 4 * 1001 + (44 if resident else 60) * 1000
+    assert bench.pcg_bytes(True, 1000, nz, nzl, 1, 0, idx, resident, fvb) - \
+        bench.pcg_bytes(True, 1000, nz, nzl, 0, 0, idx, resident, fvb) == per_it
     assert r["achieved"] == pytest.approx(want / 11e-3 / 1e9, abs=0.05)   # GB/s, rounded to 0.1
     peak, _ = bench.peaks()
     assert r["frac"] == pytest.approx(r["achieved"] / peak, abs=1e-4)

@@ -231,3 +231,25 @@ def test_mixed_pcg_when_slice_columns_span_beyond_16_bits():
     x, it, _ = d.conjugate_gradient(name, b, np.zeros(n), eps=TOL, solver="pcg_fp64")
     assert rel(xm, x) < 1e-6 and itm <= 2 * it + 10
     d.close()
+
+
+def test_fp16_factor_copies_only_within_range():
+    """The mixed PCG reads FP16 factor values where every value fits FP16's normal range (the cavity's pressure
+    factor); a system scaled by 1e-12 puts the factor's values (about its square root) below it, so the factor keeps
+    FP32 values only, and
+    the mixed PCG still reaches the FP64 residual either way."""
+    m = M.cavity(24)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    A = o.scipy_matrix("pressure_stiffness").tocsr()
+    o.close()
+    b = np.random.default_rng(12).standard_normal(A.shape[0])
+    for scale, want in ((1.0, 2), (1e-12, 4)):
+        d = nsf.GPUSimulationDevice(0)
+        As = (A * scale).tocsr()
+        d.upload_matrix("pressure_stiffness", As.indptr.astype(np.int32), As.indices, As.data, As.shape)
+        d.precond_ic0("pressure_stiffness")
+        assert d.precond_value_bytes("pressure_stiffness") == want
+        x, it, _ = d.conjugate_gradient("pressure_stiffness", b * scale, np.zeros_like(b), eps=TOL,
+                                        solver="pcg_mixed")
+        assert np.linalg.norm(b * scale - As @ x) <= 1.5 * TOL * np.linalg.norm(b * scale)
+        d.close()

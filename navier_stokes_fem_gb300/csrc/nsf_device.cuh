@@ -52,12 +52,6 @@ __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ unsigned short ld_stream(const unsigned short* p) { return __ldcs(p); }
-// Asks L2 to fetch `bytes` (a multiple of 16) from the 16-byte aligned global address p; nothing waits for it.
-__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
-                 : "memory");
-}
-
 // A 16-bit index loaded straight into a 32-bit register (zero-extended by the load itself).  On GB300 a separate
 // widening conversion of a 16-bit register issues on the FP64 pipe, which retires about 2 lanes per cycle per SM:
 // between a matrix entry's load and its gather that put a slow instruction on the critical path of every SELL
@@ -331,9 +325,6 @@ __device__ __forceinline__ void warp_spmv(const int* __restrict__ rowptr, const 
 // ---------------------------------------------------------------------------------------------------
 constexpr int kSlice = 32;
 constexpr int kUnroll = kSellChunk;
-// Steps ahead at which the 16-bit-column products and sweeps of the FP32 PCG iterations prefetch their CTA's matrix
-// block into L2 (sell_rows PF).
-constexpr int kPrefetchSteps = 2;
 
 // pre() value of the difference-form products that also carries the row's FP32 row sum (loaded with the row's own
 // vector entry when the slice starts, not after its sum); row_self() is the entry Diff subtracts.
@@ -391,17 +382,12 @@ __device__ __forceinline__ void sell_chunk(const TC* __restrict__ cp, const TV* 
 // pre(row) is evaluated when a slice starts (its loads overlap the slice's), and its value goes to epi(row, sum,
 // pre); with Diff it must be the row's own vector entry.  Rows [rb, re): rb a multiple of 32 unless rb == re.
 // With 16-bit columns (TC = unsigned short) colBase holds each slice's column base.
-// PF > 0 (one stream per warp): the CTA's warps take consecutive slices at each step, so the matrix block of the
-// CTA's step k + PF is one contiguous range of the column and value arrays; one thread of the CTA asks L2 to fetch
-// it (cp.async.bulk.prefetch, no registers, nothing waits on it), so that the warps' own loads of those entries
-// hit L2 instead of DRAM when they get there.
-template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename TC = int, int PF = 0,
-          typename Gather, typename Pre, typename Epi>
+template <typename TV, typename TA, bool Diff, int NS = 1, int U = kUnroll, typename TC = int, typename Gather,
+          typename Pre, typename Epi>
 __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, const TC* __restrict__ col,
                                           const TV* __restrict__ val, int rb, int re, Gather gather, Pre pre,
                                           Epi epi, const int* __restrict__ colBase = nullptr) {
     constexpr bool C16 = sizeof(TC) == 2;
-    static_assert(PF == 0 || NS == 1, "the block prefetch assumes one slice stream per warp");
     using PreT = decltype(pre(0));
     if (rb >= re) return;   // (an empty range may start inside the last, partial slice)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -428,30 +414,12 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
         cb[q] = C16 ? __shfl_sync(0xffffffffu, mcb[q], 0) : 0;
         sell_chunk<U, TV, TC>(col + base[q] + lane, val + base[q] + lane, W[q], 0, c[q], v[q], cb[q]);
     }
-    // (PF) the CTA's matrix block of step k: slices [rb / 32 + k nw, + nw), clipped to the range
-    auto prefetch_step = [&](int k) {
-        const int sA = rb / kSlice + k * nw;
-        if (sA >= s1) return;
-        const int sB = min(s1, sA + nw);
-        const int a0 = sliceStart[sA], a1 = sliceStart[sB];
-        if (a1 > a0) {
-            l2_prefetch(col + a0, (unsigned)((a1 - a0) * sizeof(TC)));
-            l2_prefetch(val + a0, (unsigned)((a1 - a0) * sizeof(TV)));
-        }
-    };
-    if constexpr (PF > 0) {
-        if (threadIdx.x == 0)
-            for (int k = 1; k <= PF; ++k) prefetch_step(k);
-    }
     for (int k = 0; k < per; ++k) {
         int row[NS], Wc[NS], bc[NS], cbc[NS];
         bool live[NS];
         PreT pv[NS];
         TA g[NS][U];
         RegT<TV> vk[NS][U];
-        if constexpr (PF > 0) {
-            if (threadIdx.x == 0) prefetch_step(k + PF + 1);
-        }
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
             const int i = q * per + k;
@@ -842,8 +810,8 @@ __device__ __forceinline__ void product32(SellRing* ring, const CgArgs& a, int r
     auto pre = [&](int row) { return DiffPre<float>{gather(row), a.rowsum32[row]}; };
     auto fin = [&](int row, float acc, const DiffPre<float>& q) { epi(row, fmaf(q.rs, q.self, acc), q.self); };
     if constexpr (C16 && !Wide) {
-        sell_rows<float, float, true, 1, U, unsigned short, kPrefetchSteps>(a.sellStart, a.sellCol16, a.sellVal32, rb,
-                                                                            re, gather, pre, fin, a.sellColBase);
+        sell_rows<float, float, true, 1, U, unsigned short>(a.sellStart, a.sellCol16, a.sellVal32, rb, re, gather,
+                                                            pre, fin, a.sellColBase);
         return;
     }
     if constexpr (!Wide) {

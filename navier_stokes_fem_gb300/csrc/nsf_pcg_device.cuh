@@ -80,8 +80,7 @@ __device__ __forceinline__ void sweep_rows(SellRing* ring, int maxW, const int* 
                                            int r0, int r1, Gather gather, Pre pre, Epi epi,
                                            const unsigned short* col16 = nullptr, const int* colBase = nullptr) {
     if constexpr (C16) {
-        sell_rows<TV, TA, false, 1, 4, unsigned short, kPrefetchSteps>(start, col16, val, r0, r1, gather, pre, epi,
-                                                                       colBase);
+        sell_rows<TV, TA, false, 1, 4, unsigned short>(start, col16, val, r0, r1, gather, pre, epi, colBase);
         return;
     }
     if constexpr (sizeof(TV) == 4) {
@@ -636,7 +635,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
             const TC* loCol;
             if constexpr (C16) loCol = F.loCol16;
             else loCol = F.loCol;
-            sell_rows<TF, float, false, 1, 4, TC, C16 ? kPrefetchSteps : 0>(
+            sell_rows<TF, float, false, 1, 4, TC>(
                 F.loStart, loCol, loV, r0, r1,
                 [&](int j) { return fmaf(-alphaf, a.q32[j], rOld[j]) * dinv[j]; },
                 [&](int i) {

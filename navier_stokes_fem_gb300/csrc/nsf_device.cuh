@@ -52,15 +52,6 @@ __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ unsigned short ld_stream(const unsigned short* p) { return __ldcs(p); }
-// A 16-bit index loaded straight into a 32-bit register (zero-extended by the load itself).  On GB300 a separate
-// widening conversion of a 16-bit register issues on the FP64 pipe, which retires about 2 lanes per cycle per SM:
-// between a matrix entry's load and its gather that put a slow instruction on the critical path of every SELL
-// product over 16-bit column copies (the pipe was a third busy in the FP32 PCG iterations with conversions only).
-__device__ __forceinline__ int ld_stream_u16(const unsigned short* p) {
-    unsigned v;
-    asm("ld.global.cs.u16 %0, [%1];" : "=r"(v) : "l"(p));
-    return (int)v;
-}
 __device__ __forceinline__ __half ld_stream(const __half* p) {
     return __ushort_as_half(__ldcs(reinterpret_cast<const unsigned short*>(p)));
 }
@@ -338,39 +329,23 @@ template <typename TA> __device__ __forceinline__ TA row_self(const DiffPre<TA>&
 // Column indices of a SELL-32 matrix are 32-bit (TC = int) or, when every slice's columns span fewer than 65535,
 // 16-bit offsets from a per-slice base (TC = unsigned short; kCol16Pad marks a padding entry of column -1).
 
-// The register type of a matrix value: FP16 values are widened to float when loaded.
-template <typename TV> struct RegOf { using T = TV; };
-template <> struct RegOf<__half> { using T = float; };
-template <typename TV> using RegT = typename RegOf<TV>::T;
-
-// A value loaded for the products.  An FP16 value - only ever zero or a normal FP16 number (the factor keeps FP16
-// copies only then) - is widened by integer operations on its bits (sign, exponent rebiased by 127 - 15 = 112,
-// mantissa shifted by 13): a conversion instruction would issue on GB300's narrow FP64 pipe.
-template <typename TV> __device__ __forceinline__ RegT<TV> ld_value(const TV* p) { return ld_stream(p); }
-template <> __device__ __forceinline__ float ld_value<__half>(const __half* p) {
-    const unsigned h = (unsigned)ld_stream_u16(reinterpret_cast<const unsigned short*>(p));
-    const unsigned mag = h & 0x7fffu;
-    return __uint_as_float(((h & 0x8000u) << 16) | (mag ? (mag << 13) + 0x38000000u : 0u));
-}
-
 // Loads entries [k0, k0 + U) of a lane's row in a slice (column -1 past the slice width W); cb is the slice's
 // column base of a 16-bit column array.
 template <int U, typename TV, typename TC = int>
 __device__ __forceinline__ void sell_chunk(const TC* __restrict__ cp, const TV* __restrict__ vp, int W, int k0,
-                                           int (&c)[U], RegT<TV> (&v)[U], int cb = 0) {
-    using TR = RegT<TV>;
+                                           int (&c)[U], TV (&v)[U], int cb = 0) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const bool in = k0 + u < W;
         if constexpr (sizeof(TC) == 2) {
             // a padding entry's value is zeroed too: the 16-bit copy of a matrix stores its diagonal as padding
-            const int d = in ? ld_stream_u16(cp + (k0 + u) * kSlice) : kCol16Pad;
-            const TR x = in ? ld_value(vp + (k0 + u) * kSlice) : TR(0);
+            const int d = in ? (int)ld_stream(cp + (k0 + u) * kSlice) : kCol16Pad;
+            const TV x = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
             c[u] = d == kCol16Pad ? -1 : cb + d;
-            v[u] = d == kCol16Pad ? TR(0) : x;
+            v[u] = d == kCol16Pad ? TV(0) : x;
         } else {
             c[u] = in ? ld_stream(cp + (k0 + u) * kSlice) : -1;
-            v[u] = in ? ld_value(vp + (k0 + u) * kSlice) : TR(0);
+            v[u] = in ? ld_stream(vp + (k0 + u) * kSlice) : TV(0);
         }
     }
 }
@@ -398,7 +373,7 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
     const int per = (count + NS - 1) / NS;           // per stream: stream q takes i in [q per, (q + 1) per)
     int mb[NS], me[NS], base[NS], W[NS], c[NS][U];
     int mcb[NS], cb[NS];   // 16-bit columns: the slices' column bases (lane j: slice i0 + j) and the current one's
-    RegT<TV> v[NS][U];
+    TV v[NS][U];
     auto meta_load = [&](int q, int i0) {   // lane j: start / end of stream q's slice i0 + j
         const int idx = sFirst + (q * per + i0 + lane) * nw;
         const bool in = idx < s1 && i0 + lane < per;
@@ -419,7 +394,7 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
         bool live[NS];
         PreT pv[NS];
         TA g[NS][U];
-        RegT<TV> vk[NS][U];
+        TV vk[NS][U];
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
             const int i = q * per + k;
@@ -466,7 +441,7 @@ __device__ __forceinline__ void sell_rows(const int* __restrict__ sliceStart, co
             // rows longer than U entries (P2 matrices): the rest of the slice, chunk by chunk
             for (int k0 = U; k0 < Wc[q]; k0 += U) {
                 int c2[U];
-                RegT<TV> v2[U];
+                TV v2[U];
                 TA g2[U];
                 sell_chunk<U, TV, TC>(col + bc[q] + lane, val + bc[q] + lane, Wc[q], k0, c2, v2, cbc[q]);
 #pragma unroll

@@ -363,9 +363,12 @@ def nonzeros(sim, slot):
 
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
-# 4,198,401 rows, whose vectors exceed L2): the mixed PCG's inner kernel (one 1024-thread CTA per SM, 16-bit column
-# copies) 17.49 GB over 40 iterations, cg_fp64_kernel 30.67 GB over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_cta1024": 104.1, "cg_fp64_kernel": 121.7}
+# 4,198,401 rows, whose vectors exceed L2): the mixed PCG's resident inner kernel (row state in shared memory,
+# 16-bit column copies, FP16 factor values) 11.01 GB over 40 iterations; the 1024-thread inner kernel without the
+# resident state (16-bit column copies, FP32 factor values) 17.49 GB over 40 iterations; cg_fp64_kernel 30.67 GB
+# over 60 iterations (its prologue included).
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_resident": 65.5, "pcg_mixed_inner_kernel_cta1024": 104.1,
+                                "cg_fp64_kernel": 121.7}
 
 
 def roofline(sim, arm, args):

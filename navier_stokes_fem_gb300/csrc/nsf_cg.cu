@@ -160,6 +160,7 @@ static __device__ void team_cg_mixed_inner(Team& t, const CgArgs& a, double* sta
     L.rrPrev = G.rrPrev;
     L.rrRef = G.rrRef;
     L.target = G.target;
+    L.scale = G.scale;
     L.cycleTol2 = G.cycleTol2;
     L.it = G.it;
     L.itRef = G.itRef;

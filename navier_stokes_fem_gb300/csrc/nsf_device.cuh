@@ -1180,8 +1180,23 @@ static __device__ int team_cg_fp64_pipelined(Team& t, const CgArgs& a, double* s
 // separate launches (the inner one at 4 CTAs per SM).
 // partial regions: 0 = p.q, 1 = r32.r32, 2 = r64.r64, 3 = b.b, 4 = r32.r32 after a refresh
 // ---------------------------------------------------------------------------------------------------
+// Power-of-two scaling of the FP32 recurrences.  The FP32 vectors (residual, search direction, correction) carry
+// the true residual times L.scale; a refresh that finds their mean square outside [2^-kScaleWindow, 2^kScaleWindow]
+// multiplies them by the power of two that brings it near 1.  Sums and products of FP32 values scale exactly by
+// powers of two, so the iterates and iteration counts do not depend on the scale of the system or of its
+// right-hand side (subnormals aside); unscaled, a residual near 1e-19 already made p.q underflow in FP32.
+constexpr int kScaleWindow = 24;
+__device__ __forceinline__ double rescale_factor(double meanSquare) {
+    if (!(meanSquare > 0.0) || isinf(meanSquare)) return 1.0;
+    const int e = ilogb(meanSquare);
+    if (e >= -kScaleWindow && e <= kScaleWindow) return 1.0;
+    const int k = -(e >> 1);   // floor(e / 2): the same factor for systems a power of four apart
+    return ldexp(1.0, max(-60, min(60, k)));
+}
+
 __device__ __forceinline__ void cg_loop_init(PcgLoop& L, const CgArgs& a) {
     L.rr64 = L.bb = L.target = L.rz = L.beta = 0.0;
+    L.scale = 1.0;
     L.rrBest = L.rrCycle = INFINITY;
     L.rrRef = 0.0;
     L.rr = 0.0;
@@ -1216,12 +1231,14 @@ static __device__ bool cg_mixed_refresh(Team& t, const CgArgs& a, double* stage,
     int rb, re;
     team_rows(a.n, t, rb, re);
     const double* b = a.bRowptr ? a.bOut : a.b;
+    const double sc = L.scale;
     if (!L.first) {   // fold the correction into x (FP64); the true residual gathers x across blocks
-        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
+        const double inv = 1.0 / sc;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i] * inv;
         if (!t.barrier(where++)) return false;
         if (L.innerBreakdown) L.resetP = 1;   // restart the recurrence from the true residual
     }
-    // true residual: r = b - A64 x; r32 = (float) r; d32 = 0
+    // true residual: r = b - A64 x; r32 = (float) (scale r); d32 = 0
     const double* xs = L.first ? a.x0 : a.x;
     double rrp = 0, bbp = 0, rip = 0;
     float* pp0 = L.flip ? a.p32b : a.p32a;
@@ -1231,7 +1248,7 @@ static __device__ bool cg_mixed_refresh(Team& t, const CgArgs& a, double* stage,
         [&](int row, double acc, double) {
             const double bi = b[row];
             const double ri = bi - acc;
-            const float r32 = (float)ri;
+            const float r32 = (float)(ri * sc);
             a.r32[row] = r32;
             if (f0) pp0[row] = r32;
             a.d32[row] = 0.0f;
@@ -1273,15 +1290,27 @@ static __device__ bool cg_mixed_refresh(Team& t, const CgArgs& a, double* stage,
     // more than 4x the interval returns towards innerTol.  Long cycles (the ill-conditioned pressure system, whose
     // refreshes cost nothing next to ~1000 FP32 iterations) keep innerTol.
     if (L.refresh > 0 && L.rr > 0.0) {
-        const double drift = L.rr64 / L.rr;
+        const double drift = L.rr64 * sc * sc / L.rr;
         if (drift < 4.0 && L.lastCycle < 32) L.cycleTol2 = fmax(L.cycleTol2 * 1e-2, 1e-8);
         else if (drift > 16.0) L.cycleTol2 = fmin(L.cycleTol2 * 1e2, a.innerTol2);
     }
     // continue the recurrence from the refreshed residual: beta' = |r_new|^2 / |r_prev|^2
     L.beta = L.resetP ? 0.0 : block_scalar(smem, [&] { return rrTrue / L.rrPrev; });
     L.resetP = 0;
-    L.rr = rrTrue;
-    L.rrRef = rrTrue;
+    double rrS = rrTrue;
+    const double f = rescale_factor(rrTrue / a.n);
+    if (f != 1.0) {   // own rows of r32 and of the direction the next product extends; gathered after a barrier
+        const float ff = (float)f;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) {
+            a.r32[i] *= ff;
+            pp0[i] *= ff;
+        }
+        rrS *= f * f;
+        L.scale = sc * f;
+        if (!t.barrier(where++)) return false;
+    }
+    L.rr = rrS;
+    L.rrRef = rrS;
     L.itRef = L.it;
     ++L.refresh;
     L.first = 0;
@@ -1298,6 +1327,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
     int rb, re;
     team_rows(a.n, t, rb, re);
     L.innerBreakdown = 0;
+    const double targetS = L.target * L.scale * L.scale;   // the stopping test in the FP32 vectors' scale
     while (L.it < a.maxIt) {
         const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -1367,7 +1397,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
         L.beta = block_scalar(smem, [&] { return rrs / L.rr; });
         L.rrPrev = L.rr;
         L.rr = rrs;
-        if (L.rr <= L.cycleTol2 * L.rrRef || L.rr <= L.target) break;   // time for a true residual
+        if (L.rr <= L.cycleTol2 * L.rrRef || L.rr <= targetS) break;   // time for a true residual
         if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;           // bound the work between true residuals
     }
     L.lastCycle = L.it - L.itRef;

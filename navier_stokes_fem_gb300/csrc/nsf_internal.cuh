@@ -192,6 +192,7 @@ struct GridSync {
 struct PcgLoop {
     double rr64, bb, target, rz, beta, rrBest, rrCycle, rrRef;
     double rr, rrPrev, cycleTol2;   // plain mixed CG: recursive r.r, its previous value, the cycle's tolerance
+    double scale;            // the FP32 vectors hold the true residual times this power of two
     int lastCycle;
     int it, refresh, stalls, itRef;
     int first, resetP, flip, innerBreakdown;

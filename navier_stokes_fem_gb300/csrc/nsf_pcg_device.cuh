@@ -321,6 +321,7 @@ static __device__ int pcg_fp64_body(Team& t, const CgArgs& a, double* stage, dou
 // Both return false on a barrier time-out.  partial regions: 0 = p.q, 1 = r.r, 2 = r64.r64, 3 = b.b, 4 = r.z
 __device__ __forceinline__ void pcg_loop_init(PcgLoop& L) {
     L.rr64 = L.bb = L.target = L.rz = L.beta = 0.0;
+    L.scale = 1.0;
     L.rrBest = L.rrCycle = INFINITY;
     L.rrRef = 0.0;
     L.it = L.refresh = L.stalls = L.itRef = 0;
@@ -344,12 +345,14 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
     float* w = F.w32;
     float* pprev = L.flip ? a.p32b : a.p32a;
     float* r32 = L.rflip ? a.r32b : a.r32;   // the current residual buffer
+    const double sc = L.scale;                // (the power-of-two scaling of team_cg_mixed's refresh)
     if (!L.first) {   // fold the FP32 correction into x; the true residual gathers x across blocks
-        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i];
+        const double inv = 1.0 / sc;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i] * inv;
         if (!t.barrier(where++)) return false;
         if (L.innerBreakdown) L.resetP = 1;
     }
-    // true residual r = b - A64 x, r32 = (float) r, d32 = 0, colour 0 of the forward sweep
+    // true residual r = b - A64 x, r32 = (float) (scale r), d32 = 0, colour 0 of the forward sweep
     const double* xs = L.first ? a.x0 : a.x;
     const bool resetP = L.resetP != 0;
     double rrp = 0, bbp = 0;
@@ -359,7 +362,7 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
                                                    [&](int row, double acc, double) {
                                                        const double bi = b[row];
                                                        const double ri = bi - acc;
-                                                       const float rf = (float)ri;
+                                                       const float rf = (float)(ri * sc);
                                                        r32[row] = rf;
                                                        a.d32[row] = 0.0f;
                                                        if (resetP) pprev[row] = 0.0f;   // restart: p = z
@@ -389,6 +392,20 @@ static __device__ bool pcg_mixed_refresh(Team& t, const CgArgs& a, double* stage
         L.stalls = 0;
     }
     L.rrBest = fmin(L.rrBest, L.rr64);
+    const double f = rescale_factor(L.rr64 * sc * sc / a.n);
+    if (f != 1.0) {   // own rows of r32, of y0 (colour 0) and of the previous direction; gathered after a barrier
+        const float ff = (float)f;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) {
+            r32[i] *= ff;
+            pprev[i] *= ff;
+            if (i < F.colourRow[1]) w[i] *= ff;
+        }
+        rzp.hi *= ff * ff;
+        rzp.lo *= ff * ff;
+        L.rz *= f * f;   // the previous cycle's r.z, for beta
+        L.scale = sc * f;
+        if (!t.barrier(where++)) return false;
+    }
     double rzT = 0;
     if (!precond_sweeps<float, float>(t, a, r32, w, F.loVal32, F.upVal32, F.dinv32, rzp, smem, where, rzT, ring))
         return false;
@@ -419,7 +436,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
     team_rows(a.n, t, rb, re);
     float* w = F.w32;
     L.innerBreakdown = 0;
-    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
+    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
     while (L.it < a.maxIt) {
         const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -543,7 +560,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
     }
     // The tests on p.q and r.r and the coefficient alpha are thread 0's, handed to every thread as decisions; the
     // r.z test and beta stay per thread (thread 0 alone owning them made the 64-register kernel spill).
-    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target);
+    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
     float betaf = (float)L.beta;
     while (L.it < a.maxIt) {
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -812,6 +829,7 @@ static __device__ void team_pcg_mixed_inner(Team& t, const CgArgs& a, double* st
     L.beta = G.beta;
     L.rrRef = G.rrRef;
     L.target = G.target;
+    L.scale = G.scale;
     L.it = G.it;
     L.itRef = G.itRef;
     L.flip = G.flip;

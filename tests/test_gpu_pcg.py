@@ -256,3 +256,35 @@ def test_fp16_factor_copies_only_within_range():
                                               solver="mixed")
         assert it < it_plain, (scale, it, it_plain)
         d.close()
+
+
+@pytest.mark.parametrize("name,solver", [("pressure_stiffness", "mixed"), ("pressure_stiffness", "pcg_mixed"),
+                                         ("diffusion", "mixed")])
+def test_mixed_solves_do_not_depend_on_the_scale(name, solver):
+    """The mixed solvers rescale their FP32 vectors by powers of two at the true-residual refreshes, so a right-hand
+    side 2^-60 times another (unscaled, p.q would fall below FP32's range) takes the same iterations and gives
+    exactly 2^-60 times the same solution; the plain mixed CG on the whole system times 2^-40 (its FP32 matrix
+    copy times 2^-40) gives exactly the same solution.  (The PCG's factor of 2^-40 A has values below FP16's
+    range and is read as FP32 instead, so that case would run other arithmetic.)"""
+    m = M.cavity(64)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    A = o.scipy_matrix(name).tocsr()
+    o.close()
+    b = np.random.default_rng(5).standard_normal(A.shape[0])
+    s = 2.0 ** -60
+    d = nsf.GPUSimulationDevice(0)
+    d.upload_matrix(name, A.indptr.astype(np.int32), A.indices, A.data, A.shape)
+    if solver == "pcg_mixed":
+        d.precond_ic0(name)
+    x, it, _ = d.conjugate_gradient(name, b, np.zeros_like(b), eps=TOL, solver=solver)
+    xs, its, _ = d.conjugate_gradient(name, b * s, np.zeros_like(b), eps=TOL, solver=solver)
+    d.close()
+    assert its == it and np.array_equal(xs, x * s), (it, its, rel(xs / s, x))
+    if solver == "mixed":
+        g = 2.0 ** -40
+        As = (A * g).tocsr()
+        d = nsf.GPUSimulationDevice(0)
+        d.upload_matrix(name, As.indptr.astype(np.int32), As.indices, As.data, As.shape)
+        xg, itg, _ = d.conjugate_gradient(name, b * g, np.zeros_like(b), eps=TOL, solver=solver)
+        d.close()
+        assert itg == it and np.array_equal(xg, x), (it, itg, rel(xg, x))

@@ -77,14 +77,19 @@ struct Team {
             __syncthreads();
             return true;
         }
+        // The CTA's writes reach thread 0's release through the bar.sync before it (release is cumulative), and the
+        // other CTAs' writes reach every thread's later loads through thread 0's acquire and the bar.sync after it,
+        // so no separate fences are needed.  The wait polls the counter alone and looks at the abort flag and the
+        // clock every 32nd poll (the first poll included, so a zero limit expires at once).
         __syncthreads();
         if (threadIdx.x == 0) {
             target += (unsigned long long)size;
-            __threadfence();
             red_add_release(&sync->arrived, 1ULL);
             int res = 1;
             const long long t0 = global_ns();
+            unsigned polls = 0;
             while (ld_acquire(&sync->arrived) < target) {
+                if ((polls++ & 31u) != 0) continue;
                 if (ld_volatile(&sync->abort)) { res = 0; break; }
                 if (global_ns() - t0 >= timeoutNs) {
                     if (atomicCAS(&sync->abort, 0, 1) == 0) sync->where = where;
@@ -92,7 +97,6 @@ struct Team {
                     break;
                 }
             }
-            __threadfence();
             ok = res;
         }
         __syncthreads();

@@ -255,6 +255,10 @@ int nsf_profile_read(nsf_device* h, int maxRecords, int* slot, int* mode, int* f
                      int* outer, float* ms);
 /* op 0 records a start event on the handle's stream, op 1 a stop event and writes the elapsed ms. */
 int nsf_timer(nsf_device* h, int op, float* ms);
+/* Page-locked host memory of `bytes` bytes, zeroed and mapped for the device.  Field transfers to or from it
+   (nsf_sim_set_fields, nsf_sim_get_fields, nsf_sim_step_host) run as copy kernels on the handle's stream: on a
+   coherent CPU-GPU link the copy engines are slow for a while after GPU work (12-24 ms against 1.7 ms for 302 MB
+   after a 2048-cavity step).  Other host pointers are copied with cudaMemcpyAsync.  Free with nsf_host_free. */
 int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr);
 int nsf_host_free(nsf_device* h, void* ptr);
 /* Number of kernels this handle has launched so far (all of the library's own kernels, memsets excluded). */

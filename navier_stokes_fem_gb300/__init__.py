@@ -466,7 +466,8 @@ class GPUSimulationDevice:
         self._check(library().nsf_flush_l2(self._h, int(nbytes)))
 
     def pinned(self, shape, dtype=np.float64):
-        """A numpy array in page-locked host memory (freed with the handle's process)."""
+        """A zeroed numpy array in page-locked host memory mapped for the device (freed with the handle's process);
+        set_fields, fields and step_host move fields to and from such arrays with copy kernels."""
         nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
         p = _v()
         self._check(library().nsf_host_alloc(self._h, max(nbytes, 1), ctypes.byref(p)))

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <map>
 #include <numeric>
 #include <stdexcept>
 
@@ -113,6 +114,73 @@ Factor& factor_for(nsf_device* h, int slot, bool needValues) {
     if (F.rows != A.rows || !F.lRowptr.get()) factor_structure(F, A, h->stream);
     if (needValues && !F.ready) throw Error{NSF_ERR_STATE, "slot " + std::to_string(slot) + " has no factor values"};
     return F;
+}
+
+// ---- host buffers that the GPU's own kernels copy ---------------------------------------------------------
+// On a coherent CPU-GPU link (Grace), copy-engine transfers that follow a stretch of GPU work are slow: right after
+// a step of the 2048 cavity, 12-24 ms device to host and 7-17 ms host to device for its 302 MB of fields, against
+// 1.7 ms for a copy kernel in either direction, and 1.6 ms for the copy engine once warm.  Page-locked buffers
+// from nsf_host_alloc are mapped for the device and zeroed by a kernel when they are allocated (the first kernel
+// access to host pages is slow, so it happens there), and the field transfers to and from them run as copy
+// kernels; other host pointers go through cudaMemcpyAsync.
+struct HostBlock {
+    size_t bytes;
+    char* dev;   // its device address
+};
+std::mutex g_hostMu;
+std::map<uintptr_t, HostBlock> g_hostBlocks;   // by host address
+
+// The device address of [p, p + bytes) when it lies inside one block from nsf_host_alloc, else null.
+void* host_block_device(const void* p, size_t bytes) {
+    std::lock_guard<std::mutex> lk(g_hostMu);
+    const uintptr_t a = (uintptr_t)p;
+    auto it = g_hostBlocks.upper_bound(a);
+    if (it == g_hostBlocks.begin()) return nullptr;
+    --it;
+    if (a + bytes > it->first + it->second.bytes) return nullptr;
+    return it->second.dev + (a - it->first);
+}
+
+// dst[0, bytes) = src[0, bytes) (src null: zeros), 16-byte words when both addresses and the size allow it, four
+// of them in flight per thread
+__global__ void copy_bytes_kernel(char* __restrict__ dst, const char* __restrict__ src, size_t bytes) {
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (size_t)gridDim.x * blockDim.x;
+    if ((((uintptr_t)dst | (uintptr_t)src | bytes) & 15) == 0) {
+        int4* d = reinterpret_cast<int4*>(dst);
+        const int4* s = reinterpret_cast<const int4*>(src);
+        const size_t n = bytes / 16;
+        for (size_t i0 = tid; i0 < n; i0 += 4 * nt) {
+            int4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const size_t i = i0 + u * nt;
+                v[u] = i < n && s ? s[i] : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const size_t i = i0 + u * nt;
+                if (i < n) d[i] = v[u];
+            }
+        }
+    } else {
+        for (size_t i = tid; i < bytes; i += nt) dst[i] = src ? src[i] : 0;
+    }
+}
+
+void copy_kernel_launch(nsf_device* h, void* dst, const void* src, size_t bytes) {
+    copy_bytes_kernel<<<h->smCount * 4, 256, 0, h->stream>>>(static_cast<char*>(dst), static_cast<const char*>(src),
+                                                            bytes);
+    NSF_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+// A field transfer between the device and the host on the handle's stream (see HostBlock).
+void field_copy(nsf_device* h, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    if (bytes == 0) return;
+    const bool toDevice = kind == cudaMemcpyHostToDevice;
+    void* mapped = host_block_device(toDevice ? src : dst, bytes);
+    if (mapped) copy_kernel_launch(h, toDevice ? dst : mapped, toDevice ? mapped : src, bytes);
+    else NSF_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, h->stream));
 }
 
 }  // namespace nsf
@@ -710,8 +778,8 @@ int nsf_sim_set_fields(nsf_device* h, const double* uv, const double* p) {
     sim_require(h);
     if (!uv || !p) throw bad_arg("null field");
     const int Nv = h->mesh.nNodes, P = h->mesh.nP;
-    NSF_CUDA(cudaMemcpyAsync(h->sim.uv.get(), uv, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice, h->stream));
-    NSF_CUDA(cudaMemcpyAsync(h->sim.p.get(), p, sizeof(double) * P, cudaMemcpyHostToDevice, h->stream));
+    field_copy(h, h->sim.uv.get(), uv, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice);
+    field_copy(h, h->sim.p.get(), p, sizeof(double) * P, cudaMemcpyHostToDevice);
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     NSF_END(h)
 }
@@ -720,8 +788,8 @@ int nsf_sim_get_fields(nsf_device* h, double* uv, double* p) {
     NSF_BEGIN(h)
     sim_require(h);
     const int Nv = h->mesh.nNodes, P = h->mesh.nP;
-    if (uv) NSF_CUDA(cudaMemcpyAsync(uv, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost, h->stream));
-    if (p) NSF_CUDA(cudaMemcpyAsync(p, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost, h->stream));
+    if (uv) field_copy(h, uv, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost);
+    if (p) field_copy(h, p, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost);
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     NSF_END(h)
 }
@@ -737,11 +805,11 @@ int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int 
     NSF_BEGIN(h)
     sim_require(h);
     const int Nv = h->mesh.nNodes, P = h->mesh.nP;
-    if (uvIn) NSF_CUDA(cudaMemcpyAsync(h->sim.uv.get(), uvIn, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice, h->stream));
-    if (pIn) NSF_CUDA(cudaMemcpyAsync(h->sim.p.get(), pIn, sizeof(double) * P, cudaMemcpyHostToDevice, h->stream));
+    if (uvIn) field_copy(h, h->sim.uv.get(), uvIn, sizeof(double) * 2 * Nv, cudaMemcpyHostToDevice);
+    if (pIn) field_copy(h, h->sim.p.get(), pIn, sizeof(double) * P, cudaMemcpyHostToDevice);
     run_steps(h, nsteps, iterations);
-    if (uvOut) NSF_CUDA(cudaMemcpyAsync(uvOut, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost, h->stream));
-    if (pOut) NSF_CUDA(cudaMemcpyAsync(pOut, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost, h->stream));
+    if (uvOut) field_copy(h, uvOut, h->sim.uv.get(), sizeof(double) * 2 * Nv, cudaMemcpyDeviceToHost);
+    if (pOut) field_copy(h, pOut, h->sim.p.get(), sizeof(double) * P, cudaMemcpyDeviceToHost);
     NSF_CUDA(cudaStreamSynchronize(h->stream));
     NSF_END(h)
 }
@@ -1075,13 +1143,35 @@ int nsf_timer(nsf_device* h, int op, float* ms) {
 int nsf_host_alloc(nsf_device* h, size_t bytes, void** ptr) {
     NSF_BEGIN(h)
     if (!ptr) throw bad_arg("null output pointer");
-    NSF_CUDA(cudaMallocHost(ptr, bytes));
+    if (bytes == 0) throw bad_arg("zero bytes");
+    *ptr = nullptr;
+    void* p = nullptr;
+    NSF_CUDA(cudaHostAlloc(&p, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+    try {
+        void* dev = nullptr;
+        NSF_CUDA(cudaHostGetDevicePointer(&dev, p, 0));
+        copy_kernel_launch(h, dev, nullptr, bytes);   // zeroes it from the GPU: maps its pages for the device now
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        std::lock_guard<std::mutex> lk(g_hostMu);
+        g_hostBlocks[(uintptr_t)p] = HostBlock{bytes, static_cast<char*>(dev)};
+    } catch (...) {
+        cudaFreeHost(p);
+        throw;
+    }
+    *ptr = p;
     NSF_END(h)
 }
 
 int nsf_host_free(nsf_device* h, void* ptr) {
     NSF_BEGIN(h)
-    if (ptr) NSF_CUDA(cudaFreeHost(ptr));
+    if (ptr) {
+        NSF_CUDA(cudaStreamSynchronize(h->stream));
+        {
+            std::lock_guard<std::mutex> lk(g_hostMu);
+            g_hostBlocks.erase((uintptr_t)ptr);
+        }
+        NSF_CUDA(cudaFreeHost(ptr));
+    }
     NSF_END(h)
 }
 

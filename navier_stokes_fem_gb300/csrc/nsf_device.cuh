@@ -1198,6 +1198,21 @@ __device__ __forceinline__ double rescale_factor(double meanSquare) {
     return ldexp(1.0, max(-60, min(60, k)));
 }
 
+// The FP32 correction d is folded into the FP64 iterate every kFoldEvery iterations of a cycle, inside the x/r
+// update (x_i += d_i / scale, d_i = 0; a row's own entries only, so no barrier), so that d's FP32 sums restart
+// from zero and their rounding (about eps32 |d| per update) stays small.  Summed over a whole cycle of thousands
+// of iterations, that rounding put high-frequency noise into x which the recursive residual does not see: on the
+// first steps of the 2048 cavity it made refresh cycles look drifted and cost 31,078 pressure iterations over
+// steps 1-5 of the run against 23,698 with the fold (the FP64 PCG's 5,985 and 6,010 at steps 1 and 2 are matched).
+constexpr int kFoldEvery = 16;
+__device__ __forceinline__ bool fold_iteration(const PcgLoop& L) { return (L.it + 1 - L.itRef) % kFoldEvery == 0; }
+// d_i's new value, after folding it into x_i when `fold` is set
+__device__ __forceinline__ float fold_correction(const CgArgs& a, int i, float dNew, bool fold, double inv) {
+    if (!fold) return dNew;
+    a.x[i] += (double)dNew * inv;
+    return 0.0f;
+}
+
 __device__ __forceinline__ void cg_loop_init(PcgLoop& L, const CgArgs& a) {
     L.rr64 = L.bb = L.target = L.rz = L.beta = 0.0;
     L.scale = 1.0;
@@ -1332,6 +1347,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
     team_rows(a.n, t, rb, re);
     L.innerBreakdown = 0;
     const double targetS = L.target * L.scale * L.scale;   // the stopping test in the FP32 vectors' scale
+    const double invScale = 1.0 / L.scale;
     while (L.it < a.maxIt) {
         const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -1372,6 +1388,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
         const double pqs = grid_sum(a.partials, G, smem);
         if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
         const float alphaf = (float)block_scalar(smem, [&] { return L.rr / pqs; });
+        const bool fold = fold_iteration(L);
         float rrHi = 0.f, rrLo = 0.f;
         for (int i0 = rb + (int)threadIdx.x; i0 < re; i0 += R * bs) {
             float pi[R], qi[R], di[R], ri[R];
@@ -1384,7 +1401,7 @@ static __device__ bool cg_mixed_inner(Team& t, const CgArgs& a, double* stage, d
             for (int u = 0; u < R; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) {
-                    a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                    a.d32[i] = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
                     const float rn = fmaf(-alphaf, qi[u], ri[u]);
                     a.r32[i] = rn;
                     df_acc(rrHi, rrLo, rn, rn);

@@ -437,6 +437,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
     float* w = F.w32;
     L.innerBreakdown = 0;
     const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
+    const double invScale = 1.0 / L.scale;
     while (L.it < a.maxIt) {
         const float betaf = (float)L.beta;
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -455,6 +456,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
         const double pqs = grid_sum(a.partials, G, smem);
         if (!(pqs > 0.0) || isinf(pqs)) { L.innerBreakdown = 1; break; }
         const float alphaf = (float)block_scalar(smem, [&] { return L.rz / pqs; });
+        const bool fold = fold_iteration(L);
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
         constexpr int R = Lean ? kRowsLean : kRows;
@@ -475,7 +477,7 @@ static __device__ bool pcg_mixed_inner(Team& t, const CgArgs& a, double* stage, 
             for (int u = 0; u < R; ++u) {
                 const int i = i0 + u * bs;
                 if (i < re) {
-                    a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                    a.d32[i] = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
                     const float rn = fmaf(-alphaf, qi[u], ri[u]);
                     a.r32[i] = rn;
                     df_acc(rrHi, rrLo, rn, rn);
@@ -561,6 +563,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
     // The tests on p.q and r.r and the coefficient alpha are thread 0's, handed to every thread as decisions; the
     // r.z test and beta stay per thread (thread 0 alone owning them made the 64-register kernel spill).
     const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
+    const double invScale = 1.0 / L.scale;
     float betaf = (float)L.beta;
     while (L.it < a.maxIt) {
         const float* pp = L.flip ? a.p32b : a.p32a;
@@ -607,6 +610,7 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
         const Decision da = decision_get(smem);
         if (da.code) { L.innerBreakdown = 1; break; }
         const float alphaf = da.v;
+        const bool fold = fold_iteration(L);
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
         // colours other than 1: d += alpha p, r -= alpha q; colour 0 also y0 = r / L_00
@@ -632,8 +636,9 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                 for (int u = 0; u < kRowsLean; ++u) {
                     const int i = i0 + u * bs;
                     if (i < r1) {
-                        if constexpr (Resident) nsf_row_state[i - c0b] = fmaf(alphaf, pi[u], di[u]);
-                        else a.d32[i] = fmaf(alphaf, pi[u], di[u]);
+                        const float dn = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
+                        if constexpr (Resident) nsf_row_state[i - c0b] = dn;
+                        else a.d32[i] = dn;
                         const float rn = fmaf(-alphaf, qi[u], ri[u]);
                         rNew[i] = rn;
                         df_acc(rrHi, rrLo, rn, rn);
@@ -660,11 +665,12 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
                     if constexpr (Resident) {
                         const int k = i - c1b;
                         rn = fmaf(-alphaf, nsf_row_state[n0 + 2 * n1 + k], nsf_row_state[n0 + n1 + k]);
-                        nsf_row_state[n0 + k] = fmaf(alphaf, pc[i], nsf_row_state[n0 + k]);
+                        nsf_row_state[n0 + k] =
+                            fold_correction(a, i, fmaf(alphaf, pc[i], nsf_row_state[n0 + k]), fold, invScale);
                         nsf_row_state[n0 + n1 + k] = rn;
                     } else {
                         rn = fmaf(-alphaf, a.q32[i], rOld[i]);
-                        a.d32[i] = fmaf(alphaf, pc[i], a.d32[i]);
+                        a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
                         rNew[i] = rn;
                     }
                     df_acc(rrHi, rrLo, rn, rn);

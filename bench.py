@@ -130,6 +130,10 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+# the mixed solvers fold their FP32 correction into the FP64 iterate every FOLD_EVERY iterations of a cycle
+FOLD_EVERY = 16
+
+
 def algorithmic_bytes(mode, n, nnz, its, outer, pipelined=False):
     """Minimal DRAM bytes of one persistent CG launch (int32 indices).
 
@@ -137,8 +141,9 @@ def algorithmic_bytes(mode, n, nnz, its, outer, pipelined=False):
     read+write with p and q reads; p update reads r, p and writes p).  Prologue: one SpMV with x0 plus b, r, p, x.
     The pipelined FP64 form moves 13 passes (its product gathers w; z, s, p, x, r and w read and written), and
     every replacement (outer - 1 of them) four products.
-    Mixed: inner FP32 iterations nnz*(4+4) + 4(n+1) + 11*4n; every refinement sweep one FP64 residual
-    nnz*(8+4) + 4(n+1) + 28n and an x += d pass of 20n.
+    Mixed: inner FP32 iterations nnz*(4+4) + 4(n+1) + 11*4n, plus the FP64 x read and written every
+    FOLD_EVERY iterations when the correction is folded into it (16n / FOLD_EVERY); every refinement sweep one FP64
+    residual nnz*(8+4) + 4(n+1) + 28n and an x += d pass of 20n.
     """
     if mode == 0:
         passes = 13 if pipelined else 11
@@ -146,7 +151,7 @@ def algorithmic_bytes(mode, n, nnz, its, outer, pipelined=False):
         prologue = 12 * nnz + 4 * (n + 1) + 40 * n
         extra = max(outer - 1, 0) * 4 * (12 * nnz + 4 * (n + 1) + 24 * n) if pipelined else 0
         return prologue + extra + its * it_bytes
-    inner = 8 * nnz + 4 * (n + 1) + 44 * n
+    inner = 8 * nnz + 4 * (n + 1) + 44 * n + 16 * n / FOLD_EVERY
     sweep = 12 * nnz + 4 * (n + 1) + 28 * n
     return (outer + 1) * sweep + outer * 20 * n + its * inner
 
@@ -294,11 +299,12 @@ def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None):
     update, the sweeps' right-hand sides, inverse diagonals and in-place results), 11 when the inner kernel keeps
     the correction (read and written every iteration) and the colour-1 rows' r and q (half the rows) in shared
     memory.  The mixed form moves FP32 values and vectors - the factor's values in FP16 where the factor keeps FP16
-    copies (fvb = 2 bytes per factor value) - and adds an FP64 residual (int32 indices) per refresh."""
+    copies (fvb = 2 bytes per factor value), reads and writes the FP64 x every FOLD_EVERY iterations (the correction
+    fold) - and adds an FP64 residual (int32 indices) per refresh."""
     v = 4 if mixed else 8
     fv = v if fvb is None or not mixed else fvb
     passes = 11 if resident else 15
-    it_bytes = (v + idx) * nz + (fv + idx) * 2 * nzl + 4 * (n + 1) + passes * v * n
+    it_bytes = (v + idx) * nz + (fv + idx) * 2 * nzl + 4 * (n + 1) + passes * v * n + (16 * n / FOLD_EVERY if mixed else 0)
     refresh = 12 * nz + 4 * (n + 1) + 28 * n
     return (outer + 1) * refresh + its * it_bytes
 

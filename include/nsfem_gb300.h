@@ -79,10 +79,16 @@ enum nsf_solver {
 enum nsf_cg_form {
     NSF_CG_FORM_AUTO = 0,       /* pipelined below NSF_CG_PIPELINED_MAX_ROWS rows, three barriers above */
     NSF_CG_FORM_THREE_SYNC = 1, /* q = A p and p.q | x, r and r.r | p = r + beta p: three grid barriers */
-    NSF_CG_FORM_PIPELINED = 2   /* one grid barrier per iteration: the recurrences of pipelined CG (Ghysels and
+    NSF_CG_FORM_PIPELINED = 2,  /* one grid barrier per iteration: the recurrences of pipelined CG (Ghysels and
                                  * Vanroose 2014) carry A r, A p and A A p, so the one product per iteration acts on
                                  * a vector finished before the barrier; two more vector passes and about five more
                                  * FP64 operations per row, and a final true-residual check */
+    NSF_CG_FORM_MULTI_KERNEL = 3 /* the reference's conjugateGradientMultiKernel (cpp/gpu_simulation_device.cpp:
+                                 * 293-383, its conjugateGradient(..., useMegakernel = false)): one ordinary launch
+                                 * per phase (q = A p with p.q; x, r and r.r; p = r + beta p), the kernel boundaries
+                                 * as the grid-wide syncs, alpha and beta computed on the device by the last CTA of
+                                 * each reduction, 8 iterations per CUDA graph replay and the host reading the
+                                 * stopping state once per replay instead of twice per iteration */
 };
 
 /* NSF_CG_FORM_AUTO's crossover, from GB300 measurements of both forms on the cavity and channel systems */

@@ -36,7 +36,7 @@ STATUS = {0: "NSF_OK", 1: "NSF_ERR_CUDA", 2: "NSF_ERR_NOT_CONVERGED", 3: "NSF_ER
           4: "NSF_ERR_BARRIER_TIMEOUT", 5: "NSF_ERR_BAD_ARG", 6: "NSF_ERR_STATE", 7: "NSF_ERR_NO_DEVICE"}
 SLOT = {"pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
         "pressure_divergence": 4, "velocity_lift": 5, "pressure_lift": 6}
-CG_FORM = {"auto": 0, "three_sync": 1, "pipelined": 2}
+CG_FORM = {"auto": 0, "three_sync": 1, "pipelined": 2, "multi_kernel": 3}
 SOLVER = {"fp64": 0, "mixed": 1, "pcg_mixed": 2, "pcg_fp64": 3}
 PRECOND = {0: "none", 1: "ic0", 2: "learned"}
 
@@ -366,7 +366,8 @@ class GPUSimulationDevice:
         self._check(library().nsf_set_solver(self._h, SOLVER[solver], float(inner_tolerance)))
 
     def set_cg_form(self, form="auto"):
-        """Iteration form of the plain FP64 CG: "auto", "three_sync" or "pipelined" (one grid barrier)."""
+        """Iteration form of the plain FP64 CG: "auto", "three_sync", "pipelined" (one grid barrier) or
+        "multi_kernel" (one launch per phase, the reference's conjugateGradientMultiKernel)."""
         self._check(library().nsf_set_cg_form(self._h, CG_FORM[form]))
 
     def set_barrier_timeout(self, seconds):

@@ -342,6 +342,8 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
         h->innerForm[slot] = pcg_mixed_split_launch(ws, a, h->stream);
     else if (mode == NSF_SOLVER_MIXED && wide)
         cg_mixed_split_launch(ws, a, h->stream);
+    else if (mode == NSF_SOLVER_FP64 && h->cgForm == NSF_CG_FORM_MULTI_KERNEL)
+        cg_multi_launch(ws, a, wide, h->stream);
     else if (mode == NSF_SOLVER_FP64 && use_pipelined_cg(h, S))
         cg_pipe_launch(ws, a, wide, h->stream);
     else
@@ -965,7 +967,7 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
 
 int nsf_set_cg_form(nsf_device* h, int form) {
     NSF_BEGIN(h)
-    if (form < NSF_CG_FORM_AUTO || form > NSF_CG_FORM_PIPELINED) throw bad_arg("unknown CG form");
+    if (form < NSF_CG_FORM_AUTO || form > NSF_CG_FORM_MULTI_KERNEL) throw bad_arg("unknown CG form");
     h->cgForm = form;
     NSF_END(h)
 }

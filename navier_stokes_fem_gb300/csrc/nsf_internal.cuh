@@ -258,6 +258,28 @@ struct CgArgs {
     double* wbuf1;
 };
 
+// Scalars of the multi-kernel FP64 CG (cg_multi_launch), kept on the device between its kernels.
+struct CgMultiState {
+    double rr, bb, target, alpha, beta;
+    int it, status, done, maxIt;
+    unsigned int arrived;   // CTAs of the running kernel that have posted their partial sums
+};
+
+// Page-locked host slots the multi-kernel CG's state is copied to after each graph replay, and the events the
+// host waits on (created on first use, released with the workspace).
+struct CgMultiHost {
+    CgMultiState* slot = nullptr;   // two slots: one replay is checked while the next one runs
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    CgMultiHost() = default;
+    CgMultiHost(const CgMultiHost&) = delete;
+    CgMultiHost& operator=(const CgMultiHost&) = delete;
+    ~CgMultiHost() {
+        if (slot) cudaFreeHost(slot);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
 // the workspace shared by every solve on a handle (sized for the largest system)
 struct CgWorkspace {
     DevBuf<double> r, q, p0, p1, w, xp, bp;
@@ -266,6 +288,8 @@ struct CgWorkspace {
     DevBuf<GridSync> sync;
     DevBuf<CgInfo> info;     // ring of infos (one per solve in a step)
     DevBuf<PcgLoop> loop;    // split mixed PCG control state
+    DevBuf<CgMultiState> multi;   // multi-kernel FP64 CG scalars
+    CgMultiHost multiHost;
     int grid = 0;            // persistent grid size (blocks)
     int block = 0;
     int gridInner = 0;       // grid of the split mixed PCG's inner-iteration kernel
@@ -287,6 +311,9 @@ void cg_pipe_launch(CgWorkspace& ws, const CgArgs& a, bool wide, cudaStream_t s)
 int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s);
 // The split plain mixed CG (wide systems): the same launch pattern.
 void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s);
+// The FP64 CG as one ordinary launch per phase (NSF_CG_FORM_MULTI_KERNEL), replayed as CUDA graphs of several
+// iterations; returns after the solve finished (the host polls its state once per replay).
+void cg_multi_launch(CgWorkspace& ws, const CgArgs& a, bool wide, cudaStream_t s);
 void spmv_launch(const Csr& A, const double* x, double* y, cudaStream_t s);
 void spmv_rhs_launch(const Csr& A, const double* x, const double* lift, const unsigned char* mask,
                      const double* bcValue, double* y, cudaStream_t s);

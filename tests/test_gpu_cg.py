@@ -29,10 +29,11 @@ def _relres(o, name, x, b):
     return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("form", ["three_sync", "pipelined"])
+@pytest.mark.parametrize("form", ["three_sync", "pipelined", "multi_kernel"])
 @pytest.mark.parametrize("name", ["pressure_stiffness", "diffusion", "velocity_mass"])
 def test_fp64_cg_matches_oracle(system, name, form):
-    """Both iteration forms of the FP64 megakernel (three grid barriers, or one with the pipelined recurrences)."""
+    """Every iteration form of the FP64 CG: the megakernel with three grid barriers, or one with the pipelined
+    recurrences, and the multi-kernel form (one launch per phase, the reference's conjugateGradientMultiKernel)."""
     d, o = system
     n = d.matrix_shape(name)[0]
     rng = np.random.default_rng(1)
@@ -51,7 +52,7 @@ def test_fp64_cg_matches_oracle(system, name, form):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
 
 
-@pytest.mark.parametrize("form", ["three_sync", "pipelined"])
+@pytest.mark.parametrize("form", ["three_sync", "pipelined", "multi_kernel"])
 def test_fp64_cg_forms_on_a_larger_pressure_system(form):
     """The 256 x 256 cavity's pressure system (66 k rows, about 700 iterations from zero): the true residual meets
     the tolerance and the iteration count stays within 2 % of the oracle CG's, for both forms."""
@@ -83,8 +84,17 @@ def test_mixed_cg_reaches_fp64_residual(system, name):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
 
 
-def test_cg_edge_cases(system):
+@pytest.mark.parametrize("form", ["three_sync", "multi_kernel"])
+def test_cg_edge_cases(system, form):
     d, o = system
+    d.set_cg_form(form)
+    try:
+        _edge_cases(d)
+    finally:
+        d.set_cg_form("auto")
+
+
+def _edge_cases(d):
     name = "pressure_stiffness"
     n = d.matrix_shape(name)[0]
     z = np.zeros(n)
@@ -106,8 +116,10 @@ def test_cg_edge_cases(system):
     assert e.value.status == 3
 
 
-def test_cg_breakdown_on_indefinite_matrix():
+@pytest.mark.parametrize("form", ["three_sync", "multi_kernel"])
+def test_cg_breakdown_on_indefinite_matrix(form):
     d = nsf.GPUSimulationDevice(0)
+    d.set_cg_form(form)
     n = 64
     A = sp.diags([np.r_[np.ones(n // 2), -np.ones(n // 2)]], [0]).tocsr()
     d.upload_matrix("velocity_mass", A.indptr, A.indices, A.data, A.shape)
@@ -115,6 +127,31 @@ def test_cg_breakdown_on_indefinite_matrix():
         d.conjugate_gradient("velocity_mass", np.ones(n), np.zeros(n))
     assert e.value.status == 3
     d.close()
+
+
+def test_multi_kernel_form_repeats_the_megakernel(system):
+    """The multi-kernel form runs the three-barrier megakernel's products, row partition and fixed-order
+    reductions, with alpha and beta formed on the device: the same iteration count and, up to the last bits, the same
+    iterate, on solves that stop at the tolerance and at an iteration cap (which spans several graph replays and
+    stops inside one)."""
+    d, o = system
+    for name in ("pressure_stiffness", "diffusion"):
+        n = d.matrix_shape(name)[0]
+        rng = np.random.default_rng(11)
+        b = rng.standard_normal(n)
+        x0 = 0.05 * rng.standard_normal(n)
+        for max_it in (-1, 21):
+            out = {}
+            for form in ("three_sync", "multi_kernel"):
+                d.set_cg_form(form)
+                out[form] = d.conjugate_gradient(name, b, x0, eps=TOL, max_iterations=max_it, raise_on_error=False)
+            d.set_cg_form("auto")
+            x3, it3, _, st3 = out["three_sync"]
+            xm, itm, _, stm = out["multi_kernel"]
+            assert (itm, stm) == (it3, st3), (name, max_it, itm, it3, stm, st3)
+            assert np.linalg.norm(xm - x3) <= 1e-12 * np.linalg.norm(x3), (name, max_it)
+            if max_it == 21:
+                assert stm == 2 and itm == 21
 
 
 def test_barrier_time_limit_returns_status_and_handle_survives(system):

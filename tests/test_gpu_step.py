@@ -40,6 +40,19 @@ def test_cavity32_100_steps_fp64():
     assert abs(int(it.sum()) - int(rit.sum())) <= 0.01 * rit.sum()
 
 
+def test_cavity32_steps_multi_kernel_cg():
+    """The whole step with every FP64 solve in the multi-kernel form (fused right-hand sides included)."""
+    m = M.cavity(32)
+    sim = nsf.NavierStokesAssembly(m, 0.01, 0.01)
+    sim.set_cg_form("multi_kernel")
+    it = sim.step(20)
+    uv, p = sim.fields()
+    sim.close()
+    ruv, rp, rit = _oracle(m, 0.01, 0.01, 20)
+    assert rel(uv, ruv) < FIELD_TOL and rel(p, rp) < FIELD_TOL
+    assert np.abs(it - rit).max() <= 3
+
+
 def test_mesh_small_reference_asset(golden):
     m = golden_mesh(golden, "mesh_small")
     uv, p, it = _run(m, 0.001, 0.01, 20)

@@ -91,6 +91,17 @@ enum nsf_cg_form {
                                  * stopping state once per replay instead of twice per iteration */
 };
 
+/* Iteration form of the split mixed PCG on a two-colour system (nsf_set_pcg_form).  The reference preconditions
+ * with IC0 under USE_PRECONDITIONING (include/assembly.h:33-35, 1338-1344) and has no reduced form. */
+enum nsf_pcg_form {
+    NSF_PCG_FORM_AUTO = 0,     /* full */
+    NSF_PCG_FORM_FULL = 1,     /* PCG on the whole permuted system: product, forward and backward colour sweeps */
+    NSF_PCG_FORM_REDUCED = 2   /* two colours only (else full): the colour-0 unknowns are eliminated exactly (their
+                                * block of a two-colour matrix is diagonal) and PCG runs on the Schur complement with
+                                * the factor's colour-1 diagonal as preconditioner: with IC(0) the same iterates,
+                                * half the matrix entries and gathers per iteration, no factor sweeps */
+};
+
 /* NSF_CG_FORM_AUTO's crossover, from GB300 measurements of both forms on the cavity and channel systems */
 #define NSF_CG_PIPELINED_MAX_ROWS 2000000
 
@@ -158,7 +169,8 @@ int nsf_precond_index_bytes(nsf_device* h, int slot);
 int nsf_precond_value_bytes(nsf_device* h, int slot);
 /* The inner-iteration kernel the slot's last split mixed PCG solve ran: 0 four 256-thread CTAs per SM (one colour),
  * 1 one 1024-thread CTA per SM, 2 the same with the row state only a CTA reads resident in its shared memory (two
- * colours, where it fits); -1 before the slot's first such solve. */
+ * colours, where it fits), 3 the reduced (Schur complement) iteration of nsf_pcg_form; -1 before the slot's first
+ * such solve. */
 int nsf_precond_inner_form(nsf_device* h, int slot, int* form);
 int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
@@ -228,6 +240,21 @@ int nsf_sim_step(nsf_device* h, int nsteps, int* iterations);
 int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int nsteps, double* uvOut,
                       double* pOut, int* iterations);
 
+/* Time-dependent Dirichlet data.  The reference's expression grammar accepts the variable t
+ * (cpp/expression.cpp:167-177) but its imposeVelocityDirichlet (include/assembly.h:1559-1579) evaluates the
+ * expressions with x and y only; this replaces those host evaluations by device-side ones that may use t.
+ * expressions: nExpressions strings in the mesh-file grammar (variables x, y and t; at most 64 operations and a
+ * stack depth of 16 each).  velocityU / velocityV: for every velocity Dirichlet occurrence given to nsf_sim_setup,
+ * in that order, the index of its u and v expression; pressure: the same for the pressure occurrences.  The call
+ * evaluates the data at t0 (imposed values, lifts) and imposes the velocity values on the resident field, as the
+ * set-up imposes the constant data; step k after it then uses the data at t0 + k dt, the time the step ends, for
+ * its right-hand sides, lifts and re-imposed values (one small kernel and three CSR products per step).  The
+ * data stay time-dependent until the next nsf_sim_setup.  The batched form does not take expressions. */
+int nsf_sim_set_bc_expressions(nsf_device* h, int nExpressions, const char* const* expressions, const int* velocityU,
+                               const int* velocityV, const int* pressure, double t0);
+/* Simulated time of the resident fields: t0 (0 after nsf_sim_setup) + steps taken since then x dt. */
+int nsf_sim_time(nsf_device* h, double* t);
+
 /* ---- batched form: many independent instances in one persistent launch per step -------------------- */
 /* No single counterpart in the reference, which runs one mesh per process: each instance is a complete
  * NavierStokesAssembly problem (same arguments as nsf_sim_setup).  nsf_batch_add assembles one instance and
@@ -251,6 +278,8 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance);
 /* form: nsf_cg_form; applies to the plain FP64 CG solves of this handle (the iteration count is that of CG up to
  * rounding: the pipelined recurrences may take a few more iterations on ill-conditioned systems). */
 int nsf_set_cg_form(nsf_device* h, int form);
+/* form: nsf_pcg_form; applies to the mixed-precision PCG solves (NSF_SOLVER_PCG_MIXED) of narrow systems. */
+int nsf_set_pcg_form(nsf_device* h, int form);
 int nsf_set_barrier_timeout(nsf_device* h, double seconds);
 /* Records CUDA events around every persistent CG launch while enabled (clears previous records). */
 int nsf_profile(nsf_device* h, int enable);
@@ -299,6 +328,10 @@ int nsf_conjugate_gradient_noalloc(int rows, const int* rowptr_dev, const int* c
  * other than x and y; the message is written to `message` (may be NULL) up to `messageBytes`. */
 int nsf_eval_expression(const char* expression, double x, double y, double* value, char* message,
                         size_t messageBytes);
+/* The same with the variable t as well, evaluated on the host through the postfix program that
+ * nsf_sim_set_bc_expressions compiles for the device, op for op as the device runs it. */
+int nsf_eval_expression_t(const char* expression, double x, double y, double t, double* value, char* message,
+                          size_t messageBytes);
 
 #ifdef __cplusplus
 }

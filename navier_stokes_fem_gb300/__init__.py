@@ -37,6 +37,7 @@ STATUS = {0: "NSF_OK", 1: "NSF_ERR_CUDA", 2: "NSF_ERR_NOT_CONVERGED", 3: "NSF_ER
 SLOT = {"pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
         "pressure_divergence": 4, "velocity_lift": 5, "pressure_lift": 6}
 CG_FORM = {"auto": 0, "three_sync": 1, "pipelined": 2, "multi_kernel": 3}
+PCG_FORM = {"auto": 0, "full": 1, "reduced": 2}
 SOLVER = {"fp64": 0, "mixed": 1, "pcg_mixed": 2, "pcg_fp64": 3}
 PRECOND = {0: "none", 1: "ic0", 2: "learned"}
 
@@ -88,6 +89,7 @@ _SIGS = {
     "nsf_set_tolerance": (_i, [_v, _d]),
     "nsf_set_solver": (_i, [_v, _i, _d]),
     "nsf_set_cg_form": (_i, [_v, _i]),
+    "nsf_set_pcg_form": (_i, [_v, _i]),
     "nsf_set_barrier_timeout": (_i, [_v, _d]),
     "nsf_profile": (_i, [_v, _i]),
     "nsf_profile_read": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.int32), _arr(np.int32),
@@ -123,6 +125,9 @@ _SIGS = {
     "nsf_host_alloc": (_i, [_v, _sz, _P(_v)]),
     "nsf_host_free": (_i, [_v, _v]),
     "nsf_eval_expression": (_i, [ctypes.c_char_p, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
+    "nsf_eval_expression_t": (_i, [ctypes.c_char_p, _d, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
+    "nsf_sim_set_bc_expressions": (_i, [_v, _i, _v, _v, _v, _v, _d]),
+    "nsf_sim_time": (_i, [_v, _P(_d)]),
     "nsf_launch_count": (_i, [_v, _P(_i64)]),
     "nsf_batch_clear": (_i, [_v]),
     "nsf_batch_add": (_i, [_v, _i, _arr(np.float32), _i, _arr(np.int32), _i, _i, _arr(np.int32), _arr(np.float64),
@@ -160,30 +165,42 @@ def declared_symbols():
     return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+\**(nsf_\w+)\s*\(", text, re.M)))
 
 
-def evaluate_expression(expression: str, x: float, y: float) -> float:
-    """A mesh-file boundary expression evaluated by the library's C++ evaluator (double precision)."""
+def evaluate_expression(expression: str, x: float, y: float, t: float | None = None) -> float:
+    """A mesh-file boundary expression evaluated by the library's C++ evaluator (double precision); with t, the
+    variable t as well."""
     out = _d()
     msg = ctypes.create_string_buffer(256)
-    st = library().nsf_eval_expression(expression.encode(), float(x), float(y), ctypes.byref(out), msg, 256)
+    if t is None:
+        st = library().nsf_eval_expression(expression.encode(), float(x), float(y), ctypes.byref(out), msg, 256)
+    else:
+        st = library().nsf_eval_expression_t(expression.encode(), float(x), float(y), float(t), ctypes.byref(out),
+                                             msg, 256)
     if st != 0:
         raise NSFemError(st, msg.value.decode())
     return out.value
 
 
-def bc_occurrences(mesh):
-    """Dirichlet data per listed occurrence in the mesh's group order, values evaluated at each node."""
+def uses_time(expression: str) -> bool:
+    """True when a mesh-file expression contains the variable t (the grammar's only lower-case letters are the
+    variables and the function names sin and cos)."""
+    return "t" in expression.replace("Pi", "")
+
+
+def bc_occurrences(mesh, t: float | None = None):
+    """Dirichlet data per listed occurrence in the mesh's group order, values evaluated at each node (at time t
+    when given)."""
     un, gu, gv, pn, gp = [], [], [], [], []
     for nodes, ue, ve in mesh.u_dirichlet:
         for nd in np.asarray(nodes):
             x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
             un.append(int(nd))
-            gu.append(evaluate_expression(ue, x, y))
-            gv.append(evaluate_expression(ve, x, y))
+            gu.append(evaluate_expression(ue, x, y, t))
+            gv.append(evaluate_expression(ve, x, y, t))
     for nodes, pe in mesh.p_dirichlet:
         for nd in np.asarray(nodes):
             x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
             pn.append(int(nd))
-            gp.append(evaluate_expression(pe, x, y))
+            gp.append(evaluate_expression(pe, x, y, t))
     return (np.asarray(un, np.int32), np.asarray(gu, np.float64), np.asarray(gv, np.float64),
             np.asarray(pn, np.int32), np.asarray(gp, np.float64))
 
@@ -364,6 +381,11 @@ class GPUSimulationDevice:
 
     def set_solver(self, solver="fp64", inner_tolerance=-1.0):
         self._check(library().nsf_set_solver(self._h, SOLVER[solver], float(inner_tolerance)))
+
+    def set_pcg_form(self, form="auto"):
+        """Iteration of the mixed PCG on two-colour systems: "full" (product and both colour sweeps on the whole
+        system; "auto" is the same) or "reduced" (PCG on the Schur complement of the colour-0 block)."""
+        self._check(library().nsf_set_pcg_form(self._h, PCG_FORM[form]))
 
     def set_cg_form(self, form="auto"):
         """Iteration form of the plain FP64 CG: "auto", "three_sync", "pipelined" (one grid barrier) or
@@ -599,12 +621,50 @@ class NavierStokesAssembly(GPUSimulationDevice):
         self.set_tolerance(tol)
         self.set_solver(solver, inner_tolerance)
         big = mesh.n_nodes > 200_000
-        un, gu, gv, pn, gp = _bc_fast(mesh) if big else bc_occurrences(mesh)
+        timed = any(uses_time(e) for _, ue, ve in mesh.u_dirichlet for e in (ue, ve)) or \
+            any(uses_time(pe) for _, pe in mesh.p_dirichlet)
+        un, gu, gv, pn, gp = bc_occurrences(mesh, 0.0) if timed else _bc_fast(mesh) if big else bc_occurrences(mesh)
         self._check(library().nsf_sim_setup(
             self._h, mesh.n_nodes, np.ascontiguousarray(mesh.nodes, np.float32).reshape(-1), mesh.n_elements,
             np.ascontiguousarray(mesh.elements, np.int32).reshape(-1), mesh.n_pressure, len(un), un, gu, gv,
             len(pn), pn, gp, self.viscosity, self.dt))
         self.nv, self.np_ = mesh.n_nodes, mesh.n_pressure
+        if timed:
+            self.set_bc_expressions(0.0)
+
+    def set_bc_expressions(self, t0: float = 0.0):
+        """Evaluate the mesh's Dirichlet expressions on the device at every step, at the time the step ends
+        (t0 + k dt for step k), so that they may use the variable t; imposes the data at t0 on the resident velocity
+        (nsf_sim_set_bc_expressions).  Called by the constructor when an expression uses t."""
+        exprs, index = [], {}
+
+        def idx(e):
+            if e not in index:
+                index[e] = len(exprs)
+                exprs.append(e)
+            return index[e]
+
+        u, v, p = [], [], []
+        for nodes, ue, ve in self.mesh.u_dirichlet:
+            for _ in np.asarray(nodes):
+                u.append(idx(ue))
+                v.append(idx(ve))
+        for nodes, pe in self.mesh.p_dirichlet:
+            for _ in np.asarray(nodes):
+                p.append(idx(pe))
+        if not exprs:
+            exprs.append("0")
+        arr = (ctypes.c_char_p * len(exprs))(*[e.encode() for e in exprs])
+        u, v, p = (np.ascontiguousarray(a, np.int32) for a in (u, v, p))
+        self._check(library().nsf_sim_set_bc_expressions(self._h, len(exprs), ctypes.cast(arr, _v),
+                                                         u.ctypes.data_as(_v), v.ctypes.data_as(_v),
+                                                         p.ctypes.data_as(_v), float(t0)))
+
+    def time(self) -> float:
+        """Simulated time of the resident fields (nsf_sim_time)."""
+        t = _d()
+        self._check(library().nsf_sim_time(self._h, ctypes.byref(t)))
+        return t.value
 
     @classmethod
     def init(cls, scene_path: str, **kw):

@@ -21,7 +21,7 @@ CLI = os.path.join(PKG, "bin", "nsfem")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
-CU_SOURCES = ["nsf_cg.cu", "nsf_cg_multi.cu", "nsf_sparse.cu", "nsf_locate.cu", "nsf_assembly.cu", "nsf_api.cu", "nsf_noalloc.cu",
+CU_SOURCES = ["nsf_cg.cu", "nsf_cg_multi.cu", "nsf_bc.cu", "nsf_sparse.cu", "nsf_locate.cu", "nsf_assembly.cu", "nsf_api.cu", "nsf_noalloc.cu",
               "nsf_step.cu", "nsf_precond.cu", "nsf_tc_gemm.cu", "nsf_learn.cu"]
 HOST_SOURCES = ["host/json.cpp", "host/expression.cpp", "host/scene.cpp", "host/nsfem_main.cpp"]
 LIB_HOST_SOURCES = ["host/expression.cpp"]

@@ -1,5 +1,6 @@
 #include "expression.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
@@ -141,7 +142,67 @@ double eval(const Expression::Node& n, const std::map<char, double>& vars) {
     return 0;
 }
 
+// Post-order walk: operands before their operator.  Returns the stack depth the subtree needs.
+int emit(const Expression::Node& n, std::vector<int>& ops, std::vector<double>& consts) {
+    using K = Expression::Node;
+    auto push = [&](int op, double c = 0.0) { ops.push_back(op); consts.push_back(c); };
+    switch (n.kind) {
+        case K::Num: push(kOpConst, n.value); return 1;
+        case K::Var:
+            if (n.var == 'x') push(kOpX);
+            else if (n.var == 'y') push(kOpY);
+            else if (n.var == 't') push(kOpT);
+            else throw std::runtime_error(std::string("Missing variable: ") + n.var);
+            return 1;
+        case K::Neg: case K::Sin: case K::Cos: {
+            const int d = emit(*n.a, ops, consts);
+            push(n.kind == K::Neg ? kOpNeg : n.kind == K::Sin ? kOpSin : kOpCos);
+            return d;
+        }
+        default: {
+            const int da = emit(*n.a, ops, consts);
+            const int db = emit(*n.b, ops, consts);
+            const int op = n.kind == K::Add ? kOpAdd : n.kind == K::Sub ? kOpSub : n.kind == K::Mul ? kOpMul
+                         : n.kind == K::Div ? kOpDiv : kOpPow;
+            push(op);
+            return std::max(da, db + 1);
+        }
+    }
+}
+
 }  // namespace
+
+double run_program(const std::vector<int>& ops, const std::vector<double>& consts, double x, double y, double t) {
+    std::vector<double> st;
+    st.reserve(kBcMaxStack);
+    for (size_t i = 0; i < ops.size(); ++i) {
+        const int op = ops[i];
+        if (op <= kOpT) {
+            st.push_back(op == kOpConst ? consts[i] : op == kOpX ? x : op == kOpY ? y : t);
+            continue;
+        }
+        if (op == kOpNeg || op == kOpSin || op == kOpCos) {
+            double& a = st.back();
+            a = op == kOpNeg ? -a : op == kOpSin ? std::sin(a) : std::cos(a);
+            continue;
+        }
+        const double b = st.back();
+        st.pop_back();
+        double& a = st.back();
+        switch (op) {
+            case kOpAdd: a = a + b; break;
+            case kOpSub: a = a - b; break;
+            case kOpMul: a = a * b; break;
+            case kOpDiv: a = a / b; break;
+            default: a = std::pow(a, b); break;
+        }
+    }
+    return st.empty() ? 0.0 : st.front();
+}
+
+int Expression::compile(std::vector<int>& ops, std::vector<double>& consts) const {
+    return emit(*root_, ops, consts);
+}
 
 Expression::Expression(const std::string& text) : text_(text) {
     const std::vector<Tok> toks = tokenize(text);

@@ -126,7 +126,16 @@ int main(int argc, char** argv) {
             firstStep = nsfhost::read_solution(args["resume"], scene.nNodes, scene.nPressure, uv, p) + 1;
             if ((st = nsf_sim_set_fields(h, uv.data(), p.data())) != NSF_OK) return fail(st);
             printf("Resuming after time step %d\n", firstStep - 1);
-        } else if (!outPath.empty()) {
+        }
+        if (scene.timeDependent) {
+            // Dirichlet data that use t: evaluated on the device at the end time of every step
+            std::vector<const char*> ex;
+            for (const auto& e : scene.expressions) ex.push_back(e.c_str());
+            if ((st = nsf_sim_set_bc_expressions(h, (int)ex.size(), ex.data(), scene.uExpr.data(), scene.vExpr.data(),
+                                                 scene.pExpr.data(), (firstStep - 1) * scene.dt)) != NSF_OK)
+                return fail(st);
+        }
+        if (!args.count("resume") && !outPath.empty()) {
             if ((st = nsf_sim_get_fields(h, uv.data(), p.data())) != NSF_OK) return fail(st);
             nsfhost::write_solution(outPath, 0, scene.nNodes, scene.nPressure, uv.data(), p.data());
         }

@@ -60,28 +60,47 @@ void load_mesh(const std::string& meshPath, Scene& s) {
         for (int k = 0; k < 6; ++k) s.elements[6 * (size_t)e + k] = (int)els[e][k].num;
     }
     const Json& ud = j["uDirichlet"];
+    const Json& pd = j["pDirichlet"];
+    // an expression that uses t makes the data time-dependent: evaluated here at t = 0, on the device per step
+    auto index = [&](const std::string& e) {
+        for (size_t i = 0; i < s.expressions.size(); ++i)
+            if (s.expressions[i] == e) return (int)i;
+        s.expressions.push_back(e);
+        if (e.find('t') != std::string::npos) s.timeDependent = true;
+        return (int)s.expressions.size() - 1;
+    };
+    auto vars_at = [&](int node) {
+        std::map<char, double> v{{'x', (double)s.xy[2 * node]}, {'y', (double)s.xy[2 * node + 1]}};
+        if (s.timeDependent) v['t'] = 0.0;
+        return v;
+    };
+    for (size_t g = 0; g < ud.size(); ++g) index(ud[g]["u"].str), index(ud[g]["v"].str);
+    for (size_t g = 0; g < pd.size(); ++g) index(pd[g]["p"].str);
     for (size_t g = 0; g < ud.size(); ++g) {
         const Expression u(ud[g]["u"].str), v(ud[g]["v"].str);
+        const int iu = index(ud[g]["u"].str), iv = index(ud[g]["v"].str);
         const Json& nn = ud[g]["nodes"];
         for (size_t k = 0; k < nn.size(); ++k) {
             const int node = (int)nn[k].num;
             if (node < 0 || node >= s.nNodes) throw std::runtime_error("velocity Dirichlet node out of range");
-            const std::map<char, double> vars{{'x', (double)s.xy[2 * node]}, {'y', (double)s.xy[2 * node + 1]}};
+            const auto vars = vars_at(node);
             s.uNodes.push_back(node);
             s.gu.push_back(u.evaluate(vars));
             s.gv.push_back(v.evaluate(vars));
+            s.uExpr.push_back(iu);
+            s.vExpr.push_back(iv);
         }
     }
-    const Json& pd = j["pDirichlet"];
     for (size_t g = 0; g < pd.size(); ++g) {
         const Expression p(pd[g]["p"].str);
+        const int ip = index(pd[g]["p"].str);
         const Json& nn = pd[g]["nodes"];
         for (size_t k = 0; k < nn.size(); ++k) {
             const int node = (int)nn[k].num;
             if (node < 0 || node >= s.nPressure) throw std::runtime_error("pressure Dirichlet node out of range");
-            const std::map<char, double> vars{{'x', (double)s.xy[2 * node]}, {'y', (double)s.xy[2 * node + 1]}};
             s.pNodes.push_back(node);
-            s.gp.push_back(p.evaluate(vars));
+            s.gp.push_back(p.evaluate(vars_at(node)));
+            s.pExpr.push_back(ip);
         }
     }
 }

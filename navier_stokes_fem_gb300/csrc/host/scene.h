@@ -17,9 +17,15 @@ struct Scene {
     int nNodes = 0, nElements = 0, nPressure = 0;
     std::vector<float> xy;
     std::vector<int> elements;
-    // Dirichlet data per listed occurrence, in file order, evaluated at the node (variables x, y)
+    // Dirichlet data per listed occurrence, in file order, evaluated at the node (variables x, y; and t = 0 when
+    // an expression uses t)
     std::vector<int> uNodes, pNodes;
     std::vector<double> gu, gv, gp;
+    // the groups' expression strings and, per occurrence, the index of its u, v and p expression (for
+    // nsf_sim_set_bc_expressions when the data depend on time)
+    std::vector<std::string> expressions;
+    std::vector<int> uExpr, vExpr, pExpr;
+    bool timeDependent = false;
 
     int step_count() const;
 };

@@ -45,6 +45,12 @@ void setup_instance(MeshDev& m, SimState& S, Csr* mats, cudaStream_t s, int nNod
     S.ready = false;
     S.viscosity = viscosity;
     S.dt = dt;
+    S.t0 = 0;
+    S.steps = 0;
+    S.bcTimeDependent = false;
+    S.nBcNodeV = S.nBcNodeP = 0;
+    S.hOccV.assign(velocityBCNodes, velocityBCNodes + nVelocityBC);
+    S.hOccP.assign(pressureBCNodes, pressureBCNodes + nPressureBC);
     const int Nv = nNodes, P = nPressure;
     // Dirichlet data: mask, imposed value (last listed occurrence) and lift weight (sum over occurrences,
     // because the reference subtracts the lift once per listed occurrence, include/assembly.h:505-523)
@@ -261,6 +267,13 @@ bool use_pipelined_cg(const nsf_device* h, const Csr& S) {
     return S.rows < NSF_CG_PIPELINED_MAX_ROWS;
 }
 
+// The reduced (Schur complement) iteration of the split mixed PCG: two colours, a SELL copy and the 1024-thread
+// inner grid.
+bool use_reduced_pcg(const nsf_device* h, const Csr& S, const FactorView& f) {
+    if (h->pcgForm != NSF_PCG_FORM_REDUCED) return false;
+    return f.colours == 2 && S.sellStart.get() && h->ws.gridInner1024 > 0 && f.aDiag && f.aInv32;
+}
+
 // Launch one persistent solve; returns the index of its CgInfo slot.
 int launch_solve(nsf_device* h, int slot, int mode, const double* b, const double* x0, double* x, int maxIt,
                  double tol, const CgArgs* fused) {
@@ -338,8 +351,10 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
         NSF_CUDA(cudaEventRecord(e0, h->stream));
     }
     const bool wide = S.maxWidth > kSellChunk;
-    if (mode == NSF_SOLVER_PCG_MIXED && !wide)
+    if (mode == NSF_SOLVER_PCG_MIXED && !wide) {
+        a.f.reduced = use_reduced_pcg(h, S, a.f) ? 1 : 0;
         h->innerForm[slot] = pcg_mixed_split_launch(ws, a, h->stream);
+    }
     else if (mode == NSF_SOLVER_MIXED && wide)
         cg_mixed_split_launch(ws, a, h->stream);
     else if (mode == NSF_SOLVER_FP64 && h->cgForm == NSF_CG_FORM_MULTI_KERNEL)
@@ -415,6 +430,9 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     cudaStream_t s = h->stream;
     double* uv = S.uv.get();
     double* tmp = S.tmp.get();
+    // time-dependent Dirichlet data at the time this step ends
+    ++S.steps;
+    if (S.bcTimeDependent) bc_update_launch(S, m, h->mats, S.t0 + (double)S.steps * S.dt, s);
     // advection (include/assembly.h:1519-1524)
     advect_launch(m, S.dt, uv, uv + Nv, tmp, tmp + Nv, s);
     // diffusion solves, u then v (include/assembly.h:1529-1545, 489-558): rhs = M u_adv - lift, g on Dirichlet rows
@@ -796,6 +814,23 @@ int nsf_sim_get_fields(nsf_device* h, double* uv, double* p) {
     NSF_END(h)
 }
 
+int nsf_sim_set_bc_expressions(nsf_device* h, int nExpressions, const char* const* expressions, const int* velocityU,
+                               const int* velocityV, const int* pressure, double t0) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    bc_set_programs(h->sim, h->mesh, h->mats, nExpressions, expressions, velocityU, velocityV, pressure, t0,
+                    h->stream);
+    NSF_END(h)
+}
+
+int nsf_sim_time(nsf_device* h, double* t) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    if (!t) throw bad_arg("null output");
+    *t = h->sim.t0 + (double)h->sim.steps * h->sim.dt;
+    NSF_END(h)
+}
+
 int nsf_sim_step(nsf_device* h, int nsteps, int* iterations) {
     NSF_BEGIN(h)
     run_steps(h, nsteps, iterations);
@@ -962,6 +997,13 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
         for (int slot : {NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS}) prepare_matrix(h->mats[slot], true, h->stream);
         NSF_CUDA(cudaStreamSynchronize(h->stream));
     }
+    NSF_END(h)
+}
+
+int nsf_set_pcg_form(nsf_device* h, int form) {
+    NSF_BEGIN(h)
+    if (form < NSF_PCG_FORM_AUTO || form > NSF_PCG_FORM_REDUCED) throw bad_arg("unknown PCG form");
+    h->pcgForm = form;
     NSF_END(h)
 }
 
@@ -1194,6 +1236,26 @@ int nsf_flush_l2(nsf_device* h, size_t bytes) {
 }  // extern "C"
 
 #include "host/expression.h"
+
+extern "C" int nsf_eval_expression_t(const char* expression, double x, double y, double t, double* value,
+                                     char* message, size_t messageBytes) {
+    try {
+        if (!expression || !value) throw std::runtime_error("null argument");
+        // through the compiled program that nsf_sim_set_bc_expressions hands to the device
+        std::vector<int> ops;
+        std::vector<double> consts;
+        nsfhost::Expression(expression).compile(ops, consts);
+        *value = nsfhost::run_program(ops, consts, x, y, t);
+        if (message && messageBytes) message[0] = '\0';
+        return NSF_OK;
+    } catch (const std::exception& err) {
+        if (message && messageBytes) {
+            strncpy(message, err.what(), messageBytes - 1);
+            message[messageBytes - 1] = '\0';
+        }
+        return NSF_ERR_BAD_ARG;
+    }
+}
 
 extern "C" int nsf_eval_expression(const char* expression, double x, double y, double* value, char* message,
                                    size_t messageBytes) {

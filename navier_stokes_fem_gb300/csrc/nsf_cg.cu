@@ -109,6 +109,15 @@ __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_ct
     team_pcg_mixed_inner<C16, true, false, H16>(t, a, nullptr, smem, nullptr);
 }
 
+// The reduced (Schur complement) iterations of a two-colour system in the 1024-thread form (a.f.reduced).
+template <bool C16>
+__global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_reduced(CgArgs a) {
+    __shared__ double smem[kSmemSlots];
+    if (!a.sellStart || a.f.colours != 2 || !a.f.reduced) return;   // (the host never launches it otherwise)
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_mixed_inner_reduced<C16>(t, a, smem);
+}
+
 // The same 1024-thread form with the row state only its CTA reads (the FP32 correction, and r and q of its colour-1
 // rows) in dynamic shared memory for the whole launch: two colours only, and only where that state fits.
 template <bool C16, bool H16 = false>
@@ -359,6 +368,14 @@ void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
 }
 
 int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
+    if (a.f.reduced) {   // the reduced iterations: two colours and a SELL copy, checked by the caller
+        const bool c16 = a.sellCol16 != nullptr;
+        split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes,
+                     c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true>
+                         : (const void*)pcg_mixed_inner_kernel_reduced<false>,
+                     nullptr, s);
+        return 3;
+    }
     // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;
     const bool h16 = c16 && a.f.loVal16 && a.f.upVal16;   // FP16 factor values (16-bit columns only)

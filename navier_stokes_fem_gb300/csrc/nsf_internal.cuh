@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/nsfem_gb300.h"
+#include "host/expression.h"
 
 namespace nsf {
 
@@ -131,6 +132,11 @@ struct FactorView {
     const int* upColBase = nullptr;
     const double* dinv = nullptr;             // 1 / L_ii per permuted row (1 on padding rows)
     const float* dinv32 = nullptr;
+    // the reduced (Schur complement) iteration of a two-colour system: the matrix's own diagonal per permuted row,
+    // FP64, and 1 / a_ii in FP32; reduced = 1 selects that iteration in the split mixed PCG
+    const double* aDiag = nullptr;
+    const float* aInv32 = nullptr;
+    int reduced = 0;
     double* w = nullptr;                      // work vector: forward-sweep result, then M^-1 r (in place)
     float* w32 = nullptr;
     double* xp = nullptr;                     // the iterate and right-hand side in permuted order
@@ -162,6 +168,8 @@ struct Factor {
     int loMaxW = 0, upMaxW = 0;
     DevBuf<double> loVal, upVal, dinv;
     DevBuf<float> loVal32, upVal32, dinv32;
+    DevBuf<double> aDiag;                      // diagonal of Ap per permuted row (the reduced iteration)
+    DevBuf<float> aInv32;                      // 1 / aDiag in FP32
     DevBuf<__half> loVal16, upVal16;           // FP16 copies of the values (see FactorView)
     DevBuf<int> range16;                       // set by factor_fill when a value does not fit FP16's normal range
     bool has16 = false;
@@ -367,9 +375,28 @@ void advect_launch(const MeshDev& m, double dt, const double* u, const double* v
 void advect_f32_launch(const MeshDev& m, float dt, const float* u, const float* v, float* uo, float* vo,
                        cudaStream_t s);
 
+// A Dirichlet expression compiled for the device (nsfhost::BcOp codes; c holds the constants of kOpConst).
+struct BcProgram {
+    int n;
+    int op[nsfhost::kBcMaxOps];
+    double c[nsfhost::kBcMaxOps];
+};
+
 struct SimState {
     bool ready = false;
     double viscosity = 0, dt = 0;
+    // simulated time of the resident fields: t0 + steps * dt, steps counted from the last nsf_sim_setup or
+    // nsf_sim_set_bc_expressions
+    double t0 = 0;
+    long long steps = 0;
+    std::vector<int> hOccV, hOccP;   // the Dirichlet occurrences (node per listed entry) given at setup
+    // time-dependent Dirichlet data: programs evaluated on the device at the start of every step
+    bool bcTimeDependent = false;
+    DevBuf<BcProgram> bcProg;
+    DevBuf<int> bcNodeV, bcOccStartV, bcProgU, bcProgV;   // distinct velocity Dirichlet nodes, their occurrences
+    DevBuf<int> bcNodeP, bcOccStartP, bcProgP;
+    int nBcNodeV = 0, nBcNodeP = 0;
+    DevBuf<double> gSumV[2], gSumP;   // per node, the sum of its occurrences' values (the lift's weights)
     DevBuf<double> uv, tmp, p, rhsV, rhsP;
     DevBuf<double> liftV[2], liftP;
     DevBuf<unsigned char> bcV, bcP;
@@ -378,6 +405,12 @@ struct SimState {
     std::vector<unsigned char> hbcV, hbcP;
     int nColours = 0;
 };
+
+// Time-dependent Dirichlet data (nsf_bc.cu): compiles the expressions, stores the programs and evaluates them at
+// S.t0; bc_update_launch re-evaluates values, lift weights and lifts at time t on the stream.
+void bc_set_programs(SimState& S, const MeshDev& m, Csr* mats, int nExpressions, const char* const* expressions,
+                     const int* velocityU, const int* velocityV, const int* pressure, double t0, cudaStream_t s);
+void bc_update_launch(SimState& S, const MeshDev& m, Csr* mats, double t, cudaStream_t s);
 
 // One mesh instance of the batched form: its mesh and tree, matrices, fields and CG workspace.
 struct Instance {
@@ -425,6 +458,7 @@ struct nsf_device {
     double innerTol = 0.1;   // mixed precision: FP32 residual reduction between FP64 true residuals
     long long timeoutNs = 2000000000LL;
     int solverMode = NSF_SOLVER_FP64;
+    int pcgForm = NSF_PCG_FORM_AUTO;   // mixed PCG of a two-colour system: full or reduced iteration
     int cgForm = NSF_CG_FORM_AUTO;   // plain FP64 CG: three barriers per iteration or pipelined (one)
     bool mixedOff[NSF_SLOT_COUNT] = {};   // systems whose mixed solve stalled once: solved in FP64 from then on
     nsf::Factor factors[NSF_SLOT_COUNT];  // preconditioners

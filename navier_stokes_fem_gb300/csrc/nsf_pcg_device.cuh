@@ -721,6 +721,235 @@ static __device__ bool pcg_mixed_inner_fused(Team& t, const CgArgs& a, double* s
     return true;
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Reduced (Schur complement) form of the split mixed PCG, two colours.  With two colours the colour-0 block A_00
+// of the permuted matrix is diagonal, so the colour-0 unknowns can be eliminated exactly:
+//     S x_1 = b_1 - A_10 A_00^-1 b_0,   S = A_11 - A_10 A_00^-1 A_01,   x_0 = A_00^-1 (b_0 - A_01 x_1).
+// The iteration is PCG on S with the factor's colour-1 diagonal as preconditioner, z_1 = r_1 / L_11^2, written in
+// the full system's vectors: every refresh projects x_0 (one exact Jacobi step on the colour-0 rows), so r_0 = 0;
+// the search direction's colour-0 part is u_0 = -A_00^-1 A_01 p_1, which makes q_0 = (A p)_0 = 0, and
+// q_1 = A_10 u_0 + A_11 p_1 = S p_1.  For IC(0) (L_00^2 = A_00, L_10 = A_10 L_00^-1, L_11^2 = diag S) these are the
+// iterates of the full PCG: its z_0 = -A_00^-1 A_01 z_1 when r_0 = 0.  An iteration reads each matrix row once,
+// the colour-0 rows for u_0 and the colour-1 rows for q_1, and neither factor part: about half of the full
+// iteration's matrix entries and gathers, with the same three grid barriers.
+//   H1, colour-0 rows:  u_i = -(1/a_ii) sum_j a_ij (z_j + beta p_j)            (stored as p_i)
+//   H2, colour-1 rows:  p_i = z_i + beta p_i,  q_i = sum_j a_ij (u_j - p_i) + rowsum_i p_i,  partial p.q
+//   U,  colour-1 rows:  d_i += alpha p_i,  r_i -= alpha q_i,  z_i = r_i / L_ii^2,  partials r.r and r.z
+// (u_i is a weighted mean of its neighbours' p_j on a stiffness matrix, so its FP32 sum does not cancel; q_1 is
+// taken in the difference form of the other mixed products.)
+template <bool Wide = false>
+static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, double* stage, double* smem, PcgLoop& L,
+                                                 int& where) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x, c1 = F.colourRow[1];
+    int rb, re;
+    team_rows(a.n, t, rb, re);
+    const double* b = a.b;   // permuted right-hand side (permute_in); x0 == x
+    double* x = a.x;
+    float* w = F.w32;
+    float* pprev = L.flip ? a.p32b : a.p32a;
+    float* r32 = L.rflip ? a.r32b : a.r32;
+    const double sc = L.scale;
+    if (!L.first) {   // fold the FP32 correction into x (colour-1 rows carry one; colour-0 rows hold zero)
+        const double inv = 1.0 / sc;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) a.x[i] += (double)a.d32[i] * inv;
+        if (L.innerBreakdown) L.resetP = 1;
+    } else if (x != a.x0) {
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) x[i] = a.x0[i];
+    }
+    if (!t.barrier(where++)) return false;
+    // x_0 = A_00^-1 (b_0 - A_01 x_1): x_i += (b_i - (A x)_i) / a_ii on the own colour-0 rows (which couple to
+    // colour-1 unknowns and their own diagonal only)
+    const int pe = min(re, c1);
+    if (rb < pe)
+        matrix_product<double, double, false, kResidU<Wide>, Wide>(
+            a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, pe, stage, [&](int c) { return x[c]; },
+            [&](int row, double acc, double xi) { x[row] = xi + (b[row] - acc) / F.aDiag[row]; });
+    if (!t.barrier(where++)) return false;
+    // true residual r = b - A64 x (r_0 = 0 up to rounding), r32 = (float) (scale r), d32 = 0, z_1 = r_1 / L_11^2
+    const bool resetP = L.resetP != 0;
+    double rrp = 0, bbp = 0;
+    DotAcc<float> rzp;
+    matrix_product<double, double, false, kResidU<Wide>, Wide>(
+        a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return x[c]; },
+        [&](int row, double acc, double) {
+            const double bi = b[row];
+            const double ri = bi - acc;
+            const float rf = (float)(ri * sc);
+            r32[row] = rf;
+            a.d32[row] = 0.0f;
+            if (resetP) pprev[row] = 0.0f;   // restart: p = z
+            rrp = fma(ri, ri, rrp);
+            bbp = fma(bi, bi, bbp);
+            if (row >= c1) {
+                const float d = F.dinv32[row];
+                const float z = (rf * d) * d;
+                w[row] = z;
+                rzp.add(rf, z);
+            }
+        });
+    rrp = block_sum(rrp, smem);
+    bbp = block_sum(bbp, smem);
+    const double rzb = rzp.block(smem);
+    if (threadIdx.x == 0) {
+        a.partials[2 * G + t.rank] = rrp;
+        a.partials[3 * G + t.rank] = bbp;
+        a.partials[4 * G + t.rank] = rzb;
+    }
+    if (!t.barrier(where++)) return false;
+    L.rr64 = grid_sum(a.partials + 2 * G, G, smem);
+    if (L.first) {
+        L.bb = grid_sum(a.partials + 3 * G, G, smem);
+        L.target = L.bb > 0 ? a.tol2 * L.bb : a.tol2 * L.rr64;
+    }
+    double rzT = grid_sum(a.partials + 4 * G, G, smem);
+    L.state = kLoopDone;
+    if (!(L.rr64 == L.rr64) || isinf(L.rr64)) { L.status = NSF_ERR_BREAKDOWN; return true; }
+    if (L.rr64 <= L.target) { L.status = NSF_OK; return true; }
+    if (L.it >= a.maxIt || L.refresh >= a.maxOuter) return true;
+    if (L.refresh > 0 && L.rr64 > 0.81 * L.rrBest) {   // stagnation guard (see team_cg_mixed)
+        if (++L.stalls >= 3) return true;
+    } else {
+        L.stalls = 0;
+    }
+    L.rrBest = fmin(L.rrBest, L.rr64);
+    const double f = rescale_factor(L.rr64 * sc * sc / a.n);
+    if (f != 1.0) {   // own rows of r32, z_1 and the previous direction (read by the next launch only)
+        const float ff = (float)f;
+        for (int i = rb + (int)threadIdx.x; i < re; i += bs) {
+            r32[i] *= ff;
+            pprev[i] *= ff;
+            if (i >= c1) w[i] *= ff;
+        }
+        rzT *= f * f;    // (products of powers of two are exact)
+        L.rz *= f * f;   // the previous cycle's r.z, for beta
+        L.scale = sc * f;
+    }
+    if (!(rzT > 0.0) || isinf(rzT)) { L.status = NSF_ERR_BREAKDOWN; return true; }
+    const bool drifted = L.refresh > 0 && L.rr64 > 0.25 * L.rrCycle;   // (see pcg_mixed_refresh)
+    L.beta = (L.resetP || drifted) ? 0.0 : rzT / L.rz;
+    L.resetP = 0;
+    L.rz = rzT;
+    L.rrCycle = L.rr64;
+    L.rrRef = L.rr64;
+    L.itRef = L.it;
+    ++L.refresh;
+    L.first = 0;
+    L.state = kLoopInner;
+    return true;
+}
+
+// The inner iterations of the reduced form (H1, H2, U above); the residual is updated in place, since no phase
+// gathers it.  (C16: the 16-bit column copy of the matrix, whose diagonal entries are padding.)
+template <bool C16 = false>
+static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem, PcgLoop& L, int& where) {
+    const FactorView& F = a.f;
+    const int G = t.size, bs = blockDim.x, c1 = F.colourRow[1];
+    float* w = F.w32;
+    const float* dinv = F.dinv32;
+    const float* ainv = F.aInv32;
+    float* r = L.rflip ? a.r32b : a.r32;
+    int a0, a1, b0, b1;   // own colour-0 rows [a0, a1) and colour-1 rows [b0, b1)
+    team_block(F.colourRow[0], F.colourRow[1], t, a0, a1);
+    team_block(F.colourRow[1], F.colourRow[2], t, b0, b1);
+    using TC = std::conditional_t<C16, unsigned short, int>;
+    const TC* col;
+    if constexpr (C16) col = a.sellCol16;
+    else col = a.sellCol;
+    L.innerBreakdown = 0;
+    const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
+    const double invScale = 1.0 / L.scale;
+    float betaf = (float)L.beta;
+    while (L.it < a.maxIt) {
+        const float* pp = L.flip ? a.p32b : a.p32a;
+        float* pc = L.flip ? a.p32a : a.p32b;
+        // H1: u_0 (the colour-0 columns of a colour-0 row are its own diagonal only: excluded)
+        auto h1 = [&](auto U) {
+            sell_rows<float, float, false, 1, decltype(U)::value, TC>(
+                a.sellStart, col, a.sellVal32, a0, a1,
+                [&](int j) { return j >= c1 ? fmaf(betaf, pp[j], w[j]) : 0.0f; }, [&](int i) { return ainv[i]; },
+                [&](int i, float acc, float ai) { pc[i] = -acc * ai; }, a.sellColBase);
+        };
+        if (a.sellMaxW <= 5) h1(std::integral_constant<int, 5>{});
+        else h1(std::integral_constant<int, 6>{});
+        if (!t.barrier(where++)) return false;
+        // H2: p_1 and q_1 = S p_1, p.q
+        float pqHi = 0.f, pqLo = 0.f;
+        auto g2 = [&](int c) { return c >= c1 ? fmaf(betaf, pp[c], w[c]) : pc[c]; };
+        auto e2 = [&](int row, float acc, float pi) {
+            pc[row] = pi;
+            a.q32[row] = acc;
+            df_acc(pqHi, pqLo, pi, acc);
+        };
+        if (a.sellMaxW <= 5) product32<false, 5, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
+        else product32<false, 6, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
+        const double pq = block_sum_df(pqHi, pqLo, smem);
+        if (threadIdx.x == 0) a.partials[t.rank] = pq;
+        if (!t.barrier(where++)) return false;
+        {
+            const double pqs = grid_sum0(a.partials, G);
+            if (threadIdx.x == 0) {
+                const bool bad = !(pqs > 0.0) || isinf(pqs);
+                decision_put(smem, bad ? 0.f : (float)(L.rz / pqs), bad);
+            }
+        }
+        const Decision da = decision_get(smem);
+        if (da.code) { L.innerBreakdown = 1; break; }
+        const float alphaf = da.v;
+        const bool fold = fold_iteration(L);
+        // U: colour-1 rows
+        float rrHi = 0.f, rrLo = 0.f;
+        DotAcc<float> rzn;
+        for (int i0 = b0 + (int)threadIdx.x; i0 < b1; i0 += kRowsLean * bs) {
+            float pi[kRowsLean], qi[kRowsLean], di[kRowsLean], ri[kRowsLean], vi[kRowsLean];
+#pragma unroll
+            for (int u = 0; u < kRowsLean; ++u) {
+                const int i = i0 + u * bs;
+                if (i < b1) {
+                    pi[u] = pc[i];
+                    qi[u] = a.q32[i];
+                    di[u] = a.d32[i];
+                    ri[u] = r[i];
+                    vi[u] = dinv[i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRowsLean; ++u) {
+                const int i = i0 + u * bs;
+                if (i < b1) {
+                    a.d32[i] = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
+                    const float rn = fmaf(-alphaf, qi[u], ri[u]);
+                    r[i] = rn;
+                    df_acc(rrHi, rrLo, rn, rn);
+                    const float z = (rn * vi[u]) * vi[u];
+                    w[i] = z;
+                    rzn.add(rn, z);
+                }
+            }
+        }
+        const double rrn = block_sum_df(rrHi, rrLo, smem);
+        const double rzb = rzn.block(smem);
+        if (threadIdx.x == 0) {
+            a.partials[G + t.rank] = rrn;
+            a.partials[4 * G + t.rank] = rzb;
+        }
+        if (!t.barrier(where++)) return false;
+        const double rrs = grid_sum(a.partials + G, G, smem);
+        const double rzs = grid_sum(a.partials + 4 * G, G, smem);
+        ++L.it;
+        L.flip ^= 1;
+        if (!(rrs == rrs) || isinf(rrs)) { L.innerBreakdown = 1; break; }
+        if (rrs <= rrStop) break;   // time for a true residual
+        if (L.it - L.itRef >= kMaxInnerBetweenRefresh) break;
+        if (!(rzs > 0.0) || isinf(rzs)) { L.innerBreakdown = 1; break; }
+        L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
+        L.rz = rzs;
+        betaf = (float)L.beta;
+    }
+    L.state = kLoopRefresh;
+    return true;
+}
+
 // The end of a mixed PCG solve (state kLoopDone): when it stopped short of the tolerance with budget left, plain
 // FP64 CG from the current iterate with the plain method's own budget; then the solve's info.
 template <bool Wide = false>
@@ -810,7 +1039,8 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
     } else {
         L = *a.loop;
     }
-    if (!pcg_mixed_refresh<false>(t, a, stage, smem, ring, L, where)) {
+    if (!(a.f.reduced ? pcg_mixed_refresh_reduced<false>(t, a, stage, smem, L, where)
+                      : pcg_mixed_refresh<false>(t, a, stage, smem, ring, L, where))) {
         write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, L.refresh, L.rr64, L.bb);
         L.state = kLoopDone;
         pcg_loop_store(t, a, L);
@@ -821,6 +1051,34 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
         if (st != NSF_ERR_BARRIER_TIMEOUT) permute_out(t, a);
     }
     pcg_loop_store(t, a, L);
+}
+
+// The reduced form's inner launch (two colours, a SELL copy and a.f.reduced; see pcg_mixed_inner_reduced).
+template <bool C16 = false>
+static __device__ void team_pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem) {
+    int where = 400;
+    const PcgLoop& G = *a.loop;
+    PcgLoop L;
+    L.rz = G.rz;
+    L.beta = G.beta;
+    L.rrRef = G.rrRef;
+    L.target = G.target;
+    L.scale = G.scale;
+    L.it = G.it;
+    L.itRef = G.itRef;
+    L.flip = G.flip;
+    L.rflip = G.rflip;
+    const bool ok = pcg_mixed_inner_reduced<C16>(t, a, smem, L, where);
+    if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
+    if (t.rank == 0 && threadIdx.x == 0) {
+        a.loop->rz = L.rz;
+        a.loop->beta = L.beta;
+        a.loop->it = L.it;
+        a.loop->flip = L.flip;
+        a.loop->rflip = L.rflip;
+        a.loop->innerBreakdown = L.innerBreakdown;
+        a.loop->state = ok ? L.state : kLoopDone;
+    }
 }
 
 // (FusedOnly: the caller guarantees two or more colours; the one-colour loop and its CSR staging are left out.

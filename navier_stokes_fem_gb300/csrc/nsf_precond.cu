@@ -70,6 +70,18 @@ __global__ void ap_values_kernel(int64_t nnz, const int* __restrict__ from, cons
     }
 }
 
+// The diagonal of the permuted matrix (1 on padding rows), and its FP32 inverse.
+__global__ void ap_diag_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                               const double* __restrict__ val, double* __restrict__ diag, float* __restrict__ inv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = 0.0;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (col[k] == i) d = val[k];
+    diag[i] = d;
+    inv[i] = d != 0.0 ? (float)(1.0 / d) : 0.0f;
+}
+
 // DSatur colouring of the matrix graph (Brelaz 1979): repeatedly colour the uncoloured row whose neighbours
 // already use the most distinct colours (ties: more neighbours, then the lower row index) with the smallest colour
 // none of them uses.  On the triangulated grids of this solver it finds 3 colours where first-fit in row order
@@ -260,6 +272,11 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s) {
     P.values_changed();
     ap_values_kernel<<<grid_for(P.nnz, 256), 256, 0, s>>>(P.nnz, F.apFrom.get(), A.val.get(), P.val.get());
     NSF_CUDA(cudaGetLastError());
+    F.aDiag.alloc((size_t)np);
+    F.aInv32.alloc((size_t)np);
+    ap_diag_kernel<<<grid_for(np, 256), 256, 0, s>>>(np, P.rowptr.get(), P.col.get(), P.val.get(), F.aDiag.get(),
+                                                     F.aInv32.get());
+    NSF_CUDA(cudaGetLastError());
     count_launch();
     prepare_matrix(P, true, s);
     NSF_CUDA(cudaStreamSynchronize(s));
@@ -433,6 +450,8 @@ FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     }
     v.dinv = F.dinv.get();
     v.dinv32 = F.dinv32.get();
+    v.aDiag = F.aDiag.get();
+    v.aInv32 = F.aInv32.get();
     v.w = ws.w.get();
     v.w32 = ws.w32.get();
     v.xp = ws.xp.get();

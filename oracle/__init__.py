@@ -105,6 +105,7 @@ def lib():
         L.orc_set_fields.argtypes = [_p, _dptr, _dptr]
         L.orc_get_fields.argtypes = [_p, _dptr, _dptr]
         L.orc_set_tolerance.argtypes = [_p, _d]
+        L.orc_set_bc.argtypes = [_p, _dptr, _dptr, _dptr]
         L.orc_point_in_triangle.restype = _i
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
         _u8ptr = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
@@ -252,24 +253,27 @@ def evaluate_expression(expr: str, variables: dict) -> float:
     return float(v)
 
 
-def bc_occurrences(mesh):
+def bc_occurrences(mesh, t=None):
     """Dirichlet data as the reference walks it: every (group, node) occurrence in file order.
 
     Returns (u_nodes int32, gu float64, gv float64, p_nodes int32, gp float64).  Values are the group's
-    expressions evaluated in double at the node's (float) coordinates with variables x and y.
+    expressions evaluated in double at the node's (float) coordinates with variables x and y, and t when given
+    (time-dependent data, which the reference's grammar accepts but its driver never passes).
     """
     un, gu, gv, pn, gp = [], [], [], [], []
     for nodes, ue, ve in mesh.u_dirichlet:
         for nd in nodes:
             x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
+            var = {"x": x, "y": y} if t is None else {"x": x, "y": y, "t": float(t)}
             un.append(int(nd))
-            gu.append(evaluate_expression(ue, {"x": x, "y": y}))
-            gv.append(evaluate_expression(ve, {"x": x, "y": y}))
+            gu.append(evaluate_expression(ue, var))
+            gv.append(evaluate_expression(ve, var))
     for nodes, pe in mesh.p_dirichlet:
         for nd in nodes:
             x, y = float(mesh.nodes[nd, 0]), float(mesh.nodes[nd, 1])
+            var = {"x": x, "y": y} if t is None else {"x": x, "y": y, "t": float(t)}
             pn.append(int(nd))
-            gp.append(evaluate_expression(pe, {"x": x, "y": y}))
+            gp.append(evaluate_expression(pe, var))
     return (np.asarray(un, np.int32), np.asarray(gu, np.float64), np.asarray(gv, np.float64),
             np.asarray(pn, np.int32), np.asarray(gp, np.float64))
 
@@ -281,7 +285,11 @@ class Oracle:
         L = lib()
         self.mesh = mesh
         self.nv, self.np_ = mesh.n_nodes, mesh.n_pressure
-        un, gu, gv, pn, gp = bc_occurrences(mesh)
+        exprs = [e for _, ue, ve in mesh.u_dirichlet for e in (ue, ve)] + [pe for _, pe in mesh.p_dirichlet]
+        # time-dependent Dirichlet data: evaluated at t0 + k dt before step k (t0 = 0: the initial state)
+        self.timed = any("t" in e.replace("Pi", "") for e in exprs)
+        self.t0, self.steps = 0.0, 0
+        un, gu, gv, pn, gp = bc_occurrences(mesh, 0.0 if self.timed else None)
         nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float32).reshape(-1)
         els = np.ascontiguousarray(mesh.elements, dtype=np.int32).reshape(-1)
         self._h = L.orc_create(mesh.n_nodes, nodes, mesh.n_elements, els, mesh.n_pressure, len(un), un, gu, gv,
@@ -354,7 +362,15 @@ class Oracle:
 
     def step(self, n=1):
         iters = np.zeros(5 * n, np.int32)
-        st = lib().orc_step(self._h, int(n), iters)
+        if not self.timed:
+            st = lib().orc_step(self._h, int(n), iters)
+            return st, iters.reshape(n, 5)
+        st = 0
+        for k in range(n):
+            self.steps += 1
+            _, gu, gv, _, gp = bc_occurrences(self.mesh, self.t0 + self.steps * self.dt)
+            lib().orc_set_bc(self._h, gu, gv, gp)
+            st |= lib().orc_step(self._h, 1, iters[5 * k:5 * k + 5])
         return st, iters.reshape(n, 5)
 
     def set_fields(self, uv, p):

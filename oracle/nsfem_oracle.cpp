@@ -414,6 +414,7 @@ struct SolverBase {
     virtual void get_fields(double* uv, double* p) = 0;
     virtual void spmv(int slot, const double* x, double* y) = 0;
     virtual void set_tol(double t) = 0;
+    virtual void set_bc(const double* u, const double* v, const double* p) = 0;
     KDTree tree;
     std::vector<float> xy;
     std::vector<int> el;
@@ -613,6 +614,12 @@ template <typename R> struct Solver : SolverBase {
     }
 
     void set_tol(double t) override { tol = t; }
+    // replaces the Dirichlet values of every listed occurrence (time-dependent data: the caller evaluates them at
+    // each step's time and calls this before the step); the lifts are formed from them inside each step
+    void set_bc(const double* u_, const double* v_, const double* p_) override {
+        for (size_t i = 0; i < gu.size(); ++i) { gu[i] = (R)u_[i]; gv[i] = (R)v_[i]; }
+        for (size_t i = 0; i < gp.size(); ++i) gp[i] = (R)p_[i];
+    }
 
     int solve(int slot, const R* b, const R* x0, R* x, int* it) {
         double rr;
@@ -814,6 +821,7 @@ void orc_tree_stats(void* h, int64_t* nodes, int64_t* leafEntries, int* maxDepth
 void orc_advect(void* h, const double* u, const double* v, double* uo, double* vo) { ((SolverBase*)h)->advect(u, v, uo, vo); }
 int orc_step(void* h, int nsteps, int* iters) { return ((SolverBase*)h)->step(nsteps, iters); }
 void orc_set_tolerance(void* h, double tol) { ((SolverBase*)h)->set_tol(tol); }
+void orc_set_bc(void* h, const double* u, const double* v, const double* p) { ((SolverBase*)h)->set_bc(u, v, p); }
 void orc_set_fields(void* h, const double* uv, const double* p) { ((SolverBase*)h)->set_fields(uv, p); }
 void orc_get_fields(void* h, double* uv, double* p) { ((SolverBase*)h)->get_fields(uv, p); }
 

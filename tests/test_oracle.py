@@ -240,6 +240,42 @@ def test_expression_known_answers(expr, x, y, value):
     assert nsf.evaluate_expression(expr, x, y) == pytest.approx(value, abs=1e-15)
 
 
+TIMED_EXPRESSIONS = ["4*1.5*y*(0.41-y)/(0.41*0.41)*sin(Pi*t/8)", "-x^2^-1+t", "2^-t*cos(x-y*t)/3", "1-t/2*-x",
+                     "E^(t*x)-Pi*-(y)", "(x+y)*(x-y)^2/(1+t)", "sin(cos(t))*-3^2", "0.15*t-x/y/t"]
+
+
+@pytest.mark.parametrize("expr", TIMED_EXPRESSIONS)
+def test_time_dependent_expression_programs(expr):
+    """The postfix program that nsf_sim_set_bc_expressions compiles for the device, run op for op on the host
+    (nsf_eval_expression_t), gives the oracle's tree-walk value bit for bit: precedence, associativity and unary
+    minus survive the compilation."""
+    import navier_stokes_fem_gb300 as nsf
+
+    for x, y, t in [(0.3, 0.2, 0.05), (1.0, 0.37, 2.5), (0.7, 0.1, 1e-3)]:
+        assert nsf.evaluate_expression(expr, x, y, t) == oracle.evaluate_expression(expr, {"x": x, "y": y, "t": t})
+
+
+def test_oracle_time_dependent_stepping_known_answer():
+    """A lid written as "1 + 0*t" goes through the oracle's per-step re-evaluation at t = k dt and must give the
+    constant lid's fields bit for bit (one thread: the oracle's parallel reductions are not ordered); a lid that
+    changes with t must not."""
+    fields = {}
+    prev = oracle.max_threads()
+    oracle.set_threads(1)
+    try:
+        for lid in ("1", "1+0*t", "1+t"):
+            o = oracle.Oracle(M.cavity(8, lid_u=lid), 0.01, 0.05)
+            assert o.timed == ("t" in lid)
+            st, _ = o.step(4)
+            assert st == 0
+            fields[lid] = o.fields()
+            o.close()
+    finally:
+        oracle.set_threads(prev)
+    assert all(np.array_equal(a, b) for a, b in zip(fields["1"], fields["1+0*t"]))
+    assert not np.array_equal(fields["1"][0], fields["1+t"][0])
+
+
 @pytest.mark.parametrize("bad", ["z+1", "(1+2", "sin 3", "1+*", "x$"])
 def test_expression_errors(bad):
     import navier_stokes_fem_gb300 as nsf

@@ -292,7 +292,19 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None):
+def pcg_reduced_bytes(n, nz, its, outer, idx=4):
+    """Minimal DRAM bytes of one reduced (Schur complement) mixed PCG solve of a two-colour system: per iteration
+    every matrix row once (FP32 values + idx-byte columns; the colour-0 rows for u_0, the colour-1 rows for q_1)
+    and 9 FP32 vector passes over n rows (colour-0 rows: z and p gathered, 1/a_ii read, u written; colour-1 rows:
+    the row sums, own z and p read, u gathered, p and q written; the update reads p, q, d, r and 1/L_ii^2 and
+    writes d, r and z), plus the FP64 x of the colour-1 rows read and written every FOLD_EVERY iterations.  Per
+    refresh an FP64 projection of the colour-0 unknowns (the colour-0 rows of the matrix) and an FP64 residual."""
+    it_bytes = (4 + idx) * nz + 4 * (n + 1) + 9 * 4 * n + 8 * n / FOLD_EVERY
+    refresh = 12 * nz + 12 * nz / 2 + 8 * (n + 1) + 36 * n
+    return (outer + 1) * refresh + its * it_bytes
+
+
+def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None, reduced=False):
     """Minimal DRAM bytes of one preconditioned solve: per iteration the product with the non-zeros of A and both
     triangular sweeps over the factor's nzl strictly lower entries (values + idx-byte column indices: 2 where the
     mixed iterations read 16-bit column copies), plus about 15 vector passes (product gathers and outputs, the x/r
@@ -301,6 +313,8 @@ def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None):
     memory.  The mixed form moves FP32 values and vectors - the factor's values in FP16 where the factor keeps FP16
     copies (fvb = 2 bytes per factor value), reads and writes the FP64 x every FOLD_EVERY iterations (the correction
     fold) - and adds an FP64 residual (int32 indices) per refresh."""
+    if reduced:
+        return pcg_reduced_bytes(n, nz, its, outer, idx)
     v = 4 if mixed else 8
     fv = v if fvb is None or not mixed else fvb
     passes = 11 if resident else 15
@@ -346,8 +360,13 @@ def time_arm(sim, args, pg, start=None):
 # Field agreement after the timed steps between the fast method and the plain FP64 CG (both stop every solve at a
 # 1e-8 relative residual, so their solutions may differ by up to about cond(A) * 1e-8 per solve; the pressure
 # system's condition number grows as h^-2), and between the GPU FP64 step and the FP64 oracle's step (the same
-# algorithm, summation order aside).
-FIELD_CHECK_TOL = {"u": 1e-5, "v": 1e-5, "p": 1e-3}
+# algorithm, summation order aside).  The pressure is checked through what the step uses of it, its gradient
+# (-dt grad p, the pressure divergence product that corrects the velocity): the lowest mode of the cavity's
+# pressure system (one pinned node; nearly constant elsewhere, Jacobi-scaled eigenvalue about 1e-8 of the largest
+# at 2048) is left loose by any solve that stops at a 1e-8 residual, and two solvers' pressures differ mostly by
+# that near-constant offset, which accumulates over steps through the warm start.  rel_l2_p and the same without
+# the mean are reported beside it.
+FIELD_CHECK_TOL = {"u": 1e-5, "v": 1e-5, "grad_p": 1e-5}
 ORACLE_FIELD_TOL = 1e-6
 
 
@@ -356,10 +375,17 @@ def rel_l2(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b))) / (nb if nb > 0 else 1.0)
 
 
-def field_diff(fa, fb, nv):
-    """Relative L2 differences of u, v and p between two (uv, p) field sets."""
+def field_diff(fa, fb, nv, grad=None):
+    """Relative L2 differences of u, v and p between two (uv, p) field sets; with grad (p -> -dt grad p) also of the
+    pressure gradient, and of p without the mean of the difference."""
     (uva, pa), (uvb, pb) = fa, fb
-    return {"rel_l2_u": rel_l2(uva[:nv], uvb[:nv]), "rel_l2_v": rel_l2(uva[nv:], uvb[nv:]), "rel_l2_p": rel_l2(pa, pb)}
+    d = {"rel_l2_u": rel_l2(uva[:nv], uvb[:nv]), "rel_l2_v": rel_l2(uva[nv:], uvb[nv:]), "rel_l2_p": rel_l2(pa, pb)}
+    if grad is not None:
+        diff = np.asarray(pa) - np.asarray(pb)
+        nb = float(np.linalg.norm(pb))
+        d["rel_l2_p_mean_free"] = float(np.linalg.norm(diff - diff.mean())) / (nb if nb > 0 else 1.0)
+        d["rel_l2_grad_p"] = rel_l2(grad(pa), grad(pb))
+    return d
 
 
 def nonzeros(sim, slot):
@@ -384,16 +410,18 @@ def roofline(sim, arm, args):
     that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
-    nzl, idx, res, fvb = {}, {}, {}, {}
+    nzl, idx, res, red, fvb = {}, {}, {}, {}, {}
     for slot in (0, 1, 2):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
             res[slot] = sim.precond_inner_form(slot) == "resident"
+            red[slot] = sim.precond_inner_form(slot) == "reduced"
             fvb[slot] = sim.precond_value_bytes(slot)
-    resident = any(res.values())
+    resident, reduced = any(res.values()), any(red.values())
     names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel",
-             2: "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
+             2: "pcg_mixed_inner_kernel_reduced" if reduced else
+                "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
              3: "pcg_fp64_kernel"}
     form = getattr(args, "cg_form", "auto")
     pipe_max = header_constant("NSF_CG_PIPELINED_MAX_ROWS")
@@ -404,7 +432,7 @@ def roofline(sim, arm, args):
         pipe = m_ == 0 and (form == "pipelined" or (form == "auto" and int(n_) < pipe_max))
         if m_ in (2, 3):
             b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4,
-                          res.get(sl, False) and m_ == 2, fvb.get(sl))
+                          res.get(sl, False) and m_ == 2, fvb.get(sl), red.get(sl, False) and m_ == 2)
         else:
             b = algorithmic_bytes(1 if m_ == 1 else 0, int(n_), nz[sl], int(i_), int(o_), pipe)
         name = "cg_fp64_pipe_kernel" if pipe else names[m_]
@@ -437,6 +465,7 @@ def run_gpu(args):
     sim = nsf.NavierStokesAssembly(mesh, w["nu"], w["dt"], device=local, solver=args.solver,
                                    inner_tolerance=args.inner_tol)
     sim.set_cg_form(args.cg_form)
+    sim.set_pcg_form(args.pcg_form)
     setup_s = time.perf_counter() - t0
     init = sim.fields()        # the run's initial state: u = 0 with the Dirichlet values imposed, p = 0
     learned = None
@@ -504,11 +533,12 @@ def run_gpu(args):
                  "speedup": round(parm["ms"] / ms, 3), "clocks": parm["clocks"]}
         # both arms ran the same steps from the same fields: how far apart are the fields they ended with
         tol = FIELD_CHECK_TOL
+        grad = lambda p: plain_sim.sp_r_mult("pressure_divergence", p)   # noqa: E731
         res = {"learned_pcg_mixed" if args.precond == "learned" else args.solver:
-               field_diff(arm["end_fields"], parm["end_fields"], nv)}
+               field_diff(arm["end_fields"], parm["end_fields"], nv, grad)}
         if ic0 is not None:
-            res["ic0_pcg_mixed"] = field_diff(ic0["end_fields"], parm["end_fields"], nv)
-        ok = all(d["rel_l2_u"] <= tol["u"] and d["rel_l2_v"] <= tol["v"] and d["rel_l2_p"] <= tol["p"]
+            res["ic0_pcg_mixed"] = field_diff(ic0["end_fields"], parm["end_fields"], nv, grad)
+        ok = all(d["rel_l2_u"] <= tol["u"] and d["rel_l2_v"] <= tol["v"] and d["rel_l2_grad_p"] <= tol["grad_p"]
                  for d in res.values())
         field_check = {"against": "plain FP64 CG, the same steps 1..K from the initial state", "steps": args.steps,
                        "tol": tol, "pass": ok, **res}
@@ -729,6 +759,8 @@ def main():
                     help="--impl reference: time budget of the timed whole CPU steps")
     ap.add_argument("--cg-form", default="auto", choices=["auto", "three_sync", "pipelined"],
                     help="iteration form of the plain FP64 CG (auto: by system size)")
+    ap.add_argument("--pcg-form", default="auto", choices=["auto", "full", "reduced"],
+                    help="iteration of the mixed PCG on two-colour systems (nsf_set_pcg_form)")
     ap.add_argument("--no-ic0-arm", dest="ic0_arm", action="store_false",
                     help="skip the IC(0) run beside the learned preconditioner")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -383,8 +383,8 @@ class GPUSimulationDevice:
         self._check(library().nsf_set_solver(self._h, SOLVER[solver], float(inner_tolerance)))
 
     def set_pcg_form(self, form="auto"):
-        """Iteration of the mixed PCG on two-colour systems: "full" (product and both colour sweeps on the whole
-        system; "auto" is the same) or "reduced" (PCG on the Schur complement of the colour-0 block)."""
+        """Iteration of the mixed PCG on two-colour systems: "auto" or "reduced" (PCG on the Schur complement of the
+        colour-0 block) or "full" (product and both colour sweeps on the whole system)."""
         self._check(library().nsf_set_pcg_form(self._h, PCG_FORM[form]))
 
     def set_cg_form(self, form="auto"):
@@ -460,11 +460,11 @@ class GPUSimulationDevice:
         return k
 
     def precond_inner_form(self, slot) -> str:
-        """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident" or
-        "none" (no such solve yet)."""
+        """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident",
+        "reduced" or "none" (no such solve yet)."""
         k = _i()
         self._check(library().nsf_precond_inner_form(self._h, _slot(slot), ctypes.byref(k)))
-        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident"}[k.value]
+        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced"}[k.value]
 
     def precond_clear(self, slot):
         self._check(library().nsf_precond_clear(self._h, _slot(slot)))

@@ -267,10 +267,10 @@ bool use_pipelined_cg(const nsf_device* h, const Csr& S) {
     return S.rows < NSF_CG_PIPELINED_MAX_ROWS;
 }
 
-// The reduced (Schur complement) iteration of the split mixed PCG: two colours, a SELL copy and the 1024-thread
-// inner grid.
+// The reduced (Schur complement) iteration of the split mixed PCG (NSF_PCG_FORM_AUTO and _REDUCED): two colours,
+// a SELL copy and the 1024-thread inner grid.
 bool use_reduced_pcg(const nsf_device* h, const Csr& S, const FactorView& f) {
-    if (h->pcgForm != NSF_PCG_FORM_REDUCED) return false;
+    if (h->pcgForm == NSF_PCG_FORM_FULL) return false;
     return f.colours == 2 && S.sellStart.get() && h->ws.gridInner1024 > 0 && f.aDiag && f.aInv32;
 }
 

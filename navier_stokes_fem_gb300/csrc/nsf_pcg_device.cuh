@@ -766,35 +766,26 @@ static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, doubl
             a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, pe, stage, [&](int c) { return x[c]; },
             [&](int row, double acc, double xi) { x[row] = xi + (b[row] - acc) / F.aDiag[row]; });
     if (!t.barrier(where++)) return false;
-    // true residual r = b - A64 x (r_0 = 0 up to rounding), r32 = (float) (scale r), d32 = 0, z_1 = r_1 / L_11^2
+    // true residual r = b - A64 x in FP64 (r_0 = 0 up to rounding), kept in a.r until the FP32 scale is known;
+    // d32 = 0
     const bool resetP = L.resetP != 0;
     double rrp = 0, bbp = 0;
-    DotAcc<float> rzp;
     matrix_product<double, double, false, kResidU<Wide>, Wide>(
         a.sellStart, a.sellCol, a.sellVal, a.rowptr, a.col, a.val, rb, re, stage, [&](int c) { return x[c]; },
         [&](int row, double acc, double) {
             const double bi = b[row];
             const double ri = bi - acc;
-            const float rf = (float)(ri * sc);
-            r32[row] = rf;
+            a.r[row] = ri;
             a.d32[row] = 0.0f;
             if (resetP) pprev[row] = 0.0f;   // restart: p = z
             rrp = fma(ri, ri, rrp);
             bbp = fma(bi, bi, bbp);
-            if (row >= c1) {
-                const float d = F.dinv32[row];
-                const float z = (rf * d) * d;
-                w[row] = z;
-                rzp.add(rf, z);
-            }
         });
     rrp = block_sum(rrp, smem);
     bbp = block_sum(bbp, smem);
-    const double rzb = rzp.block(smem);
     if (threadIdx.x == 0) {
         a.partials[2 * G + t.rank] = rrp;
         a.partials[3 * G + t.rank] = bbp;
-        a.partials[4 * G + t.rank] = rzb;
     }
     if (!t.barrier(where++)) return false;
     L.rr64 = grid_sum(a.partials + 2 * G, G, smem);
@@ -802,7 +793,6 @@ static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, doubl
         L.bb = grid_sum(a.partials + 3 * G, G, smem);
         L.target = L.bb > 0 ? a.tol2 * L.bb : a.tol2 * L.rr64;
     }
-    double rzT = grid_sum(a.partials + 4 * G, G, smem);
     L.state = kLoopDone;
     if (!(L.rr64 == L.rr64) || isinf(L.rr64)) { L.status = NSF_ERR_BREAKDOWN; return true; }
     if (L.rr64 <= L.target) { L.status = NSF_OK; return true; }
@@ -813,18 +803,29 @@ static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, doubl
         L.stalls = 0;
     }
     L.rrBest = fmin(L.rrBest, L.rr64);
+    // the FP32 vectors at the new scale (formed after it is known, so that a tiny residual does not underflow):
+    // r32 = (float) (scale r), z_1 = r_1 / L_11^2, the previous direction rescaled
     const double f = rescale_factor(L.rr64 * sc * sc / a.n);
-    if (f != 1.0) {   // own rows of r32, z_1 and the previous direction (read by the next launch only)
-        const float ff = (float)f;
-        for (int i = rb + (int)threadIdx.x; i < re; i += bs) {
-            r32[i] *= ff;
-            pprev[i] *= ff;
-            if (i >= c1) w[i] *= ff;
+    const double sc2 = sc * f;
+    const float ff = (float)f;
+    DotAcc<float> rzp;
+    for (int i = rb + (int)threadIdx.x; i < re; i += bs) {
+        const float rf = (float)(a.r[i] * sc2);
+        r32[i] = rf;
+        if (f != 1.0) pprev[i] *= ff;
+        if (i >= c1) {
+            const float d = F.dinv32[i];
+            const float z = (rf * d) * d;
+            w[i] = z;
+            rzp.add(rf, z);
         }
-        rzT *= f * f;    // (products of powers of two are exact)
-        L.rz *= f * f;   // the previous cycle's r.z, for beta
-        L.scale = sc * f;
     }
+    L.rz *= f * f;   // the previous cycle's r.z, for beta (products of powers of two are exact)
+    L.scale = sc2;
+    const double rzb = rzp.block(smem);
+    if (threadIdx.x == 0) a.partials[4 * G + t.rank] = rzb;
+    if (!t.barrier(where++)) return false;
+    const double rzT = grid_sum(a.partials + 4 * G, G, smem);
     if (!(rzT > 0.0) || isinf(rzT)) { L.status = NSF_ERR_BREAKDOWN; return true; }
     const bool drifted = L.refresh > 0 && L.rr64 > 0.25 * L.rrCycle;   // (see pcg_mixed_refresh)
     L.beta = (L.resetP || drifted) ? 0.0 : rzT / L.rz;
@@ -897,6 +898,10 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         if (da.code) { L.innerBreakdown = 1; break; }
         const float alphaf = da.v;
         const bool fold = fold_iteration(L);
+        // U, colour-0 rows: d_0 += alpha u_0, so that x_0 follows the directions q_1 was formed with (the rounded
+        // u_0), not their exact projection; the refresh then finds the residual the recurrence carries
+        for (int i = a0 + (int)threadIdx.x; i < a1; i += bs)
+            a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
         // U: colour-1 rows
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;

@@ -73,13 +73,13 @@ __global__ void ap_values_kernel(int64_t nnz, const int* __restrict__ from, cons
 // The diagonal of the permuted matrix (1 on padding rows), and its FP32 inverse.
 __global__ void ap_diag_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                                const double* __restrict__ val, double* __restrict__ diag, float* __restrict__ inv) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double d = 0.0;
-    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
-        if (col[k] == i) d = val[k];
-    diag[i] = d;
-    inv[i] = d != 0.0 ? (float)(1.0 / d) : 0.0f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {   // (grid_for caps)
+        double d = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] == i) d = val[k];
+        diag[i] = d;
+        inv[i] = d != 0.0 ? (float)(1.0 / d) : 0.0f;
+    }
 }
 
 // DSatur colouring of the matrix graph (Brelaz 1979): repeatedly colour the uncoloured row whose neighbours

@@ -34,3 +34,16 @@ def test_field_diff():
     assert d["rel_l2_u"] == 0.0
     assert abs(d["rel_l2_v"] - 0.5) < 1e-15
     assert abs(d["rel_l2_p"] - 1.0 / np.sqrt(5.0)) < 1e-15
+
+
+def test_field_diff_pressure_gradient_and_offset():
+    """The pressure is checked through its gradient: a uniform offset of p changes rel_l2_p but neither the
+    gradient nor the mean-free difference."""
+    nv = 2
+    uv = np.array([1.0, 2.0, 3.0, 4.0])
+    p = np.array([0.0, 1.0, 3.0])
+    grad = lambda q: np.diff(q)   # noqa: E731  (a stand-in for the pressure divergence product)
+    d = bench.field_diff((uv, p + 0.5), (uv, p), nv, grad)
+    assert d["rel_l2_p"] > 0.1
+    assert d["rel_l2_grad_p"] == 0.0 and d["rel_l2_p_mean_free"] < 1e-15
+    assert set(bench.FIELD_CHECK_TOL) == {"u", "v", "grad_p"}

@@ -149,6 +149,73 @@ def test_steps_with_preconditioned_pressure_match_oracle(solver):
     assert it[:, 2].sum() < (0.7 if solver == "pcg_fp64" else 0.9) * it_plain[:, 2].sum()
 
 
+@pytest.mark.parametrize("n", [32, 96])
+def test_reduced_pcg_matches_full_pcg(n):
+    """The reduced (Schur complement) iteration of the mixed PCG on a two-colour pressure system: with IC(0) it runs
+    the full PCG's iterates in exact arithmetic (an FP64 NumPy model of both takes 100 and 299 iterations on these
+    two systems).  In FP32 the Schur complement's near-constant mode (Jacobi-scaled condition number 7e4 at n = 96)
+    is resolved less well than by the full form's difference-form product, which costs the reduced form 25-35 %
+    more iterations on these small systems (5-6 % on the 2048 cavity).  The FP64 true residual meets the tolerance
+    and the solution is the oracle CG's; it reads the factor's colour-1 diagonal only, so a factor whose other
+    entries are scaled gives the same solve, bit for bit."""
+    m = M.cavity(n)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    d = nsf.GPUSimulationDevice(0)
+    name = "pressure_stiffness"
+    rp, col, val, shape = o.matrix(name)
+    d.upload_matrix(name, rp.astype(np.int32), col, val, shape)
+    colour = d.precond_pattern(name)[2]
+    assert colour.max() == 1                                          # two colours
+    d.precond_ic0(name)
+    b = np.random.default_rng(31).standard_normal(shape[0])
+    x0 = 0.01 * np.random.default_rng(32).standard_normal(shape[0])
+    out = {}
+    for form in ("full", "reduced"):
+        d.set_pcg_form(form)
+        out[form] = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_mixed")
+        assert (d.precond_inner_form(name) == "reduced") == (form == "reduced")
+    xf, itf, _ = out["full"]
+    xr_, itr_, _ = out["reduced"]
+    xo, st, ito, _ = o.cg(name, b, x0, tol=TOL)
+    assert st == 0
+    assert _relres(o, name, xr_, b) < 1.5 * TOL
+    assert itr_ <= 1.4 * itf + 5, (itr_, itf)
+    assert rel(xr_, xo) < 1e-6
+    # only L_11 enters: scaling the factor's off-diagonal entries and its colour-0 diagonal changes nothing
+    lower, diag = d.precond_get(name)
+    diag2 = diag.copy()
+    diag2[colour == 0] *= 1.3
+    d.precond_set(name, 1.7 * lower, diag2)
+    d.set_pcg_form("reduced")
+    x2, it2, _ = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_mixed")
+    assert it2 == itr_ and np.array_equal(x2, xr_)
+    d.set_pcg_form("full")
+    d.close()
+    o.close()
+
+
+def test_reduced_pcg_steps_match_discrete_solution():
+    """Whole steps with the reduced mixed PCG on the pressure (IC(0)): within 1e-3 of the discrete solution, as the
+    full form, with at most 40 % more pressure iterations on this small cavity."""
+    m = M.cavity(24)
+    o = oracle.Oracle(m, 0.01, 0.01)
+    o.set_tolerance(1e-13)
+    assert o.step(10)[0] == 0
+    ruv, rp = o.fields()
+    its = {}
+    for form in ("full", "reduced"):
+        sim = nsf.NavierStokesAssembly(m, 0.01, 0.01, solver="pcg_mixed")
+        sim.set_pcg_form(form)
+        sim.precond_ic0("pressure_stiffness")
+        its[form] = sim.step(10)
+        uv, p = sim.fields()
+        assert (sim.precond_inner_form("pressure_stiffness") == "reduced") == (form == "reduced")
+        sim.close()
+        assert max(rel(uv, ruv), rel(p, rp)) < 1e-3, form
+    f, r = its["full"][:, 2].sum(), its["reduced"][:, 2].sum()
+    assert r <= 1.4 * f + 10, (r, f)
+
+
 def _perturbed_cavity(n, seed=11, amp=0.3):
     """A cavity whose interior vertices are moved randomly (no edge axis-aligned): its pressure matrix has no
     exact zeros off the diagonal, three colours and at most 7 entries per row (the narrow, split solver)."""

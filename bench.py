@@ -292,14 +292,17 @@ def config_block(args, w, mesh, solver):
     return cfg
 
 
-def pcg_reduced_bytes(n, nz, its, outer, idx=4):
-    """Minimal DRAM bytes of one reduced (Schur complement) mixed PCG solve of a two-colour system: per iteration
-    every matrix row once (FP32 values + idx-byte columns; the colour-0 rows for u_0, the colour-1 rows for q_1)
-    and 9 FP32 vector passes over n rows (colour-0 rows: z and p gathered, 1/a_ii read, u written; colour-1 rows:
-    the row sums, own z and p read, u gathered, p and q written; the update reads p, q, d, r and 1/L_ii^2 and
-    writes d, r and z), plus the FP64 x of the colour-1 rows read and written every FOLD_EVERY iterations.  Per
-    refresh an FP64 projection of the colour-0 unknowns (the colour-0 rows of the matrix) and an FP64 residual."""
-    it_bytes = (4 + idx) * nz + 4 * (n + 1) + 9 * 4 * n + 8 * n / FOLD_EVERY
+def pcg_reduced_bytes(n, nz, its, outer, idx=4, resident=False):
+    """Minimal DRAM bytes of one reduced (Schur complement) mixed PCG solve of a two-colour system (half the rows
+    in each colour): per iteration every matrix row once (FP32 values + idx-byte columns; the colour-0 rows for u_0,
+    the colour-1 rows for q_1) and FP32 vector traffic of 42 bytes per row: colour-0 rows gather z and p, read
+    1/a_ii and write u (8n); colour-1 rows read the row sums and their own z and p, gather u, write p and q (12n);
+    the update reads u and d and writes d on colour-0 rows (6n), reads p, q, d, r and 1/L_ii^2 and writes d, r and
+    z on colour-1 rows (16n).  With the CTA-private state resident in shared memory (q, d and r of the colour-1
+    rows, d of the colour-0 rows) 26 bytes per row.  Plus the FP64 x read and written every FOLD_EVERY iterations.
+    Per refresh an FP64 projection of the colour-0 unknowns (the colour-0 rows of the matrix) and an FP64
+    residual."""
+    it_bytes = (4 + idx) * nz + 4 * (n + 1) + (26 if resident else 42) * n + 16 * n / FOLD_EVERY
     refresh = 12 * nz + 12 * nz / 2 + 8 * (n + 1) + 36 * n
     return (outer + 1) * refresh + its * it_bytes
 
@@ -314,7 +317,7 @@ def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None, re
     copies (fvb = 2 bytes per factor value), reads and writes the FP64 x every FOLD_EVERY iterations (the correction
     fold) - and adds an FP64 residual (int32 indices) per refresh."""
     if reduced:
-        return pcg_reduced_bytes(n, nz, its, outer, idx)
+        return pcg_reduced_bytes(n, nz, its, outer, idx, resident)
     v = 4 if mixed else 8
     fv = v if fvb is None or not mixed else fvb
     passes = 11 if resident else 15
@@ -415,12 +418,14 @@ def roofline(sim, arm, args):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
-            res[slot] = sim.precond_inner_form(slot) == "resident"
-            red[slot] = sim.precond_inner_form(slot) == "reduced"
+            form_ = sim.precond_inner_form(slot)
+            res[slot] = form_ in ("resident", "reduced_resident")
+            red[slot] = form_.startswith("reduced")
             fvb[slot] = sim.precond_value_bytes(slot)
     resident, reduced = any(res.values()), any(red.values())
     names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel",
-             2: "pcg_mixed_inner_kernel_reduced" if reduced else
+             2: ("pcg_mixed_inner_kernel_reduced_resident" if resident else "pcg_mixed_inner_kernel_reduced")
+                if reduced else
                 "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
              3: "pcg_fp64_kernel"}
     form = getattr(args, "cg_form", "auto")

@@ -172,8 +172,8 @@ int nsf_precond_index_bytes(nsf_device* h, int slot);
 int nsf_precond_value_bytes(nsf_device* h, int slot);
 /* The inner-iteration kernel the slot's last split mixed PCG solve ran: 0 four 256-thread CTAs per SM (one colour),
  * 1 one 1024-thread CTA per SM, 2 the same with the row state only a CTA reads resident in its shared memory (two
- * colours, where it fits), 3 the reduced (Schur complement) iteration of nsf_pcg_form; -1 before the slot's first
- * such solve. */
+ * colours, where it fits), 3 the reduced (Schur complement) iteration of nsf_pcg_form, 4 the same with its
+ * CTA-private row state resident in shared memory; -1 before the slot's first such solve. */
 int nsf_precond_inner_form(nsf_device* h, int slot, int* form);
 int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */

@@ -461,10 +461,10 @@ class GPUSimulationDevice:
 
     def precond_inner_form(self, slot) -> str:
         """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident",
-        "reduced" or "none" (no such solve yet)."""
+        "reduced", "reduced_resident" or "none" (no such solve yet)."""
         k = _i()
         self._check(library().nsf_precond_inner_form(self._h, _slot(slot), ctypes.byref(k)))
-        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced"}[k.value]
+        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced", 4: "reduced_resident"}[k.value]
 
     def precond_clear(self, slot):
         self._check(library().nsf_precond_clear(self._h, _slot(slot)))

@@ -109,13 +109,14 @@ __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_ct
     team_pcg_mixed_inner<C16, true, false, H16>(t, a, nullptr, smem, nullptr);
 }
 
-// The reduced (Schur complement) iterations of a two-colour system in the 1024-thread form (a.f.reduced).
-template <bool C16>
+// The reduced (Schur complement) iterations of a two-colour system in the 1024-thread form (a.f.reduced);
+// Resident: with the CTA-private row state in dynamic shared memory, where it fits.
+template <bool C16, bool Resident = false>
 __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_reduced(CgArgs a) {
     __shared__ double smem[kSmemSlots];
     if (!a.sellStart || a.f.colours != 2 || !a.f.reduced) return;   // (the host never launches it otherwise)
     Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
-    team_pcg_mixed_inner_reduced<C16>(t, a, smem);
+    team_pcg_mixed_inner_reduced<C16, Resident>(t, a, smem);
 }
 
 // The same 1024-thread form with the row state only its CTA reads (the FP32 correction, and r and q of its colour-1
@@ -286,7 +287,9 @@ void cg_configure(CgWorkspace& ws, int device) {
         size_t best = 0;
         for (const void* fn : {(const void*)pcg_mixed_inner_kernel_resident<true, true>,
                                (const void*)pcg_mixed_inner_kernel_resident<true>,
-                               (const void*)pcg_mixed_inner_kernel_resident<false>}) {
+                               (const void*)pcg_mixed_inner_kernel_resident<false>,
+                               (const void*)pcg_mixed_inner_kernel_reduced<true, true>,
+                               (const void*)pcg_mixed_inner_kernel_reduced<false, true>}) {
             cudaFuncAttributes fa{};
             NSF_CUDA(cudaFuncGetAttributes(&fa, fn));
             const int dyn = optin - (int)fa.sharedSizeBytes;
@@ -370,11 +373,15 @@ void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
 int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     if (a.f.reduced) {   // the reduced iterations: two colours and a SELL copy, checked by the caller
         const bool c16 = a.sellCol16 != nullptr;
-        split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes,
-                     c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true>
-                         : (const void*)pcg_mixed_inner_kernel_reduced<false>,
-                     nullptr, s);
-        return 3;
+        // the CTA-private row state in shared memory where it fits (the same footprint as the full resident form)
+        const size_t need = resident_bytes(a.f, ws.gridInner1024);
+        const bool res = ws.residentMaxBytes > 0 && need <= ws.residentMaxBytes;
+        const void* inner = res ? (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true, true>
+                                       : (const void*)pcg_mixed_inner_kernel_reduced<false, true>)
+                                : (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true>
+                                       : (const void*)pcg_mixed_inner_kernel_reduced<false>);
+        split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner, nullptr, s, res ? need : 0);
+        return res ? 4 : 3;
     }
     // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;

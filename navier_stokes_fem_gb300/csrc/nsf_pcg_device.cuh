@@ -841,8 +841,12 @@ static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, doubl
 }
 
 // The inner iterations of the reduced form (H1, H2, U above); the residual is updated in place, since no phase
-// gathers it.  (C16: the 16-bit column copy of the matrix, whose diagonal entries are padding.)
-template <bool C16 = false>
+// gathers it.  (C16: the 16-bit column copy of the matrix, whose diagonal entries are padding.  Resident: the row
+// state only the owning CTA reads - d of its colour-0 rows, and d, r and q of its colour-1 rows - lives in the
+// kernel's dynamic shared memory for the whole launch: nsf_row_state holds d1 at [0, n1), r1 at [n1, 2 n1), q1 at
+// [2 n1, 3 n1) and d0 at [3 n1, 3 n1 + n0); d and r are loaded when the launch starts, d is written back when it
+// ends (the refresh recomputes r).)
+template <bool C16 = false, bool Resident = false>
 static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem, PcgLoop& L, int& where) {
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x, c1 = F.colourRow[1];
@@ -857,6 +861,19 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
     const TC* col;
     if constexpr (C16) col = a.sellCol16;
     else col = a.sellCol;
+    const int n0 = a1 - a0, n1 = b1 - b0;
+    float* sd1 = nsf_row_state;
+    float* sr1 = nsf_row_state + n1;
+    float* sq1 = nsf_row_state + 2 * n1;
+    float* sd0 = nsf_row_state + 3 * n1;
+    if constexpr (Resident) {
+        for (int k = threadIdx.x; k < n1; k += bs) {
+            sd1[k] = a.d32[b0 + k];
+            sr1[k] = r[b0 + k];
+        }
+        for (int k = threadIdx.x; k < n0; k += bs) sd0[k] = a.d32[a0 + k];
+        __syncthreads();
+    }
     L.innerBreakdown = 0;
     const double rrStop = fmax(a.innerTol2 * L.rrRef, L.target) * L.scale * L.scale;   // in the FP32 vectors' scale
     const double invScale = 1.0 / L.scale;
@@ -879,7 +896,8 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         auto g2 = [&](int c) { return c >= c1 ? fmaf(betaf, pp[c], w[c]) : pc[c]; };
         auto e2 = [&](int row, float acc, float pi) {
             pc[row] = pi;
-            a.q32[row] = acc;
+            if constexpr (Resident) sq1[row - b0] = acc;
+            else a.q32[row] = acc;
             df_acc(pqHi, pqLo, pi, acc);
         };
         if (a.sellMaxW <= 5) product32<false, 5, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
@@ -900,8 +918,10 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         const bool fold = fold_iteration(L);
         // U, colour-0 rows: d_0 += alpha u_0, so that x_0 follows the directions q_1 was formed with (the rounded
         // u_0), not their exact projection; the refresh then finds the residual the recurrence carries
-        for (int i = a0 + (int)threadIdx.x; i < a1; i += bs)
-            a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
+        for (int i = a0 + (int)threadIdx.x; i < a1; i += bs) {
+            if constexpr (Resident) sd0[i - a0] = fold_correction(a, i, fmaf(alphaf, pc[i], sd0[i - a0]), fold, invScale);
+            else a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
+        }
         // U: colour-1 rows
         float rrHi = 0.f, rrLo = 0.f;
         DotAcc<float> rzn;
@@ -912,9 +932,15 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
                 const int i = i0 + u * bs;
                 if (i < b1) {
                     pi[u] = pc[i];
-                    qi[u] = a.q32[i];
-                    di[u] = a.d32[i];
-                    ri[u] = r[i];
+                    if constexpr (Resident) {
+                        qi[u] = sq1[i - b0];
+                        di[u] = sd1[i - b0];
+                        ri[u] = sr1[i - b0];
+                    } else {
+                        qi[u] = a.q32[i];
+                        di[u] = a.d32[i];
+                        ri[u] = r[i];
+                    }
                     vi[u] = dinv[i];
                 }
             }
@@ -922,9 +948,15 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
             for (int u = 0; u < kRowsLean; ++u) {
                 const int i = i0 + u * bs;
                 if (i < b1) {
-                    a.d32[i] = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
+                    const float dn = fold_correction(a, i, fmaf(alphaf, pi[u], di[u]), fold, invScale);
                     const float rn = fmaf(-alphaf, qi[u], ri[u]);
-                    r[i] = rn;
+                    if constexpr (Resident) {
+                        sd1[i - b0] = dn;
+                        sr1[i - b0] = rn;
+                    } else {
+                        a.d32[i] = dn;
+                        r[i] = rn;
+                    }
                     df_acc(rrHi, rrLo, rn, rn);
                     const float z = (rn * vi[u]) * vi[u];
                     w[i] = z;
@@ -950,6 +982,11 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         L.beta = block_scalar(smem, [&] { return rzs / L.rz; });
         L.rz = rzs;
         betaf = (float)L.beta;
+    }
+    if constexpr (Resident) {   // d of every own row back to its global copy (the refresh folds it into x)
+        __syncthreads();
+        for (int k = threadIdx.x; k < n1; k += bs) a.d32[b0 + k] = sd1[k];
+        for (int k = threadIdx.x; k < n0; k += bs) a.d32[a0 + k] = sd0[k];
     }
     L.state = kLoopRefresh;
     return true;
@@ -1059,7 +1096,7 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
 }
 
 // The reduced form's inner launch (two colours, a SELL copy and a.f.reduced; see pcg_mixed_inner_reduced).
-template <bool C16 = false>
+template <bool C16 = false, bool Resident = false>
 static __device__ void team_pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem) {
     int where = 400;
     const PcgLoop& G = *a.loop;
@@ -1073,7 +1110,7 @@ static __device__ void team_pcg_mixed_inner_reduced(Team& t, const CgArgs& a, do
     L.itRef = G.itRef;
     L.flip = G.flip;
     L.rflip = G.rflip;
-    const bool ok = pcg_mixed_inner_reduced<C16>(t, a, smem, L, where);
+    const bool ok = pcg_mixed_inner_reduced<C16, Resident>(t, a, smem, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
     if (t.rank == 0 && threadIdx.x == 0) {
         a.loop->rz = L.rz;

@@ -173,7 +173,7 @@ def test_reduced_pcg_matches_full_pcg(n):
     for form in ("full", "reduced"):
         d.set_pcg_form(form)
         out[form] = d.conjugate_gradient(name, b, x0, eps=TOL, solver="pcg_mixed")
-        assert (d.precond_inner_form(name) == "reduced") == (form == "reduced")
+        assert d.precond_inner_form(name).startswith("reduced") == (form == "reduced")
     xf, itf, _ = out["full"]
     xr_, itr_, _ = out["reduced"]
     xo, st, ito, _ = o.cg(name, b, x0, tol=TOL)
@@ -209,7 +209,7 @@ def test_reduced_pcg_steps_match_discrete_solution():
         sim.precond_ic0("pressure_stiffness")
         its[form] = sim.step(10)
         uv, p = sim.fields()
-        assert (sim.precond_inner_form("pressure_stiffness") == "reduced") == (form == "reduced")
+        assert sim.precond_inner_form("pressure_stiffness").startswith("reduced") == (form == "reduced")
         sim.close()
         assert max(rel(uv, ruv), rel(p, rp)) < 1e-3, form
     f, r = its["full"][:, 2].sum(), its["reduced"][:, 2].sum()

@@ -398,11 +398,13 @@ def nonzeros(sim, slot):
 
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
-# 4,198,401 rows, whose vectors exceed L2): the mixed PCG's resident inner kernel (row state in shared memory,
+# 4,198,401 rows, whose vectors exceed L2): the reduced (Schur complement) inner kernel with its row state in shared
+# memory 5.53 GB over 40 iterations; the full-form resident inner kernel (row state in shared memory,
 # 16-bit column copies, FP16 factor values) 11.01 GB over 40 iterations; the 1024-thread inner kernel without the
 # resident state (16-bit column copies, FP32 factor values) 17.49 GB over 40 iterations; cg_fp64_kernel 30.67 GB
 # over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_resident": 65.5, "pcg_mixed_inner_kernel_cta1024": 104.1,
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_reduced_resident": 32.9,
+                                "pcg_mixed_inner_kernel_resident": 65.5, "pcg_mixed_inner_kernel_cta1024": 104.1,
                                 "cg_fp64_kernel": 121.7}
 
 
@@ -723,6 +725,7 @@ def run_cg_probe(args):
     sim.close()
     dev = nsf.GPUSimulationDevice(0)
     dev.set_cg_form(args.cg_form)
+    dev.set_pcg_form(args.pcg_form)
     if args.inner_tol > 0:   # e.g. 1e-6: the mixed solvers' first inner launch then runs the whole probe budget
         dev.set_solver(args.solver, args.inner_tol)
     dev.upload_matrix("pressure_stiffness", *mat)

@@ -243,6 +243,20 @@ int nsf_sim_step(nsf_device* h, int nsteps, int* iterations);
 int nsf_sim_step_host(nsf_device* h, const double* uvIn, const double* pIn, int nsteps, double* uvOut,
                       double* pOut, int* iterations);
 
+/* Operator-split scheme of nsf_sim_step (nsf_sim_set_scheme). */
+enum nsf_scheme {
+    NSF_SCHEME_SEMI_LAGRANGIAN = 0,     /* NavierStokesAssembly::semiLagrangianSolve (include/assembly.h:1477-1557):
+                                         * semi-Lagrangian advection, implicit diffusion, pressure projection */
+    NSF_SCHEME_EXPLICIT_CONVECTION = 1  /* NavierStokesAssembly::solve (include/assembly.h:1065-1299), a path the
+                                         * reference's driver never calls: tentative velocity M y = -dt (C(u) + nu K) u
+                                         * with the convection matrix of the current velocity (include/assembly.h:
+                                         * 1581-1625), u += y, Dirichlet values imposed; the same pressure solve; the
+                                         * correction M y = -dt Grad p, u += y.  C and K are applied matrix free per
+                                         * element.  iterations: tentative u, v, pressure, correction u, v */
+};
+/* Selects the scheme of the following nsf_sim_step calls (NSF_ERR_STATE before nsf_sim_setup). */
+int nsf_sim_set_scheme(nsf_device* h, int scheme);
+
 /* Time-dependent Dirichlet data.  The reference's expression grammar accepts the variable t
  * (cpp/expression.cpp:167-177) but its imposeVelocityDirichlet (include/assembly.h:1559-1579) evaluates the
  * expressions with x and y only; this replaces those host evaluations by device-side ones that may use t.

@@ -128,6 +128,7 @@ _SIGS = {
     "nsf_eval_expression_t": (_i, [ctypes.c_char_p, _d, _d, _d, _P(_d), ctypes.c_char_p, _sz]),
     "nsf_sim_set_bc_expressions": (_i, [_v, _i, _v, _v, _v, _v, _d]),
     "nsf_sim_time": (_i, [_v, _P(_d)]),
+    "nsf_sim_set_scheme": (_i, [_v, _i]),
     "nsf_launch_count": (_i, [_v, _P(_i64)]),
     "nsf_batch_clear": (_i, [_v]),
     "nsf_batch_add": (_i, [_v, _i, _arr(np.float32), _i, _arr(np.int32), _i, _i, _arr(np.int32), _arr(np.float64),
@@ -659,6 +660,11 @@ class NavierStokesAssembly(GPUSimulationDevice):
         self._check(library().nsf_sim_set_bc_expressions(self._h, len(exprs), ctypes.cast(arr, _v),
                                                          u.ctypes.data_as(_v), v.ctypes.data_as(_v),
                                                          p.ctypes.data_as(_v), float(t0)))
+
+    def set_scheme(self, scheme: str = "semi_lagrangian"):
+        """Operator-split scheme of step(): "semi_lagrangian" (semiLagrangianSolve) or "explicit_convection" (the
+        reference's NavierStokesAssembly::solve: explicit convection and diffusion, then the projection)."""
+        self._check(library().nsf_sim_set_scheme(self._h, {"semi_lagrangian": 0, "explicit_convection": 1}[scheme]))
 
     def time(self) -> float:
         """Simulated time of the resident fields (nsf_sim_time)."""

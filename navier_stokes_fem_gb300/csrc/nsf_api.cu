@@ -49,6 +49,7 @@ void setup_instance(MeshDev& m, SimState& S, Csr* mats, cudaStream_t s, int nNod
     S.steps = 0;
     S.bcTimeDependent = false;
     S.nBcNodeV = S.nBcNodeP = 0;
+    S.scheme = NSF_SCHEME_SEMI_LAGRANGIAN;
     S.hOccV.assign(velocityBCNodes, velocityBCNodes + nVelocityBC);
     S.hOccP.assign(pressureBCNodes, pressureBCNodes + nPressureBC);
     const int Nv = nNodes, P = nPressure;
@@ -482,8 +483,69 @@ void sim_step_launch(nsf_device* h, int infos[5]) {
     std::swap(S.uv, S.tmp);
 }
 
+// One step of NavierStokesAssembly::solve (include/assembly.h:1137-1297), the explicit-convection scheme; `infos`
+// receives 5 info indices (tentative u, v, pressure, correction u, v).  The reference solves its mass systems with
+// the velocity as the initial guess of the increment, and so does this.
+void sim_step_explicit_launch(nsf_device* h, int infos[5]) {
+    SimState& S = h->sim;
+    MeshDev& m = h->mesh;
+    const int Nv = m.nNodes;
+    auto mode = [&](int slot) {
+        const bool pre = (h->solverMode == NSF_SOLVER_PCG_MIXED || h->solverMode == NSF_SOLVER_PCG_FP64) &&
+                         h->factors[slot].ready && !h->pcgOff[slot];
+        const bool mixed = (h->solverMode == NSF_SOLVER_MIXED || h->solverMode == NSF_SOLVER_PCG_MIXED) &&
+                           !h->mixedOff[slot];
+        if (pre) return mixed ? NSF_SOLVER_PCG_MIXED : NSF_SOLVER_PCG_FP64;
+        return mixed ? NSF_SOLVER_MIXED : NSF_SOLVER_FP64;
+    };
+    cudaStream_t s = h->stream;
+    double* uv = S.uv.get();
+    double* tmp = S.tmp.get();
+    ++S.steps;
+    if (S.bcTimeDependent) bc_update_launch(S, m, h->mats, S.t0 + (double)S.steps * S.dt, s);
+    // tentative velocity (include/assembly.h:1151-1196): rhs = -dt (C(u) + nu K) u; M y = rhs from x0 = u; u += y
+    convection_rhs_launch(m, S, uv, S.rhsV.get(), s);
+    for (int ch = 0; ch < 2; ++ch)
+        infos[ch] = launch_solve(h, NSF_VELOCITY_MASS, mode(NSF_VELOCITY_MASS), S.rhsV.get() + (size_t)ch * Nv,
+                                 uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, -1, h->tol, nullptr);
+    // u += y with the Dirichlet values imposed (imposeVelocityDirichlet, :1198): into tmp, then swapped
+    for (int ch = 0; ch < 2; ++ch)
+        axpy_bc_launch(Nv, uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, S.bcV.get(), S.gV[ch].get(), s);
+    std::swap(S.uv, S.tmp);
+    uv = S.uv.get();
+    tmp = S.tmp.get();
+    // pressure (:1204-1241): rhs_p = -(1/dt) Div u with the Dirichlet rows and lift, solved from the previous p
+    {
+        CgArgs f{};
+        Csr& Bd = h->mats[NSF_VELOCITY_DIVERGENCE];
+        prepare_matrix(Bd, false, s);
+        f.bRowptr = Bd.rowptr.get();
+        f.bCol = Bd.col.get();
+        f.bVal = Bd.val.get();
+        f.bSellStart = Bd.sellStart.get();
+        f.bSellCol = Bd.sellCol.get();
+        f.bSellVal = Bd.sellVal.get();
+        f.bX = uv;
+        f.lift = S.liftP.get();
+        f.bcMask = S.bcP.get();
+        f.bcValue = S.gP.get();
+        f.bOut = S.rhsP.get();
+        infos[2] = launch_solve(h, NSF_PRESSURE_STIFFNESS, mode(NSF_PRESSURE_STIFFNESS), f.bOut, S.p.get(), S.p.get(),
+                                -1, h->tol, &f);
+    }
+    // correction (:1250-1281): M y = -dt Grad p from x0 = u; u += y (no Dirichlet values imposed afterwards)
+    spmv_launch(h->mats[NSF_PRESSURE_DIVERGENCE], S.p.get(), S.rhsV.get(), s);
+    for (int ch = 0; ch < 2; ++ch)
+        infos[3 + ch] = launch_solve(h, NSF_VELOCITY_MASS, mode(NSF_VELOCITY_MASS), S.rhsV.get() + (size_t)ch * Nv,
+                                     uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, -1, h->tol, nullptr);
+    for (int ch = 0; ch < 2; ++ch) axpy_bc_launch(Nv, uv + (size_t)ch * Nv, tmp + (size_t)ch * Nv, nullptr, nullptr, s);
+    std::swap(S.uv, S.tmp);
+}
+
 constexpr int kSolveSlot[5] = {NSF_DIFFUSION, NSF_DIFFUSION, NSF_PRESSURE_STIFFNESS, NSF_VELOCITY_MASS,
                                 NSF_VELOCITY_MASS};
+constexpr int kSolveSlotExplicit[5] = {NSF_VELOCITY_MASS, NSF_VELOCITY_MASS, NSF_PRESSURE_STIFFNESS,
+                                        NSF_VELOCITY_MASS, NSF_VELOCITY_MASS};
 
 void run_steps(nsf_device* h, int nsteps, int* iterations) {
     sim_require(h);
@@ -494,12 +556,19 @@ void run_steps(nsf_device* h, int nsteps, int* iterations) {
     while (done < nsteps) {
         const int n = std::min(chunk, nsteps - done);
         idx.assign((size_t)5 * n, 0);
-        for (int k = 0; k < n; ++k) sim_step_launch(h, &idx[(size_t)5 * k]);
+        for (int k = 0; k < n; ++k) {
+            if (h->sim.scheme == NSF_SCHEME_EXPLICIT_CONVECTION) sim_step_explicit_launch(h, &idx[(size_t)5 * k]);
+            else sim_step_launch(h, &idx[(size_t)5 * k]);
+        }
         std::vector<CgInfo> all(h->ws.info.n);
         NSF_CUDA(cudaMemcpyAsync(all.data(), h->ws.info.get(), sizeof(CgInfo) * all.size(), cudaMemcpyDeviceToHost,
                                  h->stream));
         NSF_CUDA(cudaStreamSynchronize(h->stream));
-        static const char* names[5] = {"diffusion u", "diffusion v", "pressure", "mass u", "mass v"};
+        static const char* namesSL[5] = {"diffusion u", "diffusion v", "pressure", "mass u", "mass v"};
+        static const char* namesEx[5] = {"tentative u", "tentative v", "pressure", "correction u", "correction v"};
+        const bool ex = h->sim.scheme == NSF_SCHEME_EXPLICIT_CONVECTION;
+        const char* const* names = ex ? namesEx : namesSL;
+        const int* slots = ex ? kSolveSlotExplicit : kSolveSlot;
         for (int k = 0; k < n; ++k)
             for (int j = 0; j < 5; ++j) {
                 const CgInfo& info = all[idx[(size_t)5 * k + j]];
@@ -507,9 +576,9 @@ void run_steps(nsf_device* h, int nsteps, int* iterations) {
                 if (info.fallback) {
                     const int used = h->infoMode[idx[(size_t)5 * k + j]];
                     if (used == NSF_SOLVER_PCG_MIXED || used == NSF_SOLVER_PCG_FP64)
-                        h->pcgOff[kSolveSlot[j]] = true;    // the factor did not pay: plain CG from now on
+                        h->pcgOff[slots[j]] = true;    // the factor did not pay: plain CG from now on
                     else
-                        h->mixedOff[kSolveSlot[j]] = true;  // FP32 cannot resolve this system
+                        h->mixedOff[slots[j]] = true;  // FP32 cannot resolve this system
                 }
                 if (info.status != NSF_OK)
                     throw Error{info.status, "step " + std::to_string(done + k + 1) + ", " + names[j] + " solve: " +
@@ -820,6 +889,14 @@ int nsf_sim_set_bc_expressions(nsf_device* h, int nExpressions, const char* cons
     sim_require(h);
     bc_set_programs(h->sim, h->mesh, h->mats, nExpressions, expressions, velocityU, velocityV, pressure, t0,
                     h->stream);
+    NSF_END(h)
+}
+
+int nsf_sim_set_scheme(nsf_device* h, int scheme) {
+    NSF_BEGIN(h)
+    sim_require(h);
+    if (scheme != NSF_SCHEME_SEMI_LAGRANGIAN && scheme != NSF_SCHEME_EXPLICIT_CONVECTION) throw bad_arg("unknown scheme");
+    h->sim.scheme = scheme;
     NSF_END(h)
 }
 

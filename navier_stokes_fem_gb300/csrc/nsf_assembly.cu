@@ -30,6 +30,17 @@ struct RefIntegralsDev {
 };
 __constant__ RefIntegralsDev c_ref;
 
+// The P2 shape functions and their reference derivatives at the 7 quadrature points, with the weights: the
+// per-point values the convection integrand needs (LocalConvection in NavierStokesAssembly::solve,
+// include/assembly.h:1581-1625).
+struct QuadTableDev {
+    double psi[7][6];
+    double dxi[7][6];
+    double deta[7][6];
+    double w[7];
+};
+__constant__ QuadTableDev c_quad;
+
 static void p2_eval_h(double xi, double eta, double o[6]) {
     o[0] = 1 - 3 * xi - 3 * eta + 2 * xi * xi + 4 * xi * eta + 2 * eta * eta;
     o[1] = 2 * xi * xi - xi;
@@ -72,6 +83,25 @@ static RefIntegralsDev reference_integrals() {
             }
     }
     return I;
+}
+
+static QuadTableDev quad_table() {
+    QuadTableDev Q;
+    const double qx[7] = {0, 1, 0, 0.5, 0.5, 0, 1.0 / 3.0};
+    const double qy[7] = {0, 0, 1, 0, 0.5, 0.5, 1.0 / 3.0};
+    const double qw[7] = {3.0 / 120, 3.0 / 120, 3.0 / 120, 8.0 / 120, 8.0 / 120, 8.0 / 120, 27.0 / 120};
+    for (int k = 0; k < 7; ++k) {
+        const double xi = qx[k], eta = qy[k];
+        p2_eval_h(xi, eta, Q.psi[k]);
+        const double dx2[6] = {-3 + 4 * eta + 4 * xi, -1 + 4 * xi, 0, 4 * eta, -4 * eta, 4 - 4 * eta - 8 * xi};
+        const double de2[6] = {-3 + 4 * eta + 4 * xi, 0, -1 + 4 * eta, 4 * xi, 4 - 8 * eta - 4 * xi, -4 * xi};
+        for (int i = 0; i < 6; ++i) {
+            Q.dxi[k][i] = dx2[i];
+            Q.deta[k][i] = de2[i];
+        }
+        Q.w[k] = qw[k];
+    }
+    return Q;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -265,6 +295,111 @@ __global__ void __launch_bounds__(128) assemble_colour_kernel(AsmArgs a) {
     }
 }
 
+// The explicit-convection step's right-hand side, rhs -= dt (C(u) + nu K) u for both velocity components, matrix
+// free: per element the local convection matrix C_ij = sign sum_q w_q psi_i (u_h B dpsi_j) (the reference's
+// integrand psi^T psi U B dpsi, include/assembly.h:1601-1616, with u_h = psi U at the point, applied to the local
+// velocities without forming C) and the local stiffness K of the assembly kernel; one thread per element, one launch
+// per element colour, so no two threads of a launch add into the same row.
+struct ConvArgs {
+    const float2* xy;
+    const int* el;
+    const int* order;
+    int begin, end;
+    int nNodes;
+    double dt, nu;
+    const double* uv;   // [u | v]
+    double* rhs;        // [u | v], accumulated
+};
+
+__global__ void __launch_bounds__(128) convection_rhs_kernel(ConvArgs a) {
+    const int k = a.begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.end) return;
+    const int e = a.order[k];
+    int t[6];
+    double xy[12], u[6], v[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        t[i] = a.el[6 * (size_t)e + i];
+        const float2 p = a.xy[t[i]];
+        xy[2 * i] = p.x;
+        xy[2 * i + 1] = p.y;
+        u[i] = a.uv[t[i]];
+        v[i] = a.uv[t[i] + a.nNodes];
+    }
+    double B[2][2];
+    B[0][0] = xy[5] - xy[1];
+    B[0][1] = xy[1] - xy[3];
+    B[1][0] = xy[0] - xy[4];
+    B[1][1] = xy[2] - xy[0];
+    const double bdet = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+    const double sign = bdet > 0 ? 1.0 : -1.0;
+    const double invJ = 1.0 / fabs(bdet);
+    // per quadrature point: the convected derivative of the local u and v, (u_h B dpsi) . U
+    double cu[6] = {}, cv[6] = {};
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        double uh = 0, vh = 0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            uh = fma(c_quad.psi[q][j], u[j], uh);
+            vh = fma(c_quad.psi[q][j], v[j], vh);
+        }
+        const double g0 = uh * B[0][0] + vh * B[1][0];
+        const double g1 = uh * B[0][1] + vh * B[1][1];
+        double du = 0, dv = 0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const double gj = g0 * c_quad.dxi[q][j] + g1 * c_quad.deta[q][j];
+            du = fma(gj, u[j], du);
+            dv = fma(gj, v[j], dv);
+        }
+        const double wq = c_quad.w[q] * sign;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            cu[i] = fma(wq * c_quad.psi[q][i], du, cu[i]);
+            cv[i] = fma(wq * c_quad.psi[q][i], dv, cv[i]);
+        }
+    }
+    for (int i = 0; i < 6; ++i) {
+        double ku = 0, kv = 0;
+        for (int j = 0; j < 6; ++j) {
+            double kij = 0;
+            const double s0 = c_ref.delP2[i][j], s1 = c_ref.delP2[i][6 + j], s2 = c_ref.delP2[6 + i][j],
+                         s3 = c_ref.delP2[6 + i][6 + j];
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                kij += s0 * B[q][0] * B[q][0] + s1 * B[q][0] * B[q][1] + s2 * B[q][0] * B[q][1] + s3 * B[q][1] * B[q][1];
+            kij *= invJ;
+            ku = fma(kij, u[j], ku);
+            kv = fma(kij, v[j], kv);
+        }
+        a.rhs[t[i]] -= a.dt * (cu[i] + a.nu * ku);
+        a.rhs[t[i] + a.nNodes] -= a.dt * (cv[i] + a.nu * kv);
+    }
+}
+
+void convection_rhs_launch(const MeshDev& m, const SimState& S, const double* uv, double* rhs, cudaStream_t s) {
+    NSF_CUDA(cudaMemsetAsync(rhs, 0, sizeof(double) * 2 * (size_t)m.nNodes, s));
+    ConvArgs a{};
+    a.xy = m.xy.get();
+    a.el = m.el.get();
+    a.order = S.elOrder.get();
+    a.nNodes = m.nNodes;
+    a.dt = S.dt;
+    a.nu = S.viscosity;
+    a.uv = uv;
+    a.rhs = rhs;
+    for (size_t c = 0; c + 1 < S.elStart.size(); ++c) {
+        a.begin = S.elStart[c];
+        a.end = S.elStart[c + 1];
+        const int n = a.end - a.begin;
+        if (n == 0) continue;
+        convection_rhs_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+        NSF_CUDA(cudaGetLastError());
+        count_launch();
+    }
+}
+
 // Dirichlet rows become identity rows: the diagonal entry is the only one the pattern keeps there.
 __global__ void bc_diagonal_kernel(int n, const unsigned char* bc, const int* rp, double* val) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -352,16 +487,19 @@ int assemble_instance(MeshDev& m, SimState& sim, Csr* mats, cudaStream_t s, doub
         std::vector<int> fill(cStart.begin(), cStart.end() - 1);
         for (int e = 0; e < T; ++e) order[fill[colour[e]]++] = e;
     }
-    DevBuf<int> dOrder;
-    dOrder.upload(order.data(), order.size(), s);
+    sim.elOrder.upload(order.data(), order.size(), s);   // (kept for the explicit-convection step)
+    sim.elStart = cStart;
+    const int* dOrder = sim.elOrder.get();
 
     const RefIntegralsDev I = reference_integrals();
     NSF_CUDA(cudaMemcpyToSymbolAsync(c_ref, &I, sizeof(I), 0, cudaMemcpyHostToDevice, s));
+    const QuadTableDev Q = quad_table();
+    NSF_CUDA(cudaMemcpyToSymbolAsync(c_quad, &Q, sizeof(Q), 0, cudaMemcpyHostToDevice, s));
 
     AsmArgs a{};
     a.xy = m.xy.get();
     a.el = m.el.get();
-    a.order = dOrder.get();
+    a.order = dOrder;
     a.nNodes = Nv;
     a.dtnu = dt * viscosity;
     a.bcV = sim.bcV.get();

@@ -397,6 +397,11 @@ struct SimState {
     DevBuf<int> bcNodeP, bcOccStartP, bcProgP;
     int nBcNodeV = 0, nBcNodeP = 0;
     DevBuf<double> gSumV[2], gSumP;   // per node, the sum of its occurrences' values (the lift's weights)
+    // the element colouring of the assembly (no two elements of a colour share a node), kept for the
+    // explicit-convection step's matrix-free right-hand side
+    DevBuf<int> elOrder;
+    std::vector<int> elStart;
+    int scheme = NSF_SCHEME_SEMI_LAGRANGIAN;
     DevBuf<double> uv, tmp, p, rhsV, rhsP;
     DevBuf<double> liftV[2], liftP;
     DevBuf<unsigned char> bcV, bcP;
@@ -411,6 +416,10 @@ struct SimState {
 void bc_set_programs(SimState& S, const MeshDev& m, Csr* mats, int nExpressions, const char* const* expressions,
                      const int* velocityU, const int* velocityV, const int* pressure, double t0, cudaStream_t s);
 void bc_update_launch(SimState& S, const MeshDev& m, Csr* mats, double t, cudaStream_t s);
+
+// rhs = -dt (C(u) + nu K) u for both velocity components (NavierStokesAssembly::solve's tentative-velocity
+// right-hand side), matrix free, per element colour (nsf_assembly.cu).
+void convection_rhs_launch(const MeshDev& m, const SimState& S, const double* uv, double* rhs, cudaStream_t s);
 
 // One mesh instance of the batched form: its mesh and tree, matrices, fields and CG workspace.
 struct Instance {

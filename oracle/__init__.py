@@ -106,6 +106,7 @@ def lib():
         L.orc_get_fields.argtypes = [_p, _dptr, _dptr]
         L.orc_set_tolerance.argtypes = [_p, _d]
         L.orc_set_bc.argtypes = [_p, _dptr, _dptr, _dptr]
+        L.orc_set_scheme.argtypes = [_p, _i]
         L.orc_point_in_triangle.restype = _i
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
         _u8ptr = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
@@ -359,6 +360,10 @@ class Oracle:
     def set_tolerance(self, tol: float):
         """Relative residual of every CG solve of `step` (1e-8 by default)."""
         lib().orc_set_tolerance(self._h, float(tol))
+
+    def set_scheme(self, scheme: str = "semi_lagrangian"):
+        """"semi_lagrangian" (semiLagrangianSolve) or "explicit_convection" (NavierStokesAssembly::solve)."""
+        lib().orc_set_scheme(self._h, {"semi_lagrangian": 0, "explicit_convection": 1}[scheme])
 
     def step(self, n=1):
         iters = np.zeros(5 * n, np.int32)

@@ -134,6 +134,28 @@ template <typename R, int n, int ld> static void local_stiffness(const R* xy, co
         }
 }
 
+// Local convection matrix of NavierStokesAssembly::assembleConvectionMatrix (include/assembly.h:1581-1625): the
+// integrand psi^T psi U B dpsi times the sign of the Jacobian (U: the element's 6 x 2 nodal velocities), summed
+// over the quadrature points with their weights; evaluated here as psi_i ((psi U) B dpsi)_j.
+template <typename R> static void local_convection(const R* xy, const R vel[6][2], R out[6][6]) {
+    R B[2][2], det;
+    diff_operator(xy, det, B);
+    const R sign = det > 0 ? R(1) : R(-1);
+    const Quadrature<R> q;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) out[i][j] = 0;
+    for (int k = 0; k < q.n; ++k) {
+        R psi[6], dxi[6], deta[6];
+        p2_eval(q.x[k], q.y[k], psi);
+        p2_del(q.x[k], q.y[k], dxi, deta);
+        R uh = 0, vh = 0;
+        for (int m = 0; m < 6; ++m) { uh += psi[m] * vel[m][0]; vh += psi[m] * vel[m][1]; }
+        const R g0 = uh * B[0][0] + vh * B[1][0], g1 = uh * B[0][1] + vh * B[1][1];
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) out[i][j] += (psi[i] * (g0 * dxi[j] + g1 * deta[j]) * sign) * q.w[k];
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // Sparse matrices: triplets summed in insertion order, rows sorted by column (SMM::TripletMatrix -> CSRMatrix)
 // ------------------------------------------------------------------------------------------------
@@ -415,6 +437,7 @@ struct SolverBase {
     virtual void spmv(int slot, const double* x, double* y) = 0;
     virtual void set_tol(double t) = 0;
     virtual void set_bc(const double* u, const double* v, const double* p) = 0;
+    virtual void set_scheme(int scheme) = 0;
     KDTree tree;
     std::vector<float> xy;
     std::vector<int> el;
@@ -663,9 +686,60 @@ template <typename R> struct Solver : SolverBase {
         uv.swap(tmp);
         return st;
     }
+    // One step of NavierStokesAssembly::solve (include/assembly.h:1137-1297), the explicit-convection scheme the
+    // reference's driver never calls: rhs = -dt (C(u) + nu K) u from the element matrices (the loop at
+    // :1151-1165 over the convection and the un-eliminated stiffness matrices, here element by element), the
+    // tentative velocity M y = rhs from x0 = u per component, u += y, Dirichlet values; the pressure solve of
+    // one_step; the correction M y = -dt Grad p from x0 = u, u += y.  iters[5] = tentative u, v, pressure,
+    // correction u, v.
+    int one_step_explicit(int* iters) {
+        int st = 0;
+        R* u = uv.data();
+        R* t = tmp.data();
+        const RefIntegrals<R> I;
+        std::fill(rhsV.begin(), rhsV.end(), R(0));
+        for (int e = 0; e < T; ++e) {
+            R exy[12], vel[6][2], kloc[6][6], cloc[6][6];
+            element_xy(e, exy);
+            const int* en = el.data() + 6 * (size_t)e;
+            for (int m = 0; m < 6; ++m) { vel[m][0] = u[en[m]]; vel[m][1] = u[en[m] + Nv]; }
+            local_stiffness<R, 6, 12>(exy, I.delP2, kloc);
+            local_convection(exy, vel, cloc);
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) {
+                    const R part = -dt * (cloc[i][j] + nu * kloc[i][j]);
+                    rhsV[en[i]] += part * vel[j][0];
+                    rhsV[en[i] + Nv] += part * vel[j][1];
+                }
+        }
+        for (int ch = 0; ch < 2; ++ch) {
+            const size_t o = (size_t)ch * Nv;
+            st |= solve(VELOCITY_MASS, rhsV.data() + o, u + o, t + o, &iters[ch]);
+            for (int i = 0; i < Nv; ++i) u[o + i] += t[o + i];
+        }
+        impose_velocity(u);
+        mats[VELOCITY_DIVERGENCE].multiply(u, rhsP.data());
+        const CSR<R>& Wp = mats[PRESSURE_DIRICHLET_WEIGHTS];
+        for (size_t k = 0; k < pNodes.size(); ++k) {
+            const int nd = pNodes[k];
+            rhsP[nd] = gp[k];
+            for (int64_t q = Wp.rowptr[nd]; q < Wp.rowptr[nd + 1]; ++q) rhsP[Wp.col[q]] -= Wp.val[q] * gp[k];
+        }
+        std::vector<R> pin(p);
+        st |= solve(PRESSURE_STIFFNESS, rhsP.data(), pin.data(), p.data(), &iters[2]);
+        mats[PRESSURE_DIVERGENCE].multiply(p.data(), rhsV.data());
+        for (int ch = 0; ch < 2; ++ch) {
+            const size_t o = (size_t)ch * Nv;
+            st |= solve(VELOCITY_MASS, rhsV.data() + o, u + o, t + o, &iters[3 + ch]);
+            for (int i = 0; i < Nv; ++i) u[o + i] += t[o + i];
+        }
+        return st;
+    }
+    int scheme = 0;   // 0: semiLagrangianSolve, 1: solve (explicit convection)
+    void set_scheme(int s_) override { scheme = s_; }
     int step(int nsteps, int* iters) override {
         int st = 0;
-        for (int s = 0; s < nsteps; ++s) st |= one_step(iters + 5 * s);
+        for (int s = 0; s < nsteps; ++s) st |= scheme == 1 ? one_step_explicit(iters + 5 * s) : one_step(iters + 5 * s);
         return st;
     }
     void set_fields(const double* w, const double* pp) override {
@@ -822,6 +896,7 @@ void orc_advect(void* h, const double* u, const double* v, double* uo, double* v
 int orc_step(void* h, int nsteps, int* iters) { return ((SolverBase*)h)->step(nsteps, iters); }
 void orc_set_tolerance(void* h, double tol) { ((SolverBase*)h)->set_tol(tol); }
 void orc_set_bc(void* h, const double* u, const double* v, const double* p) { ((SolverBase*)h)->set_bc(u, v, p); }
+void orc_set_scheme(void* h, int scheme) { ((SolverBase*)h)->set_scheme(scheme); }
 void orc_set_fields(void* h, const double* uv, const double* p) { ((SolverBase*)h)->set_fields(uv, p); }
 void orc_get_fields(void* h, double* uv, double* p) { ((SolverBase*)h)->get_fields(uv, p); }
 

@@ -166,6 +166,22 @@ def test_uniform_flow_is_a_steady_state_of_the_step():
     assert np.abs(uv[:nv] - 1).max() < 1e-12 and np.abs(uv[nv:]).max() < 1e-12 and np.abs(p).max() < 1e-12
 
 
+def test_uniform_flow_is_a_steady_state_of_the_explicit_scheme():
+    """The explicit-convection scheme (the reference's NavierStokesAssembly::solve): the convection of a constant
+    velocity is zero (its nodal values are equal, so u_h . grad u_h vanishes) and the stiffness annihilates it, so the
+    tentative increment is zero; the divergence is zero, the pressure stays 0 and the correction is zero."""
+    m = M.cavity(8)
+    m.u_dirichlet = [(g[0], "1", "0.5") for g in m.u_dirichlet]
+    o = oracle.Oracle(m, 0.01, 0.02)
+    o.set_scheme("explicit_convection")
+    nv = m.n_nodes
+    o.set_fields(np.concatenate([np.ones(nv), np.full(nv, 0.5)]), np.zeros(m.n_pressure))
+    st, _ = o.step(3)
+    uv, p = o.fields()
+    assert st == 0
+    assert np.abs(uv[:nv] - 1).max() < 1e-12 and np.abs(uv[nv:] - 0.5).max() < 1e-12 and np.abs(p).max() < 1e-12
+
+
 def test_advection_reproduces_quadratic_fields_exactly():
     """Semi-Lagrangian self-advection of u = y^2, v = x^2 (both in the P2 space): the departure point of node x is
     x - dt (u, v), and P2 interpolation there reproduces the quadratics, so the new fields are (y - dt x^2)^2 and

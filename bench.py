@@ -307,6 +307,19 @@ def pcg_reduced_bytes(n, nz, its, outer, idx=4, resident=False):
     return (outer + 1) * refresh + its * it_bytes
 
 
+def pcg_schur_bytes(n, nzs, its, outer, idx=2, resident=False):
+    """Minimal DRAM bytes of one reduced mixed PCG solve with the Schur complement S formed explicitly (nzs entries
+    over the colour-1 rows, half of the n rows): per iteration S once (FP32 values + idx-byte columns) and FP32
+    vector traffic per row of 18 bytes with the CTA-private state resident (colour-1 rows: S's row sums, own z and p,
+    z and p gathered, p written; the update reads p and 1/L_ii^2 and writes z), 30 without it (q written and read,
+    d and r read and written); plus the FP64 x read and written every FOLD_EVERY iterations.  Per refresh the
+    projection of the colour-0 unknowns and an FP64 residual with the permuted matrix (nz is not needed: its rows
+    are counted as 1.5 products of S's size)."""
+    it_bytes = (4 + idx) * nzs + 4 * (n + 1) + (18 if resident else 30) * n + 16 * n / FOLD_EVERY
+    refresh = 12 * 1.5 * nzs + 8 * (n + 1) + 36 * n
+    return (outer + 1) * refresh + its * it_bytes
+
+
 def pcg_bytes(mixed, n, nz, nzl, its, outer, idx=4, resident=False, fvb=None, reduced=False):
     """Minimal DRAM bytes of one preconditioned solve: per iteration the product with the non-zeros of A and both
     triangular sweeps over the factor's nzl strictly lower entries (values + idx-byte column indices: 2 where the
@@ -415,19 +428,20 @@ def roofline(sim, arm, args):
     that kernel's name."""
     prof = arm["prof"]
     nz = {slot: nonzeros(sim, slot) for slot in (0, 1, 2)}
-    nzl, idx, res, red, fvb = {}, {}, {}, {}, {}
+    nzl, idx, res, red, fvb, nzs = {}, {}, {}, {}, {}, {}
     for slot in (0, 1, 2):
         if sim.precond_kind(slot) != "none":
             nzl[slot] = int(sim.precond_pattern(slot)[1].size)
             idx[slot] = sim.precond_index_bytes(slot)
             form_ = sim.precond_inner_form(slot)
-            res[slot] = form_ in ("resident", "reduced_resident")
-            red[slot] = form_.startswith("reduced")
+            res[slot] = form_.endswith("resident")
+            red[slot] = form_.startswith(("reduced", "schur"))
+            nzs[slot] = sim.precond_schur_nnz(slot) if form_.startswith("schur") else 0
             fvb[slot] = sim.precond_value_bytes(slot)
-    resident, reduced = any(res.values()), any(red.values())
+    resident, reduced, schur = any(res.values()), any(red.values()), any(nzs.values())
+    base = "pcg_mixed_inner_kernel_schur" if schur else "pcg_mixed_inner_kernel_reduced"
     names = {0: "cg_fp64_kernel", 1: "cg_mixed_kernel",
-             2: ("pcg_mixed_inner_kernel_reduced_resident" if resident else "pcg_mixed_inner_kernel_reduced")
-                if reduced else
+             2: (base + "_resident" if resident else base) if reduced else
                 "pcg_mixed_inner_kernel_resident" if resident else "pcg_mixed_inner_kernel_cta1024",
              3: "pcg_fp64_kernel"}
     form = getattr(args, "cg_form", "auto")
@@ -437,7 +451,9 @@ def roofline(sim, arm, args):
                                       prof["ms"]):
         m_, sl = int(m_), int(sl)
         pipe = m_ == 0 and (form == "pipelined" or (form == "auto" and int(n_) < pipe_max))
-        if m_ in (2, 3):
+        if m_ == 2 and nzs.get(sl, 0):
+            b = pcg_schur_bytes(int(n_), nzs[sl], int(i_), int(o_), idx.get(sl, 2), res.get(sl, False))
+        elif m_ in (2, 3):
             b = pcg_bytes(m_ == 2, int(n_), nz[sl], nzl.get(sl, 0), int(i_), int(o_), idx.get(sl, 4) if m_ == 2 else 4,
                           res.get(sl, False) and m_ == 2, fvb.get(sl), red.get(sl, False) and m_ == 2)
         else:
@@ -767,7 +783,7 @@ def main():
                     help="--impl reference: time budget of the timed whole CPU steps")
     ap.add_argument("--cg-form", default="auto", choices=["auto", "three_sync", "pipelined"],
                     help="iteration form of the plain FP64 CG (auto: by system size)")
-    ap.add_argument("--pcg-form", default="auto", choices=["auto", "full", "reduced"],
+    ap.add_argument("--pcg-form", default="auto", choices=["auto", "full", "reduced", "schur"],
                     help="iteration of the mixed PCG on two-colour systems (nsf_set_pcg_form)")
     ap.add_argument("--no-ic0-arm", dest="ic0_arm", action="store_false",
                     help="skip the IC(0) run beside the learned preconditioner")

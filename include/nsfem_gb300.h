@@ -94,15 +94,20 @@ enum nsf_cg_form {
 /* Iteration form of the split mixed PCG on a two-colour system (nsf_set_pcg_form).  The reference preconditions
  * with IC0 under USE_PRECONDITIONING (include/assembly.h:33-35, 1338-1344) and has no reduced form. */
 enum nsf_pcg_form {
-    NSF_PCG_FORM_AUTO = 0,     /* reduced where the system has two colours, else full */
+    NSF_PCG_FORM_AUTO = 0,     /* reduced where the system has two colours, with the Schur complement formed
+                                * explicitly where its 16-bit column copy fits (NSF_PCG_FORM_SCHUR), else full */
     NSF_PCG_FORM_FULL = 1,     /* PCG on the whole permuted system: product, forward and backward colour sweeps */
-    NSF_PCG_FORM_REDUCED = 2   /* two colours only (else full): the colour-0 unknowns are eliminated exactly (their
+    NSF_PCG_FORM_REDUCED = 2,  /* two colours only (else full): the colour-0 unknowns are eliminated exactly (their
                                 * block of a two-colour matrix is diagonal) and PCG runs on the Schur complement with
                                 * the factor's colour-1 diagonal as preconditioner.  With IC(0) these are the full
                                 * form's iterates in exact arithmetic; each iteration reads every matrix row once and
                                 * no factor part (85 against 119 us per iteration on the 2048 cavity's pressure
                                 * system), while its FP32 iterations take about 5 % more of them there (the Schur
-                                * complement's near-constant mode is resolved less well in FP32) */
+                                * complement's near-constant mode is resolved less well in FP32); the product
+                                * S p = A_10 u + A_11 p through u = -A_00^-1 A_01 p, two phases */
+    NSF_PCG_FORM_SCHUR = 3     /* the reduced iteration with S = A_11 - A_10 A_00^-1 A_01 formed once on the host
+                                * (9 entries per row on the structured meshes): one product phase and two grid
+                                * barriers per iteration, the difference form with S's own FP64 row sums */
 };
 
 /* NSF_CG_FORM_AUTO's crossover, from GB300 measurements of both forms on the cavity and channel systems */
@@ -173,8 +178,11 @@ int nsf_precond_value_bytes(nsf_device* h, int slot);
 /* The inner-iteration kernel the slot's last split mixed PCG solve ran: 0 four 256-thread CTAs per SM (one colour),
  * 1 one 1024-thread CTA per SM, 2 the same with the row state only a CTA reads resident in its shared memory (two
  * colours, where it fits), 3 the reduced (Schur complement) iteration of nsf_pcg_form, 4 the same with its
- * CTA-private row state resident in shared memory; -1 before the slot's first such solve. */
+ * CTA-private row state resident in shared memory, 5 and 6 the same two with the Schur complement formed
+ * explicitly; -1 before the slot's first such solve. */
 int nsf_precond_inner_form(nsf_device* h, int slot, int* form);
+/* Entries of the slot's explicitly formed Schur complement (NSF_PCG_FORM_SCHUR; 0 before its first such solve). */
+int nsf_precond_schur_nnz(nsf_device* h, int slot, int64_t* nnz);
 int nsf_precond_clear(nsf_device* h, int slot);
 /* Iterations a preconditioned solve of this slot may take before it falls back (0: the matrix size). */
 int nsf_precond_cap(nsf_device* h, int slot, int maxIterations);

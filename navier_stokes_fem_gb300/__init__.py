@@ -37,7 +37,7 @@ STATUS = {0: "NSF_OK", 1: "NSF_ERR_CUDA", 2: "NSF_ERR_NOT_CONVERGED", 3: "NSF_ER
 SLOT = {"pressure_stiffness": 0, "velocity_mass": 1, "diffusion": 2, "velocity_divergence": 3,
         "pressure_divergence": 4, "velocity_lift": 5, "pressure_lift": 6}
 CG_FORM = {"auto": 0, "three_sync": 1, "pipelined": 2, "multi_kernel": 3}
-PCG_FORM = {"auto": 0, "full": 1, "reduced": 2}
+PCG_FORM = {"auto": 0, "full": 1, "reduced": 2, "schur": 3}
 SOLVER = {"fp64": 0, "mixed": 1, "pcg_mixed": 2, "pcg_fp64": 3}
 PRECOND = {0: "none", 1: "ic0", 2: "learned"}
 
@@ -90,6 +90,7 @@ _SIGS = {
     "nsf_set_solver": (_i, [_v, _i, _d]),
     "nsf_set_cg_form": (_i, [_v, _i]),
     "nsf_set_pcg_form": (_i, [_v, _i]),
+    "nsf_precond_schur_nnz": (_i, [_v, _i, _P(_i64)]),
     "nsf_set_barrier_timeout": (_i, [_v, _d]),
     "nsf_profile": (_i, [_v, _i]),
     "nsf_profile_read": (_i, [_v, _i, _arr(np.int32), _arr(np.int32), _arr(np.int32), _arr(np.int32),
@@ -460,12 +461,19 @@ class GPUSimulationDevice:
             self._check(-k)
         return k
 
+    def precond_schur_nnz(self, slot) -> int:
+        """Entries of the slot's explicitly formed Schur complement (0 before its first reduced solve with it)."""
+        k = _i64()
+        self._check(library().nsf_precond_schur_nnz(self._h, _slot(slot), ctypes.byref(k)))
+        return k.value
+
     def precond_inner_form(self, slot) -> str:
         """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident",
         "reduced", "reduced_resident" or "none" (no such solve yet)."""
         k = _i()
         self._check(library().nsf_precond_inner_form(self._h, _slot(slot), ctypes.byref(k)))
-        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced", 4: "reduced_resident"}[k.value]
+        return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced", 4: "reduced_resident",
+                5: "schur", 6: "schur_resident"}[k.value]
 
     def precond_clear(self, slot):
         self._check(library().nsf_precond_clear(self._h, _slot(slot)))

@@ -354,6 +354,17 @@ int launch_solve(nsf_device* h, int slot, int mode, const double* b, const doubl
     const bool wide = S.maxWidth > kSellChunk;
     if (mode == NSF_SOLVER_PCG_MIXED && !wide) {
         a.f.reduced = use_reduced_pcg(h, S, a.f) ? 1 : 0;
+        // the Schur complement formed explicitly (once per factor) where its 16-bit copy fits
+        if (a.f.reduced && h->pcgForm != NSF_PCG_FORM_REDUCED && factor_schur(h->factors[slot], h->stream)) {
+            const FactorView v = factor_view(h->factors[slot], ws);
+            a.f.schur = 1;
+            a.f.sMaxW = v.sMaxW;
+            a.f.sStart = v.sStart;
+            a.f.sCol16 = v.sCol16;
+            a.f.sColBase = v.sColBase;
+            a.f.sVal32 = v.sVal32;
+            a.f.sRowsum32 = v.sRowsum32;
+        }
         h->innerForm[slot] = pcg_mixed_split_launch(ws, a, h->stream);
     }
     else if (mode == NSF_SOLVER_MIXED && wide)
@@ -1077,9 +1088,18 @@ int nsf_set_solver(nsf_device* h, int mode, double innerTolerance) {
     NSF_END(h)
 }
 
+int nsf_precond_schur_nnz(nsf_device* h, int slot, int64_t* nnz) {
+    NSF_BEGIN(h)
+    check_slot(slot);
+    if (!nnz) throw bad_arg("null output");
+    const Factor& F = h->factors[slot];
+    *nnz = F.hasSchur ? F.S.nnz : 0;
+    NSF_END(h)
+}
+
 int nsf_set_pcg_form(nsf_device* h, int form) {
     NSF_BEGIN(h)
-    if (form < NSF_PCG_FORM_AUTO || form > NSF_PCG_FORM_REDUCED) throw bad_arg("unknown PCG form");
+    if (form < NSF_PCG_FORM_AUTO || form > NSF_PCG_FORM_SCHUR) throw bad_arg("unknown PCG form");
     h->pcgForm = form;
     NSF_END(h)
 }

@@ -119,6 +119,15 @@ __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_re
     team_pcg_mixed_inner_reduced<C16, Resident>(t, a, smem);
 }
 
+// The same iterations with the Schur complement formed explicitly (a.f.schur): one product phase per iteration.
+template <bool Resident = false>
+__global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_schur(CgArgs a) {
+    __shared__ double smem[kSmemSlots];
+    if (a.f.colours != 2 || !a.f.reduced || !a.f.schur || !a.f.sStart) return;   // (the host never launches it otherwise)
+    Team t = Team::grid(a.sync, a.partials, a.timeoutNs);
+    team_pcg_mixed_inner_reduced<true, Resident, true>(t, a, smem);
+}
+
 // The same 1024-thread form with the row state only its CTA reads (the FP32 correction, and r and q of its colour-1
 // rows) in dynamic shared memory for the whole launch: two colours only, and only where that state fits.
 template <bool C16, bool H16 = false>
@@ -289,7 +298,8 @@ void cg_configure(CgWorkspace& ws, int device) {
                                (const void*)pcg_mixed_inner_kernel_resident<true>,
                                (const void*)pcg_mixed_inner_kernel_resident<false>,
                                (const void*)pcg_mixed_inner_kernel_reduced<true, true>,
-                               (const void*)pcg_mixed_inner_kernel_reduced<false, true>}) {
+                               (const void*)pcg_mixed_inner_kernel_reduced<false, true>,
+                               (const void*)pcg_mixed_inner_kernel_schur<true>}) {
             cudaFuncAttributes fa{};
             NSF_CUDA(cudaFuncGetAttributes(&fa, fn));
             const int dyn = optin - (int)fa.sharedSizeBytes;
@@ -376,12 +386,15 @@ int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
         // the CTA-private row state in shared memory where it fits (the same footprint as the full resident form)
         const size_t need = resident_bytes(a.f, ws.gridInner1024);
         const bool res = ws.residentMaxBytes > 0 && need <= ws.residentMaxBytes;
-        const void* inner = res ? (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true, true>
-                                       : (const void*)pcg_mixed_inner_kernel_reduced<false, true>)
-                                : (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true>
-                                       : (const void*)pcg_mixed_inner_kernel_reduced<false>);
+        const void* inner = a.f.schur
+                                ? (res ? (const void*)pcg_mixed_inner_kernel_schur<true>
+                                       : (const void*)pcg_mixed_inner_kernel_schur<false>)
+                            : res ? (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true, true>
+                                         : (const void*)pcg_mixed_inner_kernel_reduced<false, true>)
+                                  : (c16 ? (const void*)pcg_mixed_inner_kernel_reduced<true>
+                                         : (const void*)pcg_mixed_inner_kernel_reduced<false>);
         split_launch(ws, a, (const void*)pcg_mixed_refresh_kernel, kRingBytes, inner, nullptr, s, res ? need : 0);
-        return res ? 4 : 3;
+        return a.f.schur ? (res ? 6 : 5) : res ? 4 : 3;
     }
     // the fused iterations (two or more colours) in the 1024-thread form; 16-bit columns where all three copies exist
     const bool c16 = a.sellCol16 && a.f.loCol16 && a.f.upCol16 && a.f.colours >= 2;

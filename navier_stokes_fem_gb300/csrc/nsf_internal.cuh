@@ -137,6 +137,16 @@ struct FactorView {
     const double* aDiag = nullptr;
     const float* aInv32 = nullptr;
     int reduced = 0;
+    // the Schur complement S = A_11 - A_10 A_00^-1 A_01 formed explicitly (SELL-32 over the permuted rows, colour-0
+    // rows empty; FP32 values, FP64 row sums rounded once, 16-bit columns with the diagonal as padding); schur = 1:
+    // the reduced iteration multiplies by it in one phase instead of forming u_0 first
+    int schur = 0;
+    int sMaxW = 0;
+    const int* sStart = nullptr;
+    const unsigned short* sCol16 = nullptr;
+    const int* sColBase = nullptr;
+    const float* sVal32 = nullptr;
+    const float* sRowsum32 = nullptr;
     double* w = nullptr;                      // work vector: forward-sweep result, then M^-1 r (in place)
     float* w32 = nullptr;
     double* xp = nullptr;                     // the iterate and right-hand side in permuted order
@@ -170,6 +180,8 @@ struct Factor {
     DevBuf<float> loVal32, upVal32, dinv32;
     DevBuf<double> aDiag;                      // diagonal of Ap per permuted row (the reduced iteration)
     DevBuf<float> aInv32;                      // 1 / aDiag in FP32
+    Csr S;                                     // the explicit Schur complement of a two-colour factor (factor_schur)
+    bool schurTried = false, hasSchur = false;
     DevBuf<__half> loVal16, upVal16;           // FP16 copies of the values (see FactorView)
     DevBuf<int> range16;                       // set by factor_fill when a value does not fit FP16's normal range
     bool has16 = false;
@@ -346,6 +358,9 @@ void factor_structure(Factor& F, const Csr& A, cudaStream_t s);
 double factor_ic0(Factor& F, const Csr& A, cudaStream_t s);
 void factor_fill(Factor& F, cudaStream_t s);
 FactorView factor_view(const Factor& F, CgWorkspace& ws);
+// The explicit Schur complement of a two-colour factor's permuted matrix with its SELL copies (once per factor, on the
+// host; synchronises the stream).  False, with nothing kept, where its columns do not fit the 16-bit copy.
+bool factor_schur(Factor& F, cudaStream_t s);
 
 // ------------------------------------------------------------------------------------------------
 // Mesh, point-location tree and simulation state

@@ -846,7 +846,10 @@ static __device__ bool pcg_mixed_refresh_reduced(Team& t, const CgArgs& a, doubl
 // kernel's dynamic shared memory for the whole launch: nsf_row_state holds d1 at [0, n1), r1 at [n1, 2 n1), q1 at
 // [2 n1, 3 n1) and d0 at [3 n1, 3 n1 + n0); d and r are loaded when the launch starts, d is written back when it
 // ends (the refresh recomputes r).)
-template <bool C16 = false, bool Resident = false>
+// (Schur: q_1 = S p_1 in one phase with the explicitly formed Schur complement (FactorView::sStart ..., 16-bit
+// columns, difference form with its FP64 row sums), so H1, its barrier and u_0 fall away; the colour-0 unknowns
+// follow from the refresh's projection alone.)
+template <bool C16 = false, bool Resident = false, bool Schur = false>
 static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem, PcgLoop& L, int& where) {
     const FactorView& F = a.f;
     const int G = t.size, bs = blockDim.x, c1 = F.colourRow[1];
@@ -882,6 +885,7 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         const float* pp = L.flip ? a.p32b : a.p32a;
         float* pc = L.flip ? a.p32a : a.p32b;
         // H1: u_0 (the colour-0 columns of a colour-0 row are its own diagonal only: excluded)
+        if constexpr (!Schur) {
         auto h1 = [&](auto U) {
             sell_rows<float, float, false, 1, decltype(U)::value, TC>(
                 a.sellStart, col, a.sellVal32, a0, a1,
@@ -891,17 +895,27 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         if (a.sellMaxW <= 5) h1(std::integral_constant<int, 5>{});
         else h1(std::integral_constant<int, 6>{});
         if (!t.barrier(where++)) return false;
+        }
         // H2: p_1 and q_1 = S p_1, p.q
         float pqHi = 0.f, pqLo = 0.f;
-        auto g2 = [&](int c) { return c >= c1 ? fmaf(betaf, pp[c], w[c]) : pc[c]; };
         auto e2 = [&](int row, float acc, float pi) {
             pc[row] = pi;
             if constexpr (Resident) sq1[row - b0] = acc;
             else a.q32[row] = acc;
             df_acc(pqHi, pqLo, pi, acc);
         };
-        if (a.sellMaxW <= 5) product32<false, 5, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
-        else product32<false, 6, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
+        if constexpr (Schur) {
+            // every column of S is a colour-1 unknown: p_j = z_j + beta p_j on the fly
+            auto gs = [&](int c) { return fmaf(betaf, pp[c], w[c]); };
+            auto pre = [&](int row) { return DiffPre<float>{gs(row), F.sRowsum32[row]}; };
+            auto fin = [&](int row, float acc, const DiffPre<float>& q) { e2(row, fmaf(q.rs, q.self, acc), q.self); };
+            sell_rows<float, float, true, 1, 9, unsigned short>(F.sStart, F.sCol16, F.sVal32, b0, b1, gs, pre, fin,
+                                                                 F.sColBase);
+        } else {
+            auto g2 = [&](int c) { return c >= c1 ? fmaf(betaf, pp[c], w[c]) : pc[c]; };
+            if (a.sellMaxW <= 5) product32<false, 5, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
+            else product32<false, 6, C16>(nullptr, a, b0, b1, nullptr, g2, e2);
+        }
         const double pq = block_sum_df(pqHi, pqLo, smem);
         if (threadIdx.x == 0) a.partials[t.rank] = pq;
         if (!t.barrier(where++)) return false;
@@ -918,9 +932,11 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
         const bool fold = fold_iteration(L);
         // U, colour-0 rows: d_0 += alpha u_0, so that x_0 follows the directions q_1 was formed with (the rounded
         // u_0), not their exact projection; the refresh then finds the residual the recurrence carries
-        for (int i = a0 + (int)threadIdx.x; i < a1; i += bs) {
-            if constexpr (Resident) sd0[i - a0] = fold_correction(a, i, fmaf(alphaf, pc[i], sd0[i - a0]), fold, invScale);
-            else a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
+        if constexpr (!Schur) {
+            for (int i = a0 + (int)threadIdx.x; i < a1; i += bs) {
+                if constexpr (Resident) sd0[i - a0] = fold_correction(a, i, fmaf(alphaf, pc[i], sd0[i - a0]), fold, invScale);
+                else a.d32[i] = fold_correction(a, i, fmaf(alphaf, pc[i], a.d32[i]), fold, invScale);
+            }
         }
         // U: colour-1 rows
         float rrHi = 0.f, rrLo = 0.f;
@@ -1096,7 +1112,7 @@ static __device__ void team_pcg_mixed_refresh(Team& t, const CgArgs& a, double* 
 }
 
 // The reduced form's inner launch (two colours, a SELL copy and a.f.reduced; see pcg_mixed_inner_reduced).
-template <bool C16 = false, bool Resident = false>
+template <bool C16 = false, bool Resident = false, bool Schur = false>
 static __device__ void team_pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double* smem) {
     int where = 400;
     const PcgLoop& G = *a.loop;
@@ -1110,7 +1126,7 @@ static __device__ void team_pcg_mixed_inner_reduced(Team& t, const CgArgs& a, do
     L.itRef = G.itRef;
     L.flip = G.flip;
     L.rflip = G.rflip;
-    const bool ok = pcg_mixed_inner_reduced<C16, Resident>(t, a, smem, L, where);
+    const bool ok = pcg_mixed_inner_reduced<C16, Resident, Schur>(t, a, smem, L, where);
     if (!ok) write_info(t, a, L.it, NSF_ERR_BARRIER_TIMEOUT, G.refresh, G.rr64, G.bb);
     if (t.rank == 0 && threadIdx.x == 0) {
         a.loop->rz = L.rz;

@@ -14,6 +14,8 @@
 #include <queue>
 #include <tuple>
 #include <vector>
+#include <thread>
+#include <atomic>
 
 #include "nsf_internal.cuh"
 
@@ -424,6 +426,84 @@ double factor_ic0(Factor& F, const Csr& A, cudaStream_t s) {
     throw Error{NSF_ERR_BREAKDOWN, "incomplete Cholesky broke down even with a diagonal shift of 1e4"};
 }
 
+// S = A_11 - A_10 A_00^-1 A_01 over the colour-1 rows of the permuted matrix, in FP64 on the host (rows in parallel):
+// row i holds a_ii, its colour-1 entries, and -a_ij a_jk / a_jj for every colour-0 neighbour j and colour-1
+// neighbour k of j, columns ascending.  Colour-0 rows are left empty.
+bool factor_schur(Factor& F, cudaStream_t s) {
+    if (F.schurTried) return F.hasSchur;
+    F.schurTried = true;
+    if (F.colours != 2) return false;
+    const Csr& A = F.Ap;
+    const int n = A.rows, c1 = F.colourRow[1], c2 = F.colourRow[2];
+    std::vector<int> rp((size_t)n + 1), ci((size_t)A.nnz);
+    std::vector<double> av((size_t)A.nnz);
+    NSF_CUDA(cudaMemcpyAsync(rp.data(), A.rowptr.get(), sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s));
+    NSF_CUDA(cudaMemcpyAsync(ci.data(), A.col.get(), sizeof(int) * ci.size(), cudaMemcpyDeviceToHost, s));
+    NSF_CUDA(cudaMemcpyAsync(av.data(), A.val.get(), sizeof(double) * av.size(), cudaMemcpyDeviceToHost, s));
+    NSF_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> diag((size_t)c1, 0.0);
+    for (int j = 0; j < c1; ++j)
+        for (int k = rp[j]; k < rp[j + 1]; ++k)
+            if (ci[k] == j) diag[j] = av[k];
+    const int rows = c2 - c1;
+    std::vector<std::vector<std::pair<int, double>>> srow((size_t)rows);
+    const int threads = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    std::atomic<int> bad{0};
+    for (int w = 0; w < threads; ++w)
+        pool.emplace_back([&, w] {
+            std::vector<std::pair<int, double>> acc;
+            for (int r = w; r < rows; r += threads) {
+                const int i = c1 + r;
+                acc.clear();
+                auto add = [&](int c, double v) {
+                    for (auto& e : acc)
+                        if (e.first == c) { e.second += v; return; }
+                    acc.push_back({c, v});
+                };
+                for (int q = rp[i]; q < rp[i + 1]; ++q) {
+                    const int j = ci[q];
+                    if (j >= c1) { add(j, av[q]); continue; }
+                    if (diag[j] == 0.0) { bad = 1; continue; }
+                    const double f = av[q] / diag[j];
+                    for (int t = rp[j]; t < rp[j + 1]; ++t)
+                        if (ci[t] >= c1) add(ci[t], -f * av[t]);
+                }
+                std::sort(acc.begin(), acc.end());
+                srow[r] = acc;
+            }
+        });
+    for (auto& t : pool) t.join();
+    if (bad) return false;
+    std::vector<int> sp((size_t)n + 1, 0), sc;
+    std::vector<double> sv;
+    for (int r = 0; r < rows; ++r) sp[(size_t)c1 + r + 1] = (int)srow[r].size();
+    for (int i = 0; i < n; ++i) sp[i + 1] += sp[i];
+    sc.reserve((size_t)sp[n]);
+    sv.reserve((size_t)sp[n]);
+    for (int r = 0; r < rows; ++r)
+        for (const auto& e : srow[r]) {
+            sc.push_back(e.first);
+            sv.push_back(e.second);
+        }
+    Csr& S = F.S;
+    S.rows = S.cols = n;
+    S.nnz = (int64_t)sc.size();
+    S.rowptr.upload(sp.data(), sp.size(), s);
+    S.col.upload(sc.data(), sc.size(), s);
+    S.val.upload(sv.data(), sv.size(), s);
+    S.values_changed();
+    prepare_matrix(S, true, s);
+    prepare_col16(S, s);
+    NSF_CUDA(cudaStreamSynchronize(s));
+    if (!S.hasCol16) {
+        F.S = Csr();
+        return false;
+    }
+    F.hasSchur = true;
+    return true;
+}
+
 FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     FactorView v;
     v.colours = F.colours;
@@ -452,6 +532,14 @@ FactorView factor_view(const Factor& F, CgWorkspace& ws) {
     v.dinv32 = F.dinv32.get();
     v.aDiag = F.aDiag.get();
     v.aInv32 = F.aInv32.get();
+    if (F.hasSchur) {
+        v.sMaxW = F.S.maxWidth;
+        v.sStart = F.S.sellStart.get();
+        v.sCol16 = F.S.sellCol16.get();
+        v.sColBase = F.S.sellColBase.get();
+        v.sVal32 = F.S.sellVal32.get();
+        v.sRowsum32 = F.S.rowsum32.get();
+    }
     v.w = ws.w.get();
     v.w32 = ws.w32.get();
     v.xp = ws.xp.get();

@@ -80,3 +80,12 @@ def test_plain_cg_bytes_match_the_per_unit_figures():
     pipe = bench.algorithmic_bytes(0, n, nnz, 1, 1, True) - bench.algorithmic_bytes(0, n, nnz, 0, 1, True)
     assert pipe == 12 * nnz + 4 * (n + 1) + 104 * n        # the pipelined form: 13 vector passes
     assert bench.header_constant("NSF_CG_PIPELINED_MAX_ROWS") > 0
+
+
+def test_schur_form_bytes_per_iteration():
+    """The explicit Schur complement form reads S once (FP32 values, 16-bit columns) and 18 vector bytes per row with
+    its row state resident (30 without), plus the correction fold's FP64 x every FOLD_EVERY iterations."""
+    n, nzs = 1000, 4500
+    for resident, vec in ((True, 18), (False, 30)):
+        per_it = bench.pcg_schur_bytes(n, nzs, 1, 0, 2, resident) - bench.pcg_schur_bytes(n, nzs, 0, 0, 2, resident)
+        assert per_it == 6 * nzs + 4 * (n + 1) + vec * n + 16 * n / bench.FOLD_EVERY

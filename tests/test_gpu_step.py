@@ -1,5 +1,7 @@
 """Whole operator-split steps resident on the GPU against the FP64 oracle (the restated reference path):
 velocity and pressure within 1e-6 relative L2 after N steps, CG iteration counts within a few per solve."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -267,3 +269,27 @@ def test_state_errors():
         d._check(st)
     assert e.value.status == 6
     d.close()
+
+
+def test_new_entry_points_reject_bad_arguments():
+    """Time-dependent boundary data, scheme and solver forms: malformed or out-of-range arguments are statuses, and
+    the handle keeps working after them."""
+    m = M.cavity(8)
+    sim = nsf.NavierStokesAssembly(m, 0.01, 0.01)
+    lib = nsf.library()
+    n_u = sum(len(g[0]) for g in m.u_dirichlet)
+    n_p = sum(len(g[0]) for g in m.p_dirichlet)
+    idx_u = np.zeros(n_u, np.int32)
+    idx_p = np.zeros(n_p, np.int32)
+    for exprs, iu in ((["1+"], idx_u), (["z*2"], idx_u), (["1", "t"], idx_u + 2)):
+        arr = (ctypes.c_char_p * len(exprs))(*[e.encode() for e in exprs])
+        st = lib.nsf_sim_set_bc_expressions(sim.handle, len(exprs), ctypes.cast(arr, ctypes.c_void_p),
+                                            iu.ctypes.data_as(ctypes.c_void_p), iu.ctypes.data_as(ctypes.c_void_p),
+                                            idx_p.ctypes.data_as(ctypes.c_void_p), 0.0)
+        assert st == 5, exprs
+    assert lib.nsf_sim_set_scheme(sim.handle, 7) == 5
+    assert lib.nsf_set_pcg_form(sim.handle, 9) == 5
+    assert lib.nsf_set_cg_form(sim.handle, 9) == 5
+    it = sim.step(2)                                                 # still usable
+    assert it.shape == (2, 5) and sim.time() == 2 * 0.01
+    sim.close()

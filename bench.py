@@ -310,12 +310,12 @@ def pcg_reduced_bytes(n, nz, its, outer, idx=4, resident=False):
 def pcg_schur_bytes(n, nzs, its, outer, idx=2, resident=False):
     """Minimal DRAM bytes of one reduced mixed PCG solve with the Schur complement S formed explicitly (nzs entries
     over the colour-1 rows, half of the n rows): per iteration S once (FP32 values + idx-byte columns) and FP32
-    vector traffic per row of 18 bytes with the CTA-private state resident (colour-1 rows: S's row sums, own z and p,
-    z and p gathered, p written; the update reads p and 1/L_ii^2 and writes z), 30 without it (q written and read,
-    d and r read and written); plus the FP64 x read and written every FOLD_EVERY iterations.  Per refresh the
+    vector traffic per row of 16 bytes with the CTA-private state resident (colour-1 rows: S's row sums, own z and p,
+    z and p gathered, p written; the update reads p and writes z; q, d, r and 1/L_ii in shared memory), 30 without
+    it (q written and read, d and r read and written, 1/L_ii read); plus the FP64 x read and written every FOLD_EVERY iterations.  Per refresh the
     projection of the colour-0 unknowns and an FP64 residual with the permuted matrix (nz is not needed: its rows
     are counted as 1.5 products of S's size)."""
-    it_bytes = (4 + idx) * nzs + 4 * (n + 1) + (18 if resident else 30) * n + 16 * n / FOLD_EVERY
+    it_bytes = (4 + idx) * nzs + 4 * (n + 1) + (16 if resident else 30) * n + 16 * n / FOLD_EVERY
     refresh = 12 * 1.5 * nzs + 8 * (n + 1) + 36 * n
     return (outer + 1) * refresh + its * it_bytes
 

@@ -140,6 +140,11 @@ __global__ void __launch_bounds__(kInnerCtaThreads, 1) pcg_mixed_inner_kernel_re
 
 // Shared-memory bytes pcg_mixed_inner_kernel_resident needs on `grid` CTAs for a factor's colour blocks: per CTA
 // its share of each block (team_block's rule) as d, plus r and q of its colour-1 share.
+static size_t resident_bytes_schur(const FactorView& f, int grid) {
+    const int slices = (f.colourRow[2] - f.colourRow[1]) / kSlice;
+    return sizeof(float) * 4 * (size_t)((slices + grid - 1) / grid) * kSlice;
+}
+
 static size_t resident_bytes(const FactorView& f, int grid) {
     auto share = [&](int c) {
         const int slices = (f.colourRow[c + 1] - f.colourRow[c]) / kSlice;
@@ -383,8 +388,9 @@ void cg_mixed_split_launch(CgWorkspace& ws, const CgArgs& a, cudaStream_t s) {
 int pcg_mixed_split_launch(CgWorkspace& ws, CgArgs a, cudaStream_t s) {
     if (a.f.reduced) {   // the reduced iterations: two colours and a SELL copy, checked by the caller
         const bool c16 = a.sellCol16 != nullptr;
-        // the CTA-private row state in shared memory where it fits (the same footprint as the full resident form)
-        const size_t need = resident_bytes(a.f, ws.gridInner1024);
+        // the CTA-private row state in shared memory where it fits (the full resident form's footprint; the Schur
+        // form keeps four vectors of its colour-1 share: d, r, q and 1 / L_11)
+        const size_t need = a.f.schur ? resident_bytes_schur(a.f, ws.gridInner1024) : resident_bytes(a.f, ws.gridInner1024);
         const bool res = ws.residentMaxBytes > 0 && need <= ws.residentMaxBytes;
         const void* inner = a.f.schur
                                 ? (res ? (const void*)pcg_mixed_inner_kernel_schur<true>

@@ -869,12 +869,17 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
     float* sr1 = nsf_row_state + n1;
     float* sq1 = nsf_row_state + 2 * n1;
     float* sd0 = nsf_row_state + 3 * n1;
+    // (Schur, Resident: the colour-0 correction is not kept, and 1 / L_11 of the CTA's colour-1 rows takes its place
+    // in shared memory, [3 n1, 4 n1))
+    float* sv1 = nsf_row_state + 3 * n1;
     if constexpr (Resident) {
         for (int k = threadIdx.x; k < n1; k += bs) {
             sd1[k] = a.d32[b0 + k];
             sr1[k] = r[b0 + k];
+            if constexpr (Schur) sv1[k] = dinv[b0 + k];
         }
-        for (int k = threadIdx.x; k < n0; k += bs) sd0[k] = a.d32[a0 + k];
+        if constexpr (!Schur)
+            for (int k = threadIdx.x; k < n0; k += bs) sd0[k] = a.d32[a0 + k];
         __syncthreads();
     }
     L.innerBreakdown = 0;
@@ -957,7 +962,8 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
                         di[u] = a.d32[i];
                         ri[u] = r[i];
                     }
-                    vi[u] = dinv[i];
+                    if constexpr (Resident && Schur) vi[u] = sv1[i - b0];
+                    else vi[u] = dinv[i];
                 }
             }
 #pragma unroll
@@ -1002,7 +1008,8 @@ static __device__ bool pcg_mixed_inner_reduced(Team& t, const CgArgs& a, double*
     if constexpr (Resident) {   // d of every own row back to its global copy (the refresh folds it into x)
         __syncthreads();
         for (int k = threadIdx.x; k < n1; k += bs) a.d32[b0 + k] = sd1[k];
-        for (int k = threadIdx.x; k < n0; k += bs) a.d32[a0 + k] = sd0[k];
+        if constexpr (!Schur)
+            for (int k = threadIdx.x; k < n0; k += bs) a.d32[a0 + k] = sd0[k];
     }
     L.state = kLoopRefresh;
     return true;

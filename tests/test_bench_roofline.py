@@ -84,8 +84,8 @@ def test_plain_cg_bytes_match_the_per_unit_figures():
 
 def test_schur_form_bytes_per_iteration():
     """The explicit Schur complement form reads S once (FP32 values, 16-bit columns) and 18 vector bytes per row with
-    its row state resident (30 without), plus the correction fold's FP64 x every FOLD_EVERY iterations."""
+    its row state resident (16 bytes: 1/L_ii kept there too; 30 without), plus the correction fold's FP64 x every FOLD_EVERY iterations."""
     n, nzs = 1000, 4500
-    for resident, vec in ((True, 18), (False, 30)):
+    for resident, vec in ((True, 16), (False, 30)):
         per_it = bench.pcg_schur_bytes(n, nzs, 1, 0, 2, resident) - bench.pcg_schur_bytes(n, nzs, 0, 0, 2, resident)
         assert per_it == 6 * nzs + 4 * (n + 1) + vec * n + 16 * n / bench.FOLD_EVERY

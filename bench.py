@@ -412,12 +412,12 @@ def nonzeros(sim, slot):
 # DRAM traffic per row and iteration of the solver kernels, each from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum of a launch that ran a known number of iterations on the 2048 cavity's pressure system,
 # 4,198,401 rows, whose vectors exceed L2): the reduced inner kernel with the Schur complement formed explicitly and
-# its row state in shared memory 4.59 GB over 40 iterations; the reduced inner kernel forming u_0 (row state in
+# its row state (and 1 / L_11) in shared memory 4.57 GB over 40 iterations; the reduced inner kernel forming u_0 (row state in
 # shared memory) 5.53 GB over 40 iterations; the full-form resident inner kernel (row state in shared memory,
 # 16-bit column copies, FP16 factor values) 11.01 GB over 40 iterations; the 1024-thread inner kernel without the
 # resident state (16-bit column copies, FP32 factor values) 17.49 GB over 40 iterations; cg_fp64_kernel 30.67 GB
 # over 60 iterations (its prologue included).
-DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_schur_resident": 27.3,
+DRAM_BYTES_PER_ROW_ITERATION = {"pcg_mixed_inner_kernel_schur_resident": 27.2,
                                 "pcg_mixed_inner_kernel_reduced_resident": 32.9,
                                 "pcg_mixed_inner_kernel_resident": 65.5, "pcg_mixed_inner_kernel_cta1024": 104.1,
                                 "cg_fp64_kernel": 121.7}

@@ -95,3 +95,49 @@ def test_two_colour_pattern_caps_the_black_diagonal():
         F.set(lo0, d)
         _, it, _, st = F.pcg(b, np.zeros_like(b))
         assert st == 0 and abs(it - it0) <= max(2, it0 // 50), (omega, it, it0)
+
+
+def test_two_colour_ic0_pcg_is_jacobi_pcg_on_the_schur_complement():
+    """The reduced iteration's premise, in FP64: on two colours (the colour-0 block A_00 diagonal), IC(0)-PCG on A from
+    an initial guess whose colour-0 rows are projected (x_0 = A_00^-1 (b_0 - A_01 x_1), so r_0 = 0) runs the iterates of
+    PCG on the Schur complement S = A_11 - A_10 A_00^-1 A_01 with the factor's colour-1 diagonal L_11^2 = diag S as
+    preconditioner: the same iteration count, and the same solution after the colour-0 unknowns are recovered."""
+    A = _system(32)
+    F = oracle.McFactor(A)
+    assert F.colours == 2
+    F.ic0()
+    c0, c1 = np.flatnonzero(F.colour == 0), np.flatnonzero(F.colour == 1)
+    A00, A01 = A[c0][:, c0].tocsr(), A[c0][:, c1].tocsr()
+    A10, A11 = A[c1][:, c0].tocsr(), A[c1][:, c1].tocsr()
+    assert (A00 - sp.diags(A00.diagonal())).nnz == 0                    # the colour-0 block is diagonal
+    d0 = A00.diagonal()
+    S = (A11 - A10 @ sp.diags(1.0 / d0) @ A01).tocsr()
+    assert np.allclose(F.diag[c1] ** 2, S.diagonal(), rtol=1e-12)       # IC(0)'s colour-1 diagonal is diag S
+    b = A @ np.random.default_rng(9).standard_normal(A.shape[0])
+    tol = 1e-10
+    x0 = np.zeros(A.shape[0])
+    x0[c0] = b[c0] / d0                                                 # projected start: r_0 = 0
+    x, it_full, _, st = F.pcg(b, x0, tol=tol)
+    assert st == 0
+    # PCG on S with diag S, stopping on the full residual's norm (equal to the Schur residual's when r_0 = 0)
+    bS = b[c1] - A10 @ (b[c0] / d0)
+    y = np.zeros(len(c1))
+    r = bS.copy()
+    z = r / S.diagonal()
+    p = z.copy()
+    rz = r @ z
+    it_schur = 0
+    while np.linalg.norm(r) > tol * np.linalg.norm(b):
+        q = S @ p
+        alpha = rz / (p @ q)
+        y += alpha * p
+        r -= alpha * q
+        z = r / S.diagonal()
+        rz, rz_old = r @ z, rz
+        p = z + (rz / rz_old) * p
+        it_schur += 1
+    assert it_schur == it_full, (it_schur, it_full)
+    xs = np.zeros_like(x)
+    xs[c1] = y
+    xs[c0] = (b[c0] - A01 @ y) / d0
+    assert np.linalg.norm(xs - x) <= 1e-8 * np.linalg.norm(x)

@@ -107,6 +107,7 @@ def lib():
         L.orc_set_tolerance.argtypes = [_p, _d]
         L.orc_set_bc.argtypes = [_p, _dptr, _dptr, _dptr]
         L.orc_set_scheme.argtypes = [_p, _i]
+        L.orc_local_convection.argtypes = [_i, _i, _fptr, _dptr, _dptr]
         L.orc_point_in_triangle.restype = _i
         L.orc_point_in_triangle.argtypes = [_fptr, _fptr, _fptr]
         _u8ptr = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
@@ -399,6 +400,28 @@ def local_matrices(vertices, real_bits: int = 64):
     n = v.shape[0]
     out = {k: np.zeros((n,) + s) for k, s in LOCAL_MATRIX_SHAPES.items()}
     lib().orc_local_matrices(int(real_bits), n, v.reshape(-1), *[out[k].reshape(-1) for k in LOCAL_MATRIX_SHAPES])
+    return out
+
+
+def local_convection(vertices, velocities, real_bits: int = 64):
+    """The oracle's local convection matrices [n, 6, 6] of triangles ([n, 6] float32 vertices) with nodal velocities
+    [n, 12] (u0..u5, v0..v5), in float (real_bits 32) or double."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 6)
+    u = np.ascontiguousarray(velocities, np.float64).reshape(-1, 12)
+    out = np.zeros((v.shape[0], 6, 6))
+    lib().orc_local_convection(int(real_bits), v.shape[0], v.reshape(-1), u.reshape(-1), out.reshape(-1))
+    return out
+
+
+def ref_local_convection(vertices, velocities):
+    """The same from the reference's own convection functor (`make ref-assembly`), in float."""
+    path = os.path.join(_HERE, "_ref", "libref_assembly.so")
+    L = ctypes.CDLL(path)
+    L.ref_local_convection.argtypes = [_i, _fptr, _fptr, _fptr]
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 6)
+    u = np.ascontiguousarray(velocities, np.float32).reshape(-1, 12)
+    out = np.zeros((v.shape[0], 6, 6), np.float32)
+    L.ref_local_convection(v.shape[0], v.reshape(-1), u.reshape(-1), out.reshape(-1))
     return out
 
 

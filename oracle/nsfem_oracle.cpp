@@ -134,9 +134,11 @@ template <typename R, int n, int ld> static void local_stiffness(const R* xy, co
         }
 }
 
-// Local convection matrix of NavierStokesAssembly::assembleConvectionMatrix (include/assembly.h:1581-1625): the
-// integrand psi^T psi U B dpsi times the sign of the Jacobian (U: the element's 6 x 2 nodal velocities), summed
-// over the quadrature points with their weights; evaluated here as psi_i ((psi U) B dpsi)_j.
+// Local convection matrix of NavierStokesAssembly::assembleConvectionMatrix (include/assembly.h:1584-1622): at each
+// quadrature point the integrand (psi^T psi U B dpsi) sign, U the element's 6 x 2 nodal velocities, evaluated left
+// to right as the reference's StaticMatrix products do (each entry summed from zero over the inner index in order),
+// then added with its weight (TriangleIntegrator::integrate), so that the float instantiation reproduces the
+// reference's arithmetic.
 template <typename R> static void local_convection(const R* xy, const R vel[6][2], R out[6][6]) {
     R B[2][2], det;
     diff_operator(xy, det, B);
@@ -148,11 +150,28 @@ template <typename R> static void local_convection(const R* xy, const R vel[6][2
         R psi[6], dxi[6], deta[6];
         p2_eval(q.x[k], q.y[k], psi);
         p2_del(q.x[k], q.y[k], dxi, deta);
-        R uh = 0, vh = 0;
-        for (int m = 0; m < 6; ++m) { uh += psi[m] * vel[m][0]; vh += psi[m] * vel[m][1]; }
-        const R g0 = uh * B[0][0] + vh * B[1][0], g1 = uh * B[0][1] + vh * B[1][1];
+        R t1[6][6], t2[6][2], t3[6][2];
         for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) out[i][j] += (psi[i] * (g0 * dxi[j] + g1 * deta[j]) * sign) * q.w[k];
+            for (int j = 0; j < 6; ++j) t1[i][j] = R(0) + psi[i] * psi[j];          // psi^T psi
+        for (int i = 0; i < 6; ++i)
+            for (int c = 0; c < 2; ++c) {                                          // (psi^T psi) U
+                R a = 0;
+                for (int m = 0; m < 6; ++m) a += t1[i][m] * vel[m][c];
+                t2[i][c] = a;
+            }
+        for (int i = 0; i < 6; ++i)
+            for (int c = 0; c < 2; ++c) {                                          // ... B
+                R a = 0;
+                for (int m = 0; m < 2; ++m) a += t2[i][m] * B[m][c];
+                t3[i][c] = a;
+            }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {                                          // ... dpsi, sign, weight
+                R a = 0;
+                a += t3[i][0] * dxi[j];
+                a += t3[i][1] * deta[j];
+                out[i][j] += (a * sign) * q.w[k];
+            }
     }
 }
 
@@ -897,6 +916,25 @@ int orc_step(void* h, int nsteps, int* iters) { return ((SolverBase*)h)->step(ns
 void orc_set_tolerance(void* h, double tol) { ((SolverBase*)h)->set_tol(tol); }
 void orc_set_bc(void* h, const double* u, const double* v, const double* p) { ((SolverBase*)h)->set_bc(u, v, p); }
 void orc_set_scheme(void* h, int scheme) { ((SolverBase*)h)->set_scheme(scheme); }
+// The oracle's local convection matrices of `n` triangles (vertices x0 y0 .. x2 y2, velocities u0..u5 v0..v5), in
+// float (realBits 32, the reference's arithmetic) or double; row-major 6 x 6 per triangle.
+void orc_local_convection(int realBits, int n, const float* v, const double* vel, double* out) {
+    for (int e = 0; e < n; ++e) {
+        if (realBits == 32) {
+            float xy[12] = {}, u[6][2], c[6][6];
+            for (int k = 0; k < 6; ++k) xy[k] = v[6 * e + k];
+            for (int k = 0; k < 6; ++k) { u[k][0] = (float)vel[12 * e + k]; u[k][1] = (float)vel[12 * e + 6 + k]; }
+            local_convection(xy, u, c);
+            for (int k = 0; k < 36; ++k) out[36 * e + k] = c[k / 6][k % 6];
+        } else {
+            double xy[12] = {}, u[6][2], c[6][6];
+            for (int k = 0; k < 6; ++k) xy[k] = v[6 * e + k];
+            for (int k = 0; k < 6; ++k) { u[k][0] = vel[12 * e + k]; u[k][1] = vel[12 * e + 6 + k]; }
+            local_convection(xy, u, c);
+            for (int k = 0; k < 36; ++k) out[36 * e + k] = c[k / 6][k % 6];
+        }
+    }
+}
 void orc_set_fields(void* h, const double* uv, const double* p) { ((SolverBase*)h)->set_fields(uv, p); }
 void orc_get_fields(void* h, double* uv, double* p) { ((SolverBase*)h)->get_fields(uv, p); }
 

@@ -1,8 +1,9 @@
 // ORACLE (reference build) — test infrastructure only.
 // The reference's OWN element arithmetic, compiled from its lines: the P1/P2 shape functions, the Jacobian and
 // differential operator and the 7-point TriangleIntegrator (include/assembly.h:98-304), and the local mass,
-// stiffness and divergence functors (include/assembly.h:725-882).  oracle/Makefile (`make ref-assembly`) copies
-// those two line ranges verbatim into the git-ignored build folder _ref/ (checking the first and last line of
+// stiffness and divergence functors (include/assembly.h:725-882), and the convection functor of
+// assembleConvectionMatrix (include/assembly.h:1584-1622).  oracle/Makefile (`make ref-assembly`) copies
+// those line ranges verbatim into the git-ignored build folder _ref/ (checking the first and last line of
 // each range) and this file includes them.  The functors are member templates of NavierStokesAssembly<P2, P1>,
 // whose other members need the absent sparse_matrix_math submodule, TBB, OpenCV and nlohmann_json; here they sit
 // inside ElementFunctors<VelocityShape, PressureShape>, a class template of this file that provides only the two
@@ -24,6 +25,23 @@ struct ElementFunctors {
 };
 
 using Functors = ElementFunctors<P2, P1>;
+
+// The convection functor of NavierStokesAssembly::assembleConvectionMatrix (include/assembly.h:1584-1622, copied by
+// `make ref-assembly` into _ref/assembly_convection.inc): a lambda over the member `currentVelocitySolution` and
+// `grid.getNodesCount()`, which this class provides for one element whose six velocities sit at indexes 0..5 (u)
+// and 6..11 (v).
+template <typename VelocityShape>
+struct ConvectionHost {
+    struct Grid {
+        int getNodesCount() const { return 6; }
+    } grid;
+    real currentVelocitySolution[12];
+    void local(const real* elementNodes, StaticMatrix<real, VelocityShape::size, VelocityShape::size>& out) {
+#include "assembly_convection.inc"
+        const int indexes[6] = {0, 1, 2, 3, 4, 5};
+        localConvection(indexes, elementNodes, out);
+    }
+};
 
 }  // namespace NSFem
 
@@ -75,6 +93,21 @@ void ref_local_matrices(int n, const float* vertices, float* mass, float* stiffV
         fdp(unusedIndexes, nodes, gx, gy);
         store(gx, 6, 3, divPx + 18 * e);
         store(gy, 6, 3, divPy + 18 * e);
+    }
+}
+
+// The local convection matrix (6x6, row-major) of `n` triangles with the nodal velocities vel (per triangle u0..u5,
+// v0..v5), as the reference's assembleConvectionMatrix computes it in float.
+void ref_local_convection(int n, const float* vertices, const float* vel, float* conv) {
+    using namespace NSFem;
+    ConvectionHost<P2> host;
+    for (int e = 0; e < n; ++e) {
+        real nodes[12] = {};
+        for (int k = 0; k < 6; ++k) nodes[k] = vertices[6 * e + k];
+        for (int k = 0; k < 12; ++k) host.currentVelocitySolution[k] = vel[12 * e + k];
+        StaticMatrix<real, 6, 6> c;
+        host.local(nodes, c);
+        store(c, 6, 6, conv + 36 * e);
     }
 }
 

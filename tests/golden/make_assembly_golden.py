@@ -1,7 +1,8 @@
 """Writes the element-matrix fixture from the reference's OWN element code.
 
 `make -C oracle ref-assembly` compiles the reference's shape functions, quadrature, Jacobian and local mass /
-stiffness / divergence functors (include/assembly.h:98-304 and 725-882) from its own lines into
+stiffness / divergence functors (include/assembly.h:98-304 and 725-882) and the convection functor of
+assembleConvectionMatrix (include/assembly.h:1584-1622) from its own lines into
 oracle/_ref/libref_assembly.so.  This script evaluates them, in the reference's float arithmetic, on the triangles of
 the reference's assets/mesh_small.json, a perturbed 12 x 12 cavity, the 8 x 8 cavity and 256 seeded random
 counter-clockwise triangles, and stores vertices and matrices so that the oracle's restatement can be checked where
@@ -48,6 +49,10 @@ def main():
     ref = oracle.ref_local_matrices(v)
     out = {"vertices": v, "sources": np.array([len(x) for x in verts])}
     out.update({k: a for k, a in ref.items()})
+    # the convection functor of assembleConvectionMatrix, with seeded nodal velocities per triangle
+    vel = np.random.default_rng(11).standard_normal((len(v), 12)).astype(np.float32)
+    out["velocities"] = vel
+    out["convection"] = oracle.ref_local_convection(v, vel)
     np.savez_compressed(OUT, **out)
     print(len(v), "triangles")
 

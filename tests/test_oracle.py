@@ -376,6 +376,44 @@ def test_local_matrices_match_reference_element_code():
         assert (np.abs(o64[k] - ref) <= 1e-5 * scale).all(), k
 
 
+def test_local_convection_matches_reference_element_code():
+    """The oracle's local convection matrices (the explicit-convection scheme's C(u)) against the reference's own
+    convection functor of assembleConvectionMatrix (include/assembly.h:1584-1622, compiled from its lines) on the
+    fixture's 996 triangles with seeded nodal velocities: bit-identical in the reference's float arithmetic, the FP64
+    oracle within float rounding.  Known answers in FP64: the rows sum to zero (the shape-function gradients sum to
+    zero), and for a constant velocity (a, b) and a linear field c x + d y the product is (a c + b d) times the local
+    mass row sums (the integrand is psi_i times a constant, integrated exactly)."""
+    g = _assembly_fixture()
+    v, vel = g["vertices"], g["velocities"]
+    o32 = oracle.local_convection(v, vel, 32)
+    o64 = oracle.local_convection(v, vel, 64)
+    ref = g["convection"].astype(np.float64)
+    assert np.array_equal(o32, ref)
+    scale = np.abs(o64).max(axis=(1, 2), keepdims=True)
+    assert (np.abs(o64 - ref) <= 1e-5 * scale).all()
+    assert (np.abs(o64.sum(axis=2)) <= 1e-12 * scale[:, :, 0]).all()
+    # constant velocity, linear field
+    a, b_, c, d = 0.7, -1.3, 2.0, 0.5
+    n = len(v)
+    const = np.concatenate([np.full((n, 6), a), np.full((n, 6), b_)], axis=1)
+    C = oracle.local_convection(v, const, 64)
+    xy = v.astype(np.float64).reshape(n, 3, 2)
+    mid = np.stack([(xy[:, 1] + xy[:, 2]) / 2, (xy[:, 0] + xy[:, 2]) / 2, (xy[:, 0] + xy[:, 1]) / 2], axis=1)
+    nodes = np.concatenate([xy, mid], axis=1)                        # element node order v0 v1 v2 m12 m02 m01
+    phi = c * nodes[:, :, 0] + d * nodes[:, :, 1]
+    mass = oracle.local_matrices(v, 64)["mass"]
+    want = (a * c + b_ * d) * mass.sum(axis=2)
+    got = np.einsum("nij,nj->ni", C, phi)
+    assert np.abs(got - want).max() <= 1e-12 * max(1.0, np.abs(want).max())
+
+
+@pytest.mark.skipif(not oracle.ref_assembly_available(), reason="reference element code not compiled here")
+def test_local_convection_matches_reference_element_code_live():
+    g = _assembly_fixture()
+    live = oracle.ref_local_convection(g["vertices"], g["velocities"])
+    assert np.array_equal(live, g["convection"])
+
+
 @pytest.mark.skipif(not oracle.ref_assembly_available(), reason="reference element code not compiled here")
 def test_local_matrices_match_reference_element_code_live():
     g = _assembly_fixture()

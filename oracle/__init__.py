@@ -145,8 +145,21 @@ def ref_lib(int_offsets: bool = False):
         L.ref_tree_destroy.argtypes = [_p]
         L.ref_tree_locate.argtypes = [_p, _i, _fptr, _iptr, _fptr, _fptr, _iptr]
         L.ref_grid_bbox.argtypes = [_p, _fptr]
+        L.ref_expression_eval.restype = _i
+        L.ref_expression_eval.argtypes = [ctypes.c_char_p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                          ctypes.POINTER(ctypes.c_float)]
         _REF[key] = L
     return _REF[key]
+
+
+def ref_evaluate_expression(expr: str, x: float, y: float, t: float = 0.0) -> float:
+    """The reference's own Expression::init + ::evaluate (cpp/expression.cpp), float variables x, y, t as
+    cpp/grid.cpp:80-94 passes them; the float result.  Raises ValueError where the reference reports an error."""
+    out = ctypes.c_float(0.0)
+    st = ref_lib().ref_expression_eval(expr.encode(), x, y, t, ctypes.byref(out))
+    if st != 0:
+        raise ValueError(f"reference rejects {expr!r} ({'init' if st == 1 else 'evaluate'})")
+    return out.value
 
 
 # ---------------------------------------------------------------------------------------------------

@@ -2,7 +2,8 @@
 // A thin C entry layer around the reference's OWN KD tree: cpp/kd_tree_builder.cpp (KDTreeBuilder::build)
 // and gpu_cpu_shared/kd_tree.cuh (KDTree<FemGrid2D>::findElement), compiled unchanged from the reference
 // sources by oracle/Makefile into oracle/_ref/.  It exists to pin the element-lookup oracle and to write
-// golden element-ID fixtures; no product code links it.
+// golden element-ID fixtures; no product code links it.  It also exposes the reference's expression evaluator
+// (cpp/expression.cpp) to pin the restated boundary-condition expression language.
 //
 // FemGrid2D is filled through a derived class (its members are protected, include/grid.h:110-128) in
 // the same order FemGrid2D::loadJSON uses (cpp/grid.cpp:25-36), so BBox2D::expand reproduces the
@@ -10,6 +11,8 @@
 #include "grid.h"
 #include "kd_tree.cuh"
 #include "kd_tree_builder.h"
+#include "expression.h"
+#include "error_code.h"
 
 namespace {
 
@@ -66,6 +69,20 @@ void ref_tree_locate(void* h, int n, const float* pts, int* elem, float* xi, flo
         eta[i] = b;
         nearest[i] = e >= 0 ? -1 : nn;
     }
+}
+
+// The reference's boundary-condition expression (cpp/expression.cpp, Expression::init and ::evaluate), evaluated
+// the way VelocityDirichlet::eval / PressureDirichlet::eval do (cpp/grid.cpp:80-94): float variables in an
+// unordered_map keyed by name.  Returns 0 and the float result, 1 when init rejects the text, 2 when evaluate
+// fails (an unknown variable).
+int ref_expression_eval(const char* text, float x, float y, float t, float* out) {
+    NSFem::Expression e;
+    if (e.init(text).hasError()) return 1;
+    const std::unordered_map<char, float> vars = {{'x', x}, {'y', y}, {'t', t}};
+    float r = 0;
+    if (e.evaluate(&vars, r).hasError()) return 2;
+    *out = r;
+    return 0;
 }
 
 void ref_grid_bbox(void* h, float* out4) {

@@ -271,6 +271,48 @@ def test_time_dependent_expression_programs(expr):
         assert nsf.evaluate_expression(expr, x, y, t) == oracle.evaluate_expression(expr, {"x": x, "y": y, "t": t})
 
 
+def _expression_fixture():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_expressions.json")) as f:
+        return json.load(f)
+
+
+def test_expressions_match_reference_evaluator():
+    """The restated expression language (oracle) and the product's host evaluator, both in double at the points'
+    float coordinates, against the reference's own Expression::evaluate in float (tests/golden/ref_expressions.json,
+    written by make_expression_golden.py from cpp/expression.cpp): within 8 float ulps of the value (the
+    reference rounds every operation to float).  Texts the reference rejects are rejected by both.  Two texts the
+    reference cannot be run on in-process ("(1+2" ends it in an assert, "1+*" does not terminate) are covered by
+    test_expression_errors: both evaluators here return an error for them."""
+    import navier_stokes_fem_gb300 as nsf
+
+    g = _expression_fixture()
+    pts = [tuple(float(np.float32(v)) for v in p) for p in g["points"]]
+    assert len(g["values"]) >= 20
+    for expr, want in g["values"].items():
+        for (x, y, t), w in zip(pts, want):
+            got = oracle.evaluate_expression(expr, {"x": x, "y": y, "t": t})
+            assert abs(got - w) <= 8 * 2.0 ** -24 * abs(w), (expr, x, y, t, got, w)
+            assert nsf.evaluate_expression(expr, x, y, t) == got
+    for bad in g["rejected"]:
+        with pytest.raises(Exception):
+            oracle.evaluate_expression(bad, {"x": 0.0, "y": 0.0, "t": 0.0})
+        with pytest.raises(Exception):
+            nsf.evaluate_expression(bad, 0.0, 0.0, 0.0)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference checkout not compiled here")
+def test_expressions_match_reference_evaluator_live():
+    g = _expression_fixture()
+    for expr, want in g["values"].items():
+        assert [oracle.ref_evaluate_expression(expr, *p) for p in g["points"]] == want, expr
+    for bad, where in g["rejected"].items():
+        with pytest.raises(ValueError, match=f"\\({where}\\)"):
+            oracle.ref_evaluate_expression(bad, *g["points"][0])
+
+
 def test_oracle_time_dependent_stepping_known_answer():
     """A lid written as "1 + 0*t" goes through the oracle's per-step re-evaluation at t = k dt and must give the
     constant lid's fields bit for bit (one thread: the oracle's parallel reductions are not ordered); a lid that

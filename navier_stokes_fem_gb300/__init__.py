@@ -468,8 +468,9 @@ class GPUSimulationDevice:
         return k.value
 
     def precond_inner_form(self, slot) -> str:
-        """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident",
-        "reduced", "reduced_resident" or "none" (no such solve yet)."""
+        """The inner-iteration kernel of the slot's last split mixed PCG solve: "cta256", "cta1024", "resident"
+        (the full iteration), "reduced", "reduced_resident" (the reduced iteration forming u_0), "schur",
+        "schur_resident" (the explicit Schur complement) or "none" (no such solve yet)."""
         k = _i()
         self._check(library().nsf_precond_inner_form(self._h, _slot(slot), ctypes.byref(k)))
         return {-1: "none", 0: "cta256", 1: "cta1024", 2: "resident", 3: "reduced", 4: "reduced_resident",
